@@ -1,0 +1,286 @@
+/*
+ * snisr.h — C ABI of the GB300-native sparse-voxel tile renderer.
+ *
+ * One hot path from Scalable Neural Indoor Scene Rendering, rebuilt for
+ * sm_103a: per ray, a tile-grid DDA and a voxel DDA over per-tile occupancy
+ * bitfields, samples only inside occupied voxels, trilinear per-corner
+ * features into a per-tile MLP, front-to-back compositing with early stop.
+ *
+ * Conventions shared by every entry point
+ *   - Plain C types only; no exceptions cross this boundary.  Every call
+ *     returns an snisr_status; snisr_last_error_string() describes the last
+ *     failure of the calling thread.
+ *   - Pointers named *_dev are device pointers (cudaMalloc / torch), *_host
+ *     are host pointers.  `stream` is a cudaStream_t passed as void*
+ *     (NULL = legacy default stream).  Calls enqueue work and return without
+ *     synchronising unless the comment says otherwise.
+ *   - The caller owns output buffers.  A scene owns its device copy of the
+ *     scene data and a workspace sized at creation: rendering allocates no
+ *     device memory after snisr_scene_create().
+ *   - Index conventions follow the reference: dense grids are x-major,
+ *     idx = (x*NY + y)*NZ + z (rendering/src/include/cuda_utils.h:137-140).
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   FASTRENDERING pybind module   rendering/src/binding.cpp:13-27
+ *   CUDA_EXT pybind module        training/src/binding.cpp:4-12
+ *   render_TileScene (C++ host)   training/src/cuda_func.cu:2395-2480
+ */
+#ifndef SNISR_H_
+#define SNISR_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SNISR_ABI_VERSION 1
+
+typedef enum snisr_status {
+  SNISR_OK = 0,
+  SNISR_INVALID_ARG = 1,     /* bad pointer, size, shape or enum            */
+  SNISR_OOM = 2,             /* device or host allocation failed            */
+  SNISR_CUDA_ERROR = 3,      /* a CUDA runtime call or launch failed        */
+  SNISR_DEVICE_TIMEOUT = 4,  /* a bounded device wait ran out               */
+  SNISR_CORRUPT_SCENE = 5,   /* scene data inconsistent (counts, indices)   */
+  SNISR_OVERFLOW = 6,        /* a workspace bound was exceeded on device    */
+  SNISR_UNSUPPORTED = 7      /* shape/configuration not supported by a form */
+} snisr_status;
+
+typedef enum snisr_dtype { SNISR_F32 = 0, SNISR_F16 = 1 } snisr_dtype;
+
+/* Render forms.  PLAIN_FP32: one thread per ray, FP32 features, weights and
+ * math on CUDA cores.  TC: batched form — traversal emits compacted samples,
+ * grouped by tile, and the per-tile MLP runs as tcgen05 FP16 MMAs with FP32
+ * accumulation in tensor memory. */
+typedef enum snisr_form { SNISR_FORM_PLAIN_FP32 = 0, SNISR_FORM_TC = 1 } snisr_form;
+
+/* ------------------------------------------------------------------------ */
+/* Scene description (host arrays, borrowed for the duration of create).     */
+/* ------------------------------------------------------------------------ */
+typedef struct snisr_scene_desc {
+  int32_t grid[3];            /* tiles along x, y, z                          */
+  float scene_min[3];         /* world position of the grid's min corner      */
+  float tile_size;            /* edge of a cubic tile (world units)           */
+  int32_t res;                /* voxels per tile edge N (multiple of 4)       */
+  int32_t num_tiles;          /* NT: tiles with an id in tile_index           */
+  const int32_t* tile_index;  /* [grid x*y*z] dense tile -> sparse id or -1   */
+  const uint64_t* occupancy;  /* [NT][N^3/64] bit (v&63) of word v>>6,
+                                 v = (x*N + y)*N + z                          */
+  int64_t num_voxels;         /* occupied voxels = total popcount             */
+  const int32_t* voxel_corners; /* [num_voxels][8] vertex ids, voxels in
+                                 (tile, v) order; corner k = dx*4+dy*2+dz     */
+  int64_t num_vertices;       /* NV                                            */
+  int32_t feat_dim;           /* F: 16 or 32                                   */
+  snisr_dtype feat_type;      /* storage type of vertex_feat / vertex_density */
+  const void* vertex_feat;    /* [NV][F]                                       */
+  const void* vertex_density; /* [NV] density logits (softplus applied after
+                                 trilinear interpolation)                     */
+  /* per-tile MLP: in = F + 3 + 6*dir_freqs -> hidden x n_hidden -> 3        */
+  int32_t dir_freqs;          /* view-direction encoding frequencies (4)      */
+  int32_t mlp_hidden;         /* width: 32 or 64                               */
+  int32_t mlp_layers;         /* hidden layers: 2 or 3                          */
+  const float* mlp_params;    /* [NT][P]; per Linear: W[out][in] then b[out]   */
+  /* proxy mesh (optional: num_triangles == 0 -> rays start at the AABB entry) */
+  int64_t num_mesh_vertices;
+  const float* mesh_vertices; /* [num_mesh_vertices][3]                        */
+  int64_t num_triangles;
+  const int32_t* mesh_faces;  /* [num_triangles][3]                            */
+  /* marching parameters */
+  float step_vox;             /* sample spacing in voxel lengths (0.5)        */
+  float early_stop;           /* stop when transmittance < early_stop (1e-3)  */
+  float start_offset_vox;     /* ray start = proxy hit - offset*voxel (2.0)   */
+  /* workspace bound for the TC form: samples per pixel, on average         */
+  int32_t max_samples_per_ray;
+  int32_t max_pixels;         /* largest frame the workspace serves           */
+} snisr_scene_desc;
+
+typedef struct snisr_scene snisr_scene;
+
+typedef struct snisr_scene_info {
+  int64_t num_voxels, num_vertices, num_triangles, bvh_nodes;
+  int32_t num_tiles, res, feat_dim, mlp_in, mlp_hidden, mlp_layers;
+  int32_t params_per_tile;    /* P */
+  int64_t device_bytes;       /* device memory the scene holds              */
+  int64_t sample_capacity;    /* TC-form workspace in samples               */
+} snisr_scene_info;
+
+/* Pinhole camera, reference convention (rendering/src/compute_rays.cu:7-17):
+ * x = (px - cx)*inv_focal, y = (py - cy)*inv_focal, d = R*[x, y, 1],
+ * then normalised.  c2w is row-major 3x4 [R | origin]. */
+typedef struct snisr_camera {
+  int32_t width, height;
+  float cx, cy, inv_focal;
+  float c2w[12];
+} snisr_camera;
+
+/* Number of parameters of one tile's MLP for the given shape. */
+int64_t snisr_mlp_param_count(int32_t feat_dim, int32_t dir_freqs,
+                              int32_t hidden, int32_t layers);
+
+/* Builds device-resident scene state on `device`: occupancy words with rank
+ * prefixes, per-voxel 8-corner feature blocks (FP32 and FP16), per-tile MLP
+ * images, the proxy-mesh BVH and the TC-form workspace.  Synchronous.
+ * Replaces the scene-tensor setup of FRender (rendering/src/__init__.py:98-136). */
+snisr_status snisr_scene_create(const snisr_scene_desc* desc, int32_t device,
+                                snisr_scene** out);
+snisr_status snisr_scene_destroy(snisr_scene* scene);
+snisr_status snisr_scene_get_info(const snisr_scene* scene, snisr_scene_info* info);
+/* Reads (and clears) the device-side error word of the scene: overflow of the
+ * sample workspace or a bounded wait that ran out.  Synchronises `stream`. */
+snisr_status snisr_scene_check(snisr_scene* scene, void* stream);
+/* Replaces the per-tile MLP parameters ([NT][P] FP32, device pointer). */
+snisr_status snisr_scene_set_mlp(snisr_scene* scene, const float* params_dev, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Render: camera + scene -> colour/depth/opacity.                           */
+/* Generalises render_TileScene (training/src/cuda_func.cu:2395-2480) and the */
+/* per-frame op chain of FRender.render (rendering/src/__init__.py:246-341).  */
+/* ------------------------------------------------------------------------ */
+/* rgb_dev [H*W*3], depth_dev [H*W], opacity_dev [H*W] FP32 device buffers.
+ * depth = sum_i w_i t_i (ray distance), opacity = 1 - final transmittance. */
+snisr_status snisr_render(snisr_scene* scene, const snisr_camera* cam, int32_t form,
+                          float* rgb_dev, float* depth_dev, float* opacity_dev,
+                          void* stream);
+/* Same, with host output buffers (pinned for best speed): device->host copies
+ * are enqueued on `stream` and the call synchronises it before returning. */
+snisr_status snisr_render_host(snisr_scene* scene, const snisr_camera* cam, int32_t form,
+                               float* rgb_host, float* depth_host, float* opacity_host,
+                               void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Per-stage entry points (parity harnesses and drop-in ops).               */
+/* ------------------------------------------------------------------------ */
+/* Normalised pinhole ray directions for a camera: dirs_dev [H*W*3]. */
+snisr_status snisr_camera_rays(const snisr_camera* cam, float* dirs_dev, void* stream);
+
+/* Proxy-mesh nearest hit through the BVH, FP32 Moller-Trumbore with an FP64
+ * re-test in the near-degenerate band.  Replaces ray_firstHit_inTile_kernel
+ * (training/src/cuda_func.cu:130-282).  t_dev [n] (-1 on miss), tri_dev [n]. */
+snisr_status snisr_proxy_hit(snisr_scene* scene, const float* origins_dev,
+                             const float* dirs_dev, int64_t n, float* t_dev,
+                             int32_t* tri_dev, void* stream);
+
+/* Occupied-voxel sequence of each ray (global voxel ids, in visit order,
+ * -1 padded to K), ignoring transmittance; the start point honours the proxy
+ * mesh when the scene has one.  count_dev [n] = number visited (may exceed K). */
+snisr_status snisr_trace_voxels(snisr_scene* scene, const float* origins_dev,
+                                const float* dirs_dev, int64_t n, int32_t K,
+                                int32_t* visited_dev, int32_t* count_dev, void* stream);
+
+/* Render arbitrary rays (rgb [n*3], depth [n], opacity [n]). */
+snisr_status snisr_render_rays(snisr_scene* scene, const float* origins_dev,
+                               const float* dirs_dev, int64_t n, int32_t form,
+                               float* rgb_dev, float* depth_dev, float* opacity_dev,
+                               void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Training: forward / hand-written adjoint (per-ray recomputation).         */
+/* Replaces the autograd graph sparse_sampling + compute_voxels + query_voxel */
+/* + volume_rendering (training/scripts/tile/tile.py:667-704,                */
+/* training/scripts/utils.py:823-837).  Parameters are passed explicitly so  */
+/* that an optimiser outside the library owns them.                          */
+/* ------------------------------------------------------------------------ */
+/* vfeat_dev [NV][F] FP32, vdens_dev [NV] FP32, mlp_dev [NT][P] FP32.
+ * rgb_dev [n*3] out.  Rays must be normalised.  form: PLAIN_FP32 or TC
+ * (TC = BF16 compute copies with FP32 accumulation). */
+snisr_status snisr_train_forward(snisr_scene* scene, const float* vfeat_dev,
+                                 const float* vdens_dev, const float* mlp_dev,
+                                 const float* origins_dev, const float* dirs_dev,
+                                 int64_t n, int32_t form, float* rgb_dev, void* stream);
+/* grad_rgb_dev [n*3] = dL/drgb, rgb_dev = the forward output.  Gradients are
+ * ACCUMULATED (+=) into gvfeat_dev [NV][F], gvdens_dev [NV], gmlp_dev [NT][P]. */
+snisr_status snisr_train_backward(snisr_scene* scene, const float* vfeat_dev,
+                                  const float* vdens_dev, const float* mlp_dev,
+                                  const float* origins_dev, const float* dirs_dev,
+                                  int64_t n, int32_t form, const float* rgb_dev,
+                                  const float* grad_rgb_dev, float* gvfeat_dev,
+                                  float* gvdens_dev, float* gmlp_dev, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Reference-op drop-ins (argument meaning as in the reference; device ptrs) */
+/* ------------------------------------------------------------------------ */
+/* FASTRENDERING.compute_rays (rendering/src/compute_rays.cu:46-68):
+ * intrinsic = [cx, cy, 1/f], c2w_rotation row-major 3x3, both device arrays;
+ * rays_d [H][W][3] unnormalised. */
+snisr_status snisr_op_compute_rays(const float* intrinsic_dev, const float* c2w_rot_dev,
+                                   int32_t H, int32_t W, float* rays_d_dev, void* stream);
+/* FASTRENDERING.tracing_tiles (rendering/src/raytile_tracing.cu:63-95):
+ * origin[3], tile_shape[3] (int), scene_min_corner[3], scene_size[3] device
+ * arrays; visited_dev [npix][K], -1 padded. */
+snisr_status snisr_op_tracing_tiles(const float* rays_d_dev, int64_t npix,
+                                    const int32_t* index_map_dev, const float* origin_dev,
+                                    const int32_t* tile_shape_dev,
+                                    const float* scene_min_dev, const float* scene_size_dev,
+                                    float tile_size, int32_t K, int32_t* visited_dev,
+                                    void* stream);
+/* CUDA_EXT.Sample_sparse (training/src/Sample_kernel.cu:397-434): node_flags
+ * [N][N][N] int16 (x-major, 1 = occupied), z_vals/dists [B][Nsamples], caller
+ * pre-fills -1 as utils.sparse_sampling does (training/scripts/utils.py:797-805). */
+snisr_status snisr_op_sample_sparse(const float* rays_o_dev, const float* rays_d_dev,
+                                    int64_t B, const int16_t* node_flags_dev,
+                                    float cx, float cy, float cz, float tile_size,
+                                    int32_t num_voxel, int32_t nsamples,
+                                    float* z_vals_dev, float* dists_dev, void* stream);
+/* FASTRENDERING.inverse_z_sampling (rendering/src/sampling.cu:48-81):
+ * origin[3], inverse_near [npix], inverse_bound [npix] (all device);
+ * sample j of the call sits at z = 1/((offset+j)*inverse_bound + inverse_near);
+ * points [npix][spr][3], steps [npix][spr] = max(z_{j+1} - z_j, 0). */
+snisr_status snisr_op_inverse_z_sampling(const float* rays_d_dev, const float* origin_dev,
+                                         const float* inverse_near_dev,
+                                         const float* inverse_bound_dev, int64_t npix,
+                                         int32_t offset, int32_t spr, float* points_dev,
+                                         float* steps_dev, void* stream);
+/* FASTRENDERING.integrate_points (rendering/src/volume_rendering.cu:60-87):
+ * rgba [npix][16][4] (colour, sigma), z_dists [npix][16], frame [npix][3] and
+ * transparency [npix] carried across calls. */
+snisr_status snisr_op_integrate_points(const float* rgba_dev, const float* z_dists_dev,
+                                       int64_t npix, float early_stop, float* frame_dev,
+                                       float* transparency_dev, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Seeded synthetic scenes (input generation for tests and benchmarks).      */
+/* ------------------------------------------------------------------------ */
+typedef struct snisr_synth_params {
+  int32_t kind;        /* 0 small room (1 tile), 1 room, 2 multi-room        */
+  int32_t grid[3];
+  float tile_size;
+  int32_t res;
+  int32_t feat_dim;
+  snisr_dtype feat_type;
+  int32_t mlp_hidden, mlp_layers, dir_freqs;
+  int32_t num_boxes;
+  float box_min, box_max;   /* box side range (world units)                */
+  int32_t with_mesh;        /* build the proxy mesh                         */
+  float mesh_cell;          /* target triangle-grid cell (world units)      */
+  float density_mean, density_std, feat_std;
+  uint64_t seed;            /* scene seed; tile weights use seed ^ tile     */
+  int32_t round_weights_f16;/* store MLP weights rounded to FP16 values     */
+} snisr_synth_params;
+
+typedef struct snisr_synth_scene snisr_synth_scene;
+/* Generates a scene; `desc` is filled with pointers owned by *out. */
+snisr_status snisr_synth_create(const snisr_synth_params* p, snisr_synth_scene** out,
+                                snisr_scene_desc* desc);
+snisr_status snisr_synth_destroy(snisr_synth_scene* s);
+/* Seeded interior camera pose (origin inside free space, random heading). */
+snisr_status snisr_synth_camera(const snisr_synth_scene* s, uint64_t pose_seed,
+                                int32_t width, int32_t height, float fov_x_deg,
+                                snisr_camera* cam);
+
+/* Diagnostics: one 128 x N x 64 tcgen05 MMA (N = 32 or 64) through the
+ * descriptors of the tensor-core MLP.  A [128][64], B [N][64] row-major FP16
+ * (bf16 = 0) or BF16 (bf16 = 1) bit patterns, D [128][N] FP32 = A * B^T.
+ * Synchronises `stream`. */
+snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev,
+                            int32_t N, int32_t bf16, void* stream);
+
+const char* snisr_last_error_string(void);
+const char* snisr_version(void);
+int32_t snisr_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SNISR_H_ */

@@ -1,0 +1,176 @@
+"""ORACLE — test infrastructure only (CPU restatement of the reference path).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
+the checker; the product library never loads it.  See oracle.cpp for the
+reference file:line each function follows.
+
+Parity pinning: the reference has no tests or golden vectors for this path.
+The restatement is pinned (a) against the reference's own header functions
+compiled for the host from the reference tree by oracle/build_ref.py (only
+where the reference tree is present), and (b) against golden vectors made by
+running the reference's Python code (training/scripts/utils.py volume_rendering,
+tile.py query_voxel, networks.py PE/MLP) with tests/golden/make_golden.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.cpp")
+    hdr = os.path.join(ROOT, "include", "snisr.h")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    # -ffp-contract=off: every binary32 operation rounds separately (the
+    # specification of the traversal arithmetic) on x86-64 and AArch64 alike.
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-I", os.path.join(ROOT, "include"), src, "-o", LIB + ".tmp", "-lpthread"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+P = C.c_void_p
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        sig = {
+            "oracle_scene_create": (P, [P]),
+            "oracle_scene_destroy": (None, [P]),
+            "oracle_camera_dirs": (None, [P, P]),
+            "oracle_proxy": (None, [P, P, P, C.c_int64, P, P, P, C.c_int]),
+            "oracle_trace": (None, [P, P, P, P, C.c_int64, C.c_int, P, P, C.c_int]),
+            "oracle_render": (None, [P, P, P, P, C.c_int64, C.c_int, P, P, P, P, C.c_int]),
+            "oracle_op_compute_rays": (None, [P, P, C.c_int, C.c_int, P]),
+            "oracle_op_tracing_tiles": (None, [P, C.c_int64, P, P, P, P, P, C.c_float, C.c_int, P]),
+            "oracle_op_sample_sparse": (None, [P, P, C.c_int64, P, C.c_float, C.c_float, C.c_float, C.c_float,
+                                               C.c_int, C.c_int, P, P]),
+            "oracle_op_inverse_z": (None, [P, P, P, P, C.c_int64, C.c_int, C.c_int, P, P]),
+            "oracle_op_integrate": (None, [P, P, C.c_int64, C.c_float, P, P]),
+            "oracle_ray_aabb": (None, [P, P, P, C.c_float, P]),
+            "oracle_voxel_traversal": (C.c_int, [P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float]),
+            "oracle_ray_triangle_onesided": (C.c_float, [P, P, P, P, P]),
+            "oracle_trilinear_base": (None, [P, C.c_int, C.c_int, C.c_int, P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+class OracleScene:
+    """Oracle view of a scene description (borrows the desc's host arrays)."""
+
+    def __init__(self, desc):
+        self.desc = desc
+        self._h = lib().oracle_scene_create(C.byref(desc))
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().oracle_scene_destroy(self._h)
+        except Exception:
+            pass
+
+    def proxy(self, o: np.ndarray, d: np.ndarray, nthreads: int | None = None):
+        n = o.shape[0]
+        ts = np.zeros(n, np.float32)
+        th = np.zeros(n, np.float32)
+        tri = np.zeros(n, np.int32)
+        lib().oracle_proxy(self._h, _p(o), _p(d), n, _p(ts), _p(th), _p(tri), nthreads or threads())
+        return ts, th, tri
+
+    def trace(self, o, d, t_start, K: int, nthreads: int | None = None):
+        n = o.shape[0]
+        vis = np.zeros((n, K), np.int32)
+        cnt = np.zeros(n, np.int32)
+        lib().oracle_trace(self._h, _p(o), _p(d), _p(t_start), n, K, _p(vis), _p(cnt), nthreads or threads())
+        return vis, cnt
+
+    def render(self, o, d, t_start, form: int, nthreads: int | None = None):
+        """form: 0 plain FP32, 1 FP64, 2 tensor-core emulation (FP16 MLP inputs, FP64 math)."""
+        n = o.shape[0]
+        rgb = np.zeros((n, 3), np.float32)
+        depth = np.zeros(n, np.float32)
+        opac = np.zeros(n, np.float32)
+        stats = np.zeros(2, np.int64)
+        lib().oracle_render(self._h, _p(o), _p(d), _p(t_start), n, form, _p(rgb), _p(depth), _p(opac), _p(stats),
+                            nthreads or threads())
+        return rgb, depth, opac, stats
+
+
+def camera_dirs(cam) -> np.ndarray:
+    out = np.zeros((cam.height * cam.width, 3), np.float32)
+    lib().oracle_camera_dirs(C.byref(cam), _p(out))
+    return out
+
+
+def camera_origins(cam, n: int) -> np.ndarray:
+    o = np.array([cam.c2w[3], cam.c2w[7], cam.c2w[11]], np.float32)
+    return np.ascontiguousarray(np.broadcast_to(o, (n, 3)))
+
+
+def op_compute_rays(intr, rot, H, W):
+    out = np.zeros((H, W, 3), np.float32)
+    lib().oracle_op_compute_rays(_p(intr), _p(rot), H, W, _p(out))
+    return out
+
+
+def op_tracing_tiles(rays_d, imap, origin, shape, smin, ssize, tile, K):
+    n = rays_d.shape[0]
+    out = np.zeros((n, K), np.int32)
+    lib().oracle_op_tracing_tiles(_p(rays_d), n, _p(imap), _p(origin), _p(shape), _p(smin), _p(ssize), tile, K,
+                                  _p(out))
+    return out
+
+
+def op_sample_sparse(ro, rd, flags, center, tile, N, ns):
+    B = ro.shape[0]
+    z = np.full((B, ns), -1, np.float32)
+    d = np.full((B, ns), -1, np.float32)
+    lib().oracle_op_sample_sparse(_p(ro), _p(rd), B, _p(flags), center[0], center[1], center[2], tile, N, ns, _p(z),
+                                  _p(d))
+    return z, d
+
+
+def op_inverse_z(rays_d, origin, inv_near, inv_bound, offset, spr):
+    n = rays_d.shape[0]
+    pts = np.zeros((n, spr, 3), np.float32)
+    steps = np.zeros((n, spr), np.float32)
+    lib().oracle_op_inverse_z(_p(rays_d), _p(origin), _p(inv_near), _p(inv_bound), n, offset, spr, _p(pts),
+                              _p(steps))
+    return pts, steps
+
+
+def op_integrate(rgba, dz, early, frame, trans):
+    n = frame.shape[0]
+    lib().oracle_op_integrate(_p(rgba), _p(dz), n, early, _p(frame), _p(trans))
+    return frame, trans

@@ -1,0 +1,800 @@
+// ORACLE — test infrastructure only.  Scalar CPU restatement of the
+// reference's algorithm for the tiled sparse-voxel hot path, used by tests/,
+// __graft_entry__.smoke() and bench.py's CPU baseline as the checker.  It is
+// never linked into, loaded by or called from the product library.
+//
+// Independent of the GPU code: written from the algorithm, not from the
+// kernels.  Traversal is evaluated in IEEE binary32 with every operation
+// rounded separately (compile with -ffp-contract=off), which is the
+// specification of the visited-voxel sequence; shading (trilinear, MLP,
+// compositing) runs in float (mode 0) or double (mode 1, the FP64 oracle).
+//
+// Reference functions restated (paths inside the reference project):
+//   safe_divide / signf            rendering/src/include/cutil_math.h:856-876
+//   RayAABBIntersection            rendering/src/include/cuda_utils.h:506-598
+//   voxel_traversal (tie rules)    rendering/src/include/cuda_utils.h:158-238
+//   RayTriangleIntersection        rendering/src/include/cuda_utils.h:403-436
+//   tracing_tiles_kernel           rendering/src/raytile_tracing.cu:9-60
+//   per-tile clip + march          rendering/src/raydiffuse_render_octree_fp16.cu:20-139,199-225
+//   voxel DDA of Sample_sparse     training/src/Sample_kernel.cu:181-394
+//   compute_rays / get_direction   rendering/src/compute_rays.cu:7-44
+//   inverse_z_sampling_kernel      rendering/src/sampling.cu:5-45
+//   integrate_points_kernel        rendering/src/volume_rendering.cu:5-58
+//   volume_rendering (cumprod)     training/scripts/utils.py:823-837
+//   Positional_Encoding / MLP      training/scripts/networks.py:4-41
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "snisr.h"
+
+namespace {
+
+const float kInf = 100000000.0f;
+
+float f16_to_f32(uint16_t h) {
+  uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+  uint32_t exp = (h >> 10) & 0x1F, mant = h & 0x3FFu, x;
+  if (exp == 0) {
+    if (mant == 0) x = sign;
+    else {
+      int e = -1;
+      do { mant <<= 1; ++e; } while (!(mant & 0x400u));
+      x = sign | ((uint32_t)(127 - 15 - e) << 23) | ((mant & 0x3FFu) << 13);
+    }
+  } else if (exp == 31) x = sign | 0x7F800000u | (mant << 13);
+  else x = sign | ((exp - 15 + 127) << 23) | (mant << 13);
+  float f;
+  std::memcpy(&f, &x, 4);
+  return f;
+}
+
+// round to nearest-even FP16, returned as float
+float round_f16(float f) {
+  uint32_t x;
+  std::memcpy(&x, &f, 4);
+  uint32_t sign = (x >> 16) & 0x8000u;
+  int32_t exp = (int32_t)((x >> 23) & 0xFF) - 127 + 15;
+  uint32_t mant = x & 0x7FFFFFu;
+  uint16_t h;
+  if (((x >> 23) & 0xFF) == 0xFF) h = (uint16_t)(sign | 0x7C00u | (mant ? 0x200u : 0u));
+  else if (exp >= 31) h = (uint16_t)(sign | 0x7C00u);
+  else if (exp <= 0) {
+    if (exp < -10) h = (uint16_t)sign;
+    else {
+      mant |= 0x800000u;
+      int shift = 14 - exp;
+      uint32_t half = mant >> shift, rem = mant & ((1u << shift) - 1u), mid = 1u << (shift - 1);
+      if (rem > mid || (rem == mid && (half & 1u))) ++half;
+      h = (uint16_t)(sign | half);
+    }
+  } else {
+    uint32_t half = sign | ((uint32_t)exp << 10) | (mant >> 13), rem = mant & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (half & 1u))) ++half;
+    h = (uint16_t)half;
+  }
+  return f16_to_f32(h);
+}
+
+// reference safe_divide (cutil_math.h:867-869)
+inline float safe_divide(float a, float b) { return b != 0.0f ? a / b : kInf; }
+
+struct Bound { float lo, hi; };
+
+// reference RayAABBIntersection (cuda_utils.h:553-598), per-axis half size
+Bound ray_aabb(const float o[3], const float d[3], const float c[3], const float h[3]) {
+  float f_low = 0.0f, f_high = 100000.0f;
+  for (int a = 0; a < 3; ++a) {
+    float inv = safe_divide(1.0f, d[a]);
+    float lo = ((c[a] - h[a]) - o[a]) * inv;
+    float hi = ((c[a] + h[a]) - o[a]) * inv;
+    if (hi < lo) std::swap(lo, hi);
+    if (hi < f_low) return {-1.0f, -1.0f};
+    if (lo > f_high) return {-1.0f, -1.0f};
+    f_low = (lo > f_low) ? lo : f_low;
+    f_high = (hi < f_high) ? hi : f_high;
+    if (f_low > f_high) return {-1.0f, -1.0f};
+  }
+  return {f_low, f_high};
+}
+
+// Amanatides-Woo axis choice with the reference tie rule (cuda_utils.h:195-216)
+inline int dda_axis(const float m[3]) {
+  if (m[0] < m[1]) return (m[0] < m[2]) ? 0 : 2;
+  return (m[1] < m[2]) ? 1 : 2;
+}
+
+struct Scene {
+  const snisr_scene_desc* d;
+  int N, NT, F, H, L, in, P;
+  int64_t words;
+  float tile, voxel, inv_voxel, step_len, early, start_off;
+  std::vector<float> centers;      // [NT][3]
+  std::vector<uint32_t> base;      // [NT*words] first global voxel of a word
+  std::vector<float> vfeat, vdens; // vertex data as float
+};
+
+bool occupied(const Scene& s, int tile, int vid, uint32_t& rec) {
+  int64_t w = (int64_t)tile * s.words + (vid >> 6);
+  uint64_t bits = s.d->occupancy[w];
+  int b = vid & 63;
+  if (!((bits >> b) & 1ull)) return false;
+  rec = s.base[(size_t)w] + (uint32_t)__builtin_popcountll(bits & ((1ull << b) - 1ull));
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Per-ray traversal: callback on every occupied voxel segment, in order.
+// visit(tile, rec, vc[3], near, far, t_in, q[3]) returns false to stop.
+// ---------------------------------------------------------------------------
+template <class Visit>
+void march(const Scene& s, const float o[3], const float d[3], float t_start, Visit&& visit) {
+  const snisr_scene_desc* D = s.d;
+  const int g[3] = {D->grid[0], D->grid[1], D->grid[2]};
+  float size[3], half[3], cen[3];
+  for (int a = 0; a < 3; ++a) {
+    size[a] = (float)g[a] * s.tile;
+    half[a] = size[a] * 0.5f;
+    cen[a] = D->scene_min[a] + half[a];
+  }
+  Bound b = ray_aabb(o, d, cen, half);
+  if (b.lo == -1.0f) return;
+  float t0 = std::max(b.lo, t_start);
+  if (!(t0 < b.hi)) return;
+  int tc[3], ts[3];
+  float tmax[3], tdel[3];
+  for (int a = 0; a < 3; ++a) {
+    float p = (o[a] + t0 * d[a]) - D->scene_min[a];
+    p = std::min(std::max(p, 0.0f), size[a] - 0.000001f);
+    int c = (int)std::floor(p / s.tile);
+    tc[a] = std::min(std::max(c, 0), g[a] - 1);
+    ts[a] = d[a] >= 0.0f ? 1 : -1;
+    float nb = (float)(tc[a] + ts[a]) * s.tile;
+    if (ts[a] < 0) nb = nb + s.tile;
+    tmax[a] = d[a] != 0.0f ? (nb - p) / d[a] : kInf;
+    tdel[a] = d[a] != 0.0f ? (s.tile / d[a]) * (float)ts[a] : kInf;
+  }
+  const int N = s.N;
+  for (;;) {
+    int id = D->tile_index[((int64_t)tc[0] * g[1] + tc[1]) * g[2] + tc[2]];
+    if (id >= 0) {
+      float c[3], h[3];
+      for (int a = 0; a < 3; ++a) { c[a] = s.centers[(size_t)id * 3 + a]; h[a] = s.tile * 0.5f; }
+      Bound tb = ray_aabb(o, d, c, h);
+      float ti = std::max(tb.lo, t_start);
+      if (tb.lo != -1.0f && ti < tb.hi) {
+        float q[3], vmax[3], vdel[3];
+        int vc[3], vs[3];
+        for (int a = 0; a < 3; ++a) {
+          float corner = c[a] - h[a];
+          q[a] = (o[a] + ti * d[a]) - corner;
+          q[a] = std::min(std::max(q[a], 0.0f), s.tile - 0.00001f);
+          int v = (int)(q[a] / s.voxel);
+          vc[a] = std::min(std::max(v, 0), N - 1);
+          vs[a] = d[a] >= 0.0f ? 1 : -1;
+          float nb = (float)(vc[a] + vs[a]) * s.voxel;
+          if (vs[a] < 0) nb = nb + s.voxel;
+          vmax[a] = safe_divide(nb - q[a], d[a]);
+          vdel[a] = safe_divide((float)vs[a] * s.voxel, d[a]);
+        }
+        float near_ = 0.0f;
+        for (;;) {
+          float far_ = std::min(std::min(vmax[0], vmax[1]), vmax[2]);
+          int vid = (vc[0] * N + vc[1]) * N + vc[2];
+          uint32_t rec;
+          if (occupied(s, id, vid, rec))
+            if (!visit(id, rec, vc, near_, far_, ti, q)) return;
+          int a = dda_axis(vmax);
+          vc[a] += vs[a];
+          vmax[a] = vmax[a] + vdel[a];
+          near_ = far_;
+          if (vc[a] < 0 || vc[a] >= N) break;
+        }
+      }
+    }
+    int a = dda_axis(tmax);
+    tc[a] += ts[a];
+    tmax[a] = tmax[a] + tdel[a];
+    if (tc[a] < 0 || tc[a] >= g[a]) return;
+  }
+}
+
+template <class T>
+T softplus(T x) { return std::max(x, T(0)) + std::log1p(std::exp(-std::fabs(x))); }
+template <class T>
+T sigmoid(T x) { return T(1) / (T(1) + std::exp(-x)); }
+
+// view encoding [d, sin(2^i d), cos(2^i d)] (networks.py:4-15)
+template <class T>
+void dir_enc(const float d[3], T* out) {
+  for (int a = 0; a < 3; ++a) out[a] = (T)d[a];
+  T scale = 1;
+  for (int i = 0; i < 4; ++i) {
+    for (int a = 0; a < 3; ++a) {
+      out[3 + 6 * i + a] = std::sin(scale * (T)d[a]);
+      out[3 + 6 * i + 3 + a] = std::cos(scale * (T)d[a]);
+    }
+    scale *= 2;
+  }
+}
+
+// MLP of one tile: Linear -> ReLU (L times) -> Linear; layout per Linear
+// W[out][in] then b[out].  `half_inputs`: round every Linear input to FP16
+// (tensor-core form) for the hidden layers.
+template <class T>
+void mlp(const Scene& s, int tile, const T* x, T out[3], bool half_inputs = false) {
+  const float* p = s.d->mlp_params + (int64_t)tile * s.P;
+  std::vector<T> cur(x, x + s.in), nxt;
+  int64_t off = 0;
+  for (int l = 0; l <= s.L; ++l) {
+    int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
+    nxt.assign((size_t)fo, T(0));
+    for (int o = 0; o < fo; ++o) {
+      T acc = 0;
+      for (int i = 0; i < fi; ++i) {
+        T w = (T)p[off + (int64_t)o * fi + i];
+        T xi = cur[(size_t)i];
+        if (half_inputs && l < s.L) { w = (T)round_f16((float)w); xi = (T)round_f16((float)xi); }
+        acc += w * xi;
+      }
+      nxt[(size_t)o] = acc + (T)p[off + (int64_t)fi * fo + o];
+    }
+    off += (int64_t)fi * fo + fo;
+    if (l < s.L)
+      for (auto& v : nxt) v = std::max(v, T(0));
+    cur.swap(nxt);
+  }
+  for (int c = 0; c < 3; ++c) out[c] = cur[(size_t)c];
+}
+
+struct SampleGeom {
+  float f[3];
+  float interval;
+  float t;
+};
+
+// Fixed-step samples inside one occupied voxel segment
+// (block_traversal_rendering's march, raydiffuse_render_octree_fp16.cu:67-106).
+template <class Emit>
+bool voxel_samples(const Scene& s, const int vc[3], float near_, float far_, float t_in, const float q[3], const float d[3],
+                   Emit&& emit) {
+  for (float z = near_; z < far_; z = z + s.step_len) {
+    SampleGeom g;
+    for (int a = 0; a < 3; ++a) {
+      float pos = q[a] + z * d[a];
+      float f = pos * s.inv_voxel - (float)vc[a];
+      g.f[a] = std::min(std::max(f, 0.0f), 1.0f);
+    }
+    g.interval = std::min(s.step_len, far_ - z);
+    g.t = t_in + z;
+    if (!emit(g)) return false;
+  }
+  return true;
+}
+
+template <class T>
+void trilinear_w(const float f[3], T w[8]) {
+  T wx[2] = {T(1) - (T)f[0], (T)f[0]}, wy[2] = {T(1) - (T)f[1], (T)f[1]}, wz[2] = {T(1) - (T)f[2], (T)f[2]};
+  for (int k = 0; k < 8; ++k) w[k] = wx[(k >> 2) & 1] * wy[(k >> 1) & 1] * wz[k & 1];
+}
+
+struct RayStats {
+  int64_t samples = 0;
+  int64_t voxels = 0;
+};
+
+// form: 0 plain FP32 semantics, 1 FP64, 2 tensor-core emulation (FP16-rounded
+// MLP inputs, FP64 arithmetic)
+template <class T>
+void render_ray(const Scene& s, const float o[3], const float d[3], float t_start, int form, float rgb[3], float& depth,
+                float& opac, RayStats& st) {
+  T C[3] = {0, 0, 0}, Dp = 0, Tr = 1;
+  std::vector<T> x((size_t)s.in, T(0));
+  dir_enc<T>(d, x.data() + s.F);
+  if (form == 2)
+    for (int i = s.F; i < s.in; ++i) x[(size_t)i] = (T)round_f16((float)x[(size_t)i]);
+  bool stop = false;
+  march(s, o, d, t_start, [&](int tile, uint32_t rec, const int* vc, float nr, float fr, float ti, const float* q) {
+    st.voxels++;
+    return voxel_samples(s, vc, nr, fr, ti, q, d, [&](const SampleGeom& g) {
+      T w[8];
+      trilinear_w<T>(g.f, w);
+      const int32_t* cn = s.d->voxel_corners + (int64_t)rec * 8;
+      T logit = 0;
+      for (int k = 0; k < 8; ++k) logit += w[k] * (T)s.vdens[(size_t)cn[k]];
+      T sigma = softplus<T>(logit);
+      T alpha = T(1) - std::exp(-sigma * (T)(g.interval * s.inv_voxel));
+      T wt = Tr * alpha;
+      for (int c = 0; c < s.F; ++c) {
+        T acc = 0;
+        for (int k = 0; k < 8; ++k) acc += w[k] * (T)s.vfeat[(size_t)cn[k] * s.F + c];
+        x[(size_t)c] = form == 2 ? (T)round_f16((float)acc) : acc;
+      }
+      T out[3];
+      mlp<T>(s, tile, x.data(), out, form == 2);
+      for (int c = 0; c < 3; ++c) C[c] += wt * sigmoid<T>(out[c]);
+      Dp += wt * (T)g.t;
+      Tr *= (T(1) - alpha);
+      st.samples++;
+      if (Tr < (T)s.early) { stop = true; return false; }
+      return true;
+    });
+  });
+  (void)stop;
+  for (int c = 0; c < 3; ++c) rgb[c] = (float)C[c];
+  depth = (float)Dp;
+  opac = (float)(T(1) - Tr);
+}
+
+// ---------------------------------------------------------------------------
+// Proxy mesh: brute-force nearest hit, FP32 Moller-Trumbore two-sided with the
+// FP64 re-test band (ties -> lower triangle id).
+// ---------------------------------------------------------------------------
+const float kDetBand = 1e-7f, kBaryBand = 1e-5f;
+
+inline float dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+inline void cross3(const float a[3], const float b[3], float c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+inline double ddot3(const double a[3], const double b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+inline void dcross3(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+bool tri_hit(const float o[3], const float d[3], const float* A, const float* B, const float* C, float& th) {
+  float e1[3], e2[3], s[3], p[3], q[3];
+  for (int a = 0; a < 3; ++a) { e1[a] = B[a] - A[a]; e2[a] = C[a] - A[a]; s[a] = o[a] - A[a]; }
+  cross3(d, e2, p);
+  float det = dot3(e1, p);
+  cross3(s, e1, q);
+  float un = dot3(s, p), vn = dot3(d, q), tn = dot3(e2, q);
+  bool band = !(std::fabs(det) >= kDetBand);
+  float u = 0, v = 0, t = 0, uv = 0;
+  if (!band) {
+    float inv = 1.0f / det;
+    u = un * inv; v = vn * inv; t = tn * inv;
+    uv = u + v;
+    band = std::fabs(u) < kBaryBand || std::fabs(v) < kBaryBand || std::fabs(uv - 1.0f) < kBaryBand;
+  }
+  if (!band) {
+    if (u >= 0.0f && v >= 0.0f && uv <= 1.0f && t > 0.0f) { th = t; return true; }
+    return false;
+  }
+  double de1[3], de2[3], ds[3], dd[3], dp[3], dq[3];
+  for (int a = 0; a < 3; ++a) {
+    de1[a] = (double)B[a] - (double)A[a];
+    de2[a] = (double)C[a] - (double)A[a];
+    ds[a] = (double)o[a] - (double)A[a];
+    dd[a] = d[a];
+  }
+  dcross3(dd, de2, dp);
+  double ddet = ddot3(de1, dp);
+  if (ddet == 0.0) return false;
+  dcross3(ds, de1, dq);
+  double du = ddot3(ds, dp) / ddet, dv = ddot3(dd, dq) / ddet, dt = ddot3(de2, dq) / ddet;
+  if (du >= 0.0 && dv >= 0.0 && du + dv <= 1.0 && dt > 0.0) {
+    th = (float)dt;
+    return th > 0.0f;
+  }
+  return false;
+}
+
+float nearest_hit(const snisr_scene_desc* D, const float o[3], const float d[3], int& tri) {
+  float best = 3.0e38f;
+  int bid = -1;
+  for (int64_t t = 0; t < D->num_triangles; ++t) {
+    const float* A = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t];
+    const float* B = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 1];
+    const float* C = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 2];
+    float th;
+    if (tri_hit(o, d, A, B, C, th) && (th < best || (th == best && t < bid))) { best = th; bid = (int)t; }
+  }
+  tri = bid;
+  return bid >= 0 ? best : -1.0f;
+}
+
+template <class F>
+void parallel_for(int64_t n, int threads, F&& fn) {
+  if (threads <= 1 || n < 64) {
+    for (int64_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<int64_t> next(0);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t)
+    pool.emplace_back([&]() {
+      for (;;) {
+        int64_t i0 = next.fetch_add(64);
+        if (i0 >= n) break;
+        for (int64_t i = i0; i < std::min(n, i0 + 64); ++i) fn(i);
+      }
+    });
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+struct oracle_scene;
+
+oracle_scene* oracle_scene_create(const snisr_scene_desc* d) {
+  Scene* s = new Scene();
+  s->d = d;
+  s->N = d->res;
+  s->NT = d->num_tiles;
+  s->F = d->feat_dim;
+  s->H = d->mlp_hidden;
+  s->L = d->mlp_layers;
+  s->in = s->F + 3 + 6 * d->dir_freqs;
+  s->P = 0;
+  for (int l = 0; l <= s->L; ++l) {
+    int fi = l == 0 ? s->in : s->H, fo = l == s->L ? 3 : s->H;
+    s->P += fi * fo + fo;
+  }
+  s->words = (int64_t)s->N * s->N * s->N / 64;
+  s->tile = d->tile_size;
+  s->voxel = d->tile_size / (float)s->N;
+  s->inv_voxel = (float)s->N / d->tile_size;
+  s->step_len = d->step_vox * s->voxel;
+  s->early = d->early_stop;
+  s->start_off = d->start_offset_vox * s->voxel;
+  s->centers.assign((size_t)s->NT * 3, 0.0f);
+  for (int x = 0; x < d->grid[0]; ++x)
+    for (int y = 0; y < d->grid[1]; ++y)
+      for (int z = 0; z < d->grid[2]; ++z) {
+        int id = d->tile_index[((int64_t)x * d->grid[1] + y) * d->grid[2] + z];
+        if (id < 0) continue;
+        const int tc[3] = {x, y, z};
+        for (int a = 0; a < 3; ++a) s->centers[(size_t)id * 3 + a] = d->scene_min[a] + ((float)tc[a] + 0.5f) * d->tile_size;
+      }
+  s->base.assign((size_t)(s->NT * s->words), 0u);
+  uint64_t acc = 0;
+  for (int64_t w = 0; w < (int64_t)s->NT * s->words; ++w) {
+    s->base[(size_t)w] = (uint32_t)acc;
+    acc += (uint64_t)__builtin_popcountll(d->occupancy[w]);
+  }
+  const int64_t nv = d->num_vertices;
+  s->vfeat.resize((size_t)(nv * s->F));
+  s->vdens.resize((size_t)nv);
+  for (int64_t i = 0; i < nv * s->F; ++i)
+    s->vfeat[(size_t)i] = d->feat_type == SNISR_F16 ? f16_to_f32(((const uint16_t*)d->vertex_feat)[i]) : ((const float*)d->vertex_feat)[i];
+  for (int64_t i = 0; i < nv; ++i)
+    s->vdens[(size_t)i] = d->feat_type == SNISR_F16 ? f16_to_f32(((const uint16_t*)d->vertex_density)[i]) : ((const float*)d->vertex_density)[i];
+  return reinterpret_cast<oracle_scene*>(s);
+}
+
+void oracle_scene_destroy(oracle_scene* s) { delete reinterpret_cast<Scene*>(s); }
+
+// Normalised camera directions, same operation order as the GPU ray setup.
+void oracle_camera_dirs(const snisr_camera* cam, float* dirs) {
+  for (int64_t i = 0; i < (int64_t)cam->width * cam->height; ++i) {
+    int py = (int)(i / cam->width), px = (int)(i % cam->width);
+    float x = ((float)px - cam->cx) * cam->inv_focal, y = ((float)py - cam->cy) * cam->inv_focal;
+    float r[3];
+    for (int a = 0; a < 3; ++a) r[a] = (cam->c2w[4 * a] * x + cam->c2w[4 * a + 1] * y) + cam->c2w[4 * a + 2];
+    float n = std::sqrt((r[0] * r[0] + r[1] * r[1]) + r[2] * r[2]);
+    for (int a = 0; a < 3; ++a) dirs[3 * i + a] = r[a] / n;
+  }
+}
+
+// Proxy-mesh start distances: t_start = max(hit - offset, 0), 0 on a miss or
+// without a mesh.  t_hit / tri may be null.
+void oracle_proxy(const oracle_scene* os, const float* o, const float* d, int64_t n, float* t_start, float* t_hit,
+                  int32_t* tri, int threads) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  parallel_for(n, threads, [&](int64_t i) {
+    int id = -1;
+    float th = s.d->num_triangles > 0 ? nearest_hit(s.d, o + 3 * i, d + 3 * i, id) : -1.0f;
+    if (t_hit) t_hit[i] = th;
+    if (tri) tri[i] = id;
+    if (t_start) t_start[i] = th >= 0.0f ? std::max(th - s.start_off, 0.0f) : 0.0f;
+  });
+}
+
+// Occupied-voxel sequence per ray (no transmittance).
+void oracle_trace(const oracle_scene* os, const float* o, const float* d, const float* t_start, int64_t n, int K,
+                  int32_t* visited, int32_t* count, int threads) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  parallel_for(n, threads, [&](int64_t i) {
+    int c = 0;
+    march(s, o + 3 * i, d + 3 * i, t_start ? t_start[i] : 0.0f,
+          [&](int, uint32_t rec, const int*, float, float, float, const float*) {
+            if (c < K) visited[i * K + c] = (int32_t)rec;
+            ++c;
+            return true;
+          });
+    for (int k = c; k < K; ++k) visited[i * K + k] = -1;
+    count[i] = c;
+  });
+}
+
+// Render rays.  form: 0 plain FP32, 1 FP64, 2 tensor-core emulation in FP64.
+// stats (optional, [2]): total samples, total occupied voxels visited.
+void oracle_render(const oracle_scene* os, const float* o, const float* d, const float* t_start, int64_t n, int form,
+                   float* rgb, float* depth, float* opac, int64_t* stats, int threads) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  std::vector<RayStats> per((size_t)n);
+  parallel_for(n, threads, [&](int64_t i) {
+    float ts = t_start ? t_start[i] : 0.0f;
+    if (form == 0) render_ray<float>(s, o + 3 * i, d + 3 * i, ts, 0, rgb + 3 * i, depth[i], opac[i], per[(size_t)i]);
+    else render_ray<double>(s, o + 3 * i, d + 3 * i, ts, form, rgb + 3 * i, depth[i], opac[i], per[(size_t)i]);
+  });
+  if (stats) {
+    stats[0] = stats[1] = 0;
+    for (const auto& p : per) { stats[0] += p.samples; stats[1] += p.voxels; }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reference-op restatements (bit-exact specification of the drop-in ops).
+// ---------------------------------------------------------------------------
+void oracle_op_compute_rays(const float* intr, const float* rot, int H, int W, float* rays_d) {
+  for (int64_t i = 0; i < (int64_t)H * W; ++i) {
+    int py = (int)(i / W), px = (int)(i % W);
+    float x = ((float)px - intr[0]) * intr[2], y = ((float)py - intr[1]) * intr[2];
+    for (int a = 0; a < 3; ++a) rays_d[3 * i + a] = (rot[3 * a] * x + rot[3 * a + 1] * y) + rot[3 * a + 2];
+  }
+}
+
+void oracle_op_tracing_tiles(const float* rays_d, int64_t npix, const int32_t* imap, const float* origin,
+                             const int32_t* shape, const float* smin, const float* ssize, float tile, int K,
+                             int32_t* visited) {
+  for (int64_t i = 0; i < npix; ++i) {
+    int32_t* vis = visited + i * K;
+    for (int j = 0; j < K; ++j) vis[j] = -1;
+    const float* d = rays_d + 3 * i;
+    float p[3];
+    for (int a = 0; a < 3; ++a) p[a] = origin[a] - smin[a];
+    if (p[0] < 0 || p[0] >= ssize[0] || p[1] < 0 || p[1] >= ssize[1] || p[2] < 0 || p[2] >= ssize[2]) {
+      float c[3], h[3];
+      for (int a = 0; a < 3; ++a) { h[a] = ssize[a] / 2.0f; c[a] = smin[a] + h[a]; }
+      Bound b = ray_aabb(origin, d, c, h);
+      for (int a = 0; a < 3; ++a) {
+        p[a] = p[a] + b.lo * d[a];
+        p[a] = std::min(std::max(p[a], 0.0f), ssize[a] - 0.000001f);
+      }
+    }
+    int cur[3], st[3];
+    float tmax[3], tdel[3];
+    for (int a = 0; a < 3; ++a) {
+      cur[a] = std::min(std::max((int)std::floor(p[a] / tile), 0), shape[a] - 1);
+      st[a] = d[a] >= 0 ? 1 : -1;
+      float nb = (float)(cur[a] + st[a]) * tile;
+      if (st[a] < 0) nb = nb + tile;
+      tmax[a] = d[a] != 0 ? (nb - p[a]) / d[a] : kInf;
+      tdel[a] = d[a] != 0 ? (tile / d[a]) * (float)st[a] : kInf;
+    }
+    int idx = 0;
+    int id = imap[((int64_t)cur[0] * shape[1] + cur[1]) * shape[2] + cur[2]];
+    if (id != -1) vis[idx++] = id;
+    while (idx < K) {
+      int a = dda_axis(tmax);
+      cur[a] += st[a];
+      tmax[a] = tmax[a] + tdel[a];
+      if (cur[a] < 0 || cur[a] >= shape[a]) break;
+      id = imap[((int64_t)cur[0] * shape[1] + cur[1]) * shape[2] + cur[2]];
+      if (id != -1) vis[idx++] = id;
+    }
+  }
+}
+
+static void uniform_v3(float* z, float* dist, float near_, float far_, int n) {
+  float interval = (far_ - near_) / (float)n;
+  for (int i = 0; i < n; ++i) {
+    z[i] = near_ + (float)i * interval;
+    dist[i] = interval;
+  }
+}
+
+void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const int16_t* flags, float cx, float cy,
+                             float cz, float tile, int N, int ns, float* zv, float* dv) {
+  const float half = tile * 0.5f, vs = tile / (float)N;
+  const float center[3] = {cx, cy, cz};
+  float minc[3];
+  for (int a = 0; a < 3; ++a) minc[a] = center[a] - half;
+  const float hh[3] = {half, half, half};
+  for (int64_t i = 0; i < B; ++i) {
+    float* z = zv + i * ns;
+    float* dd = dv + i * ns;
+    const float* o = ro + 3 * i;
+    const float* d = rd + 3 * i;
+    Bound nf = ray_aabb(o, d, center, hh);
+    if (nf.lo == -1.0f && nf.hi == -1.0f) continue;
+    float near_ = nf.lo, far_ = nf.hi, total = 0.0f;
+    float loc[3], nb[3], tmax[3], tdel[3];
+    int cur[3], st[3];
+    for (int a = 0; a < 3; ++a) {
+      loc[a] = (o[a] + near_ * d[a]) - minc[a];
+      loc[a] = std::min(std::max(loc[a], 0.0f), tile - 0.000001f);
+      cur[a] = std::min(std::max((int)(loc[a] / vs), 0), N - 1);
+      st[a] = d[a] >= 0 ? 1 : -1;
+      nb[a] = (float)(cur[a] + st[a]) * vs;
+      if (st[a] < 0) nb[a] = nb[a] + vs;
+      tmax[a] = safe_divide(nb[a] - loc[a], d[a]);
+      tdel[a] = safe_divide((float)st[a] * vs, d[a]);
+    }
+    auto vbound = [&]() {
+      float vc[3];
+      for (int a = 0; a < 3; ++a) vc[a] = (minc[a] + (float)cur[a] * vs) + 0.5f * vs;
+      const float h5 = 0.5f * vs;
+      const float h3[3] = {h5, h5, h5};
+      return ray_aabb(o, d, vc, h3);
+    };
+    auto step = [&]() {
+      int a = dda_axis(tmax);
+      cur[a] += st[a];
+      tmax[a] = tmax[a] + tdel[a];
+      return !(cur[a] < 0 || cur[a] >= N);
+    };
+    for (;;) {
+      if (flags[((int64_t)cur[0] * N + cur[1]) * N + cur[2]] == 1) {
+        Bound b = vbound();
+        total = total + (b.hi - b.lo);
+      }
+      if (!step()) break;
+    }
+    if (total == 0.0f) continue;
+    for (int a = 0; a < 3; ++a) {
+      cur[a] = std::min(std::max((int)(loc[a] / vs), 0), N - 1);
+      tmax[a] = safe_divide(nb[a] - loc[a], d[a]);
+    }
+    int count = 0, bsm = 4;
+    bool acc = false, first = false;
+    const int ins = ns - 2 * bsm;
+    for (;;) {
+      if (flags[((int64_t)cur[0] * N + cur[1]) * N + cur[2]] == 1) {
+        Bound b = vbound();
+        if (b.lo != -1.0f && b.hi != -1.0f) {
+          if (acc) far_ = b.hi;
+          else {
+            near_ = b.lo;
+            far_ = b.hi;
+            acc = true;
+            if (!first) {
+              first = true;
+              uniform_v3(z + count, dd + count, near_ - vs, near_ - 0.000001f, bsm);
+              count += bsm;
+            }
+          }
+        }
+      } else if (acc) {
+        int num = (int)std::ceil(((float)ins * (far_ - near_)) / total);
+        num = std::min(ns - count, num);
+        uniform_v3(z + count, dd + count, near_, far_, num);
+        count += num;
+        acc = false;
+      }
+      if (!step()) break;
+    }
+    if (acc) {
+      int num = (int)std::ceil(((float)ins * (far_ - near_)) / total);
+      num = std::min(ns - count, num);
+      uniform_v3(z + count, dd + count, near_, far_, num);
+      count += num;
+    }
+    bsm = std::min(ns - count, bsm);
+    uniform_v3(z + count, dd + count, far_ + 0.000001f, far_ + vs, bsm);
+  }
+}
+
+void oracle_op_inverse_z(const float* rays_d, const float* origin, const float* inv_near, const float* inv_bound,
+                         int64_t npix, int offset, int spr, float* pts, float* steps) {
+  for (int64_t t = 0; t < npix * spr; ++t) {
+    int64_t p = t / spr;
+    int j = (int)(t % spr);
+    float z = 1.0f / ((float)(offset + j) * inv_bound[p] + inv_near[p]);
+    float zn = 1.0f / ((float)(offset + j + 1) * inv_bound[p] + inv_near[p]);
+    steps[t] = std::max(zn - z, 0.0f);
+    for (int a = 0; a < 3; ++a) pts[3 * t + a] = origin[a] + z * rays_d[3 * p + a];
+  }
+}
+
+void oracle_op_integrate(const float* rgba, const float* dz, int64_t npix, float early, float* frame, float* trans) {
+  for (int64_t i = 0; i < npix; ++i) {
+    float T = trans[i];
+    if (T < early) continue;
+    float c[3] = {0, 0, 0};
+    for (int s = 0; s < 16; ++s) {
+      const float* v = rgba + (i * 16 + s) * 4;
+      float alpha = 1.0f - std::exp((-1.0f * v[3]) * dz[i * 16 + s]);
+      float w = alpha * T;
+      for (int a = 0; a < 3; ++a) c[a] = c[a] + w * v[a];
+      T = T * (1.0f - alpha);
+    }
+    trans[i] = T;
+    for (int a = 0; a < 3; ++a) frame[3 * i + a] = frame[3 * i + a] + c[a];
+  }
+}
+
+// Pieces exposed for the reference-harness cross-check.
+void oracle_ray_aabb(const float* o, const float* d, const float* c, float h, float* out) {
+  const float hh[3] = {h, h, h};
+  Bound b = ray_aabb(o, d, c, hh);
+  out[0] = b.lo;
+  out[1] = b.hi;
+}
+int oracle_voxel_traversal(const float* o, const float* d, const int32_t* imap, int32_t* visited, int K, int Mx, int My,
+                           int Mz, float vs) {
+  int cur[3], st[3];
+  float tmax[3], tdel[3];
+  const int M[3] = {Mx, My, Mz};
+  for (int a = 0; a < 3; ++a) {
+    cur[a] = (int)std::floor(o[a] / vs);
+    st[a] = d[a] >= 0 ? 1 : -1;
+    float nb = (float)(cur[a] + st[a]) * vs;
+    if (st[a] < 0) nb = nb + vs;
+    tmax[a] = d[a] != 0 ? (nb - o[a]) / d[a] : kInf;
+    tdel[a] = d[a] != 0 ? (vs / d[a]) * (float)st[a] : kInf;
+  }
+  int idx = 0;
+  int id = imap[((int64_t)cur[0] * My + cur[1]) * Mz + cur[2]];
+  if (id != -1) visited[idx++] = id;
+  while (idx < K) {
+    int a = dda_axis(tmax);
+    cur[a] += st[a];
+    tmax[a] = tmax[a] + tdel[a];
+    if (cur[a] < 0 || cur[a] >= M[a]) break;
+    id = imap[((int64_t)cur[0] * My + cur[1]) * Mz + cur[2]];
+    if (id != -1) visited[idx++] = id;
+  }
+  return idx;
+}
+float oracle_ray_triangle_onesided(const float* o, const float* d, const float* A, const float* B, const float* C) {
+  // the reference's single-sided test with blur 0 (cuda_utils.h:403-436)
+  float e1[3], e2[3], s[3], p[3], q[3];
+  for (int a = 0; a < 3; ++a) { e1[a] = B[a] - A[a]; e2[a] = C[a] - A[a]; s[a] = o[a] - A[a]; }
+  cross3(d, e2, p);
+  float det = dot3(e1, p);
+  if (det < 0.00000001f) return -kInf;
+  det = 1.0f / det;
+  float u = dot3(s, p) * det;
+  if (u < 0.0f || u > 1.0f) return -kInf;
+  cross3(s, e1, q);
+  float v = dot3(d, q) * det;
+  if (v < 0.0f || v > 1.0f) return -kInf;
+  if ((u + v) < 0.0f || (u + v) > 1.0f) return -kInf;
+  return dot3(e2, q) * det;
+}
+void oracle_trilinear_base(const float* voxels, int Mx, int My, int Mz, const float* point, float* out) {
+  // FP32 trilinear with edge fallbacks (interpolation.h:41-116), float4 voxels
+  int MYZ = My * Mz;
+  int x0 = (int)point[0], y0 = (int)point[1], z0 = (int)point[2];
+  int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+  float x = point[0] - x0, y = point[1] - y0, z = point[2] - z0;
+  if (x < 0) x = 0;
+  if (y < 0) y = 0;
+  if (z < 0) z = 0;
+  auto V = [&](int i, int j, int k, int c) { return voxels[((int64_t)i * MYZ + j * Mz + k) * 4 + c]; };
+  auto i1 = [](float a, float b, float t) { return a * (1.0f - t) + b * t; };
+  for (int c = 0; c < 4; ++c) {
+    float r;
+    if (x1 >= Mx) {
+      if (y1 >= My) r = (z1 >= Mz) ? V(x0, y0, z0, c) : i1(V(x0, y0, z0, c), V(x0, y0, z1, c), z);
+      else if (z1 >= Mz) r = i1(V(x0, y0, z0, c), V(x0, y1, z0, c), y);
+      else r = i1(i1(V(x0, y0, z0, c), V(x0, y1, z0, c), y), i1(V(x0, y0, z1, c), V(x0, y1, z1, c), y), z);
+    } else {
+      if (y1 >= My) {
+        if (z1 >= Mz) r = i1(V(x0, y0, z0, c), V(x1, y0, z0, c), x);
+        else r = i1(i1(V(x0, y0, z0, c), V(x1, y0, z0, c), x), i1(V(x0, y0, z1, c), V(x1, y0, z1, c), x), z);
+      } else if (z1 >= Mz) {
+        r = i1(i1(V(x0, y0, z0, c), V(x1, y0, z0, c), x), i1(V(x0, y1, z0, c), V(x1, y1, z0, c), x), y);
+      } else {
+        float s = i1(i1(V(x0, y0, z0, c), V(x1, y0, z0, c), x), i1(V(x0, y1, z0, c), V(x1, y1, z0, c), x), y);
+        float t = i1(i1(V(x0, y0, z1, c), V(x1, y0, z1, c), x), i1(V(x0, y1, z1, c), V(x1, y1, z1, c), x), y);
+        r = i1(s, t, z);
+      }
+    }
+    out[c] = r;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,286 @@
+// Device-side scene view and ray traversal shared by the GB300 kernels.
+//
+// Traversal arithmetic is written with explicit round-to-nearest intrinsics
+// (__fadd_rn, __fmul_rn, __fdiv_rn) so that no multiply-add is contracted:
+// the visited voxel sequence is then bit-identical to an IEEE single
+// precision evaluation of the same expressions on the host.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "scene_dev.h"
+
+namespace snisr {
+
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+// reference safe_divide (rendering/src/include/cutil_math.h:867-869)
+__device__ __forceinline__ float safe_div(float a, float b) { return b != 0.0f ? __fdiv_rn(a, b) : SNISR_INF; }
+
+// Slab test with the reference's conventions (RayAABBIntersection,
+// rendering/src/include/cuda_utils.h:506-598): t_low starts at 0, t_high at
+// 1e5, a miss returns (-1, -1).
+__device__ __forceinline__ float2 slab(const float o[3], const float d[3], const float c[3], const float h[3]) {
+  float lo = 0.0f, hi = 100000.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float inv = safe_div(1.0f, d[a]);
+    float l = fmul(fsub(fsub(c[a], h[a]), o[a]), inv);
+    float u = fmul(fsub(fadd(c[a], h[a]), o[a]), inv);
+    if (u < l) { float t = l; l = u; u = t; }
+    if (u < lo) return make_float2(-1.0f, -1.0f);
+    if (l > hi) return make_float2(-1.0f, -1.0f);
+    lo = (l > lo) ? l : lo;
+    hi = (u < hi) ? u : hi;
+    if (lo > hi) return make_float2(-1.0f, -1.0f);
+  }
+  return make_float2(lo, hi);
+}
+
+__device__ __forceinline__ bool occupied(const SceneDev& S, int tile, int vid, uint32_t& rec) {
+  const OccWord* w = S.occ + (size_t)tile * S.words_per_tile + (vid >> 6);
+  uint4 raw = __ldg(reinterpret_cast<const uint4*>(w));
+  unsigned long long bits = ((unsigned long long)raw.y << 32) | raw.x;
+  int b = vid & 63;
+  if (!((bits >> b) & 1ull)) return false;
+  rec = raw.z + (uint32_t)__popcll(bits & ((1ull << b) - 1ull));
+  return true;
+}
+
+__device__ __forceinline__ bool block_occupied(const SceneDev& S, int tile, int cx, int cy, int cz) {
+  int nb = S.res >> 2;
+  int bid = (cx * nb + cy) * nb + cz;
+  int words = (nb * nb * nb + 31) >> 5;
+  uint32_t w = __ldg(S.block_mask + (size_t)tile * words + (bid >> 5));
+  return (w >> (bid & 31)) & 1u;
+}
+
+// Ray state machine: tile DDA over the scene grid, voxel DDA inside each
+// visited tile, fixed-step samples inside each occupied voxel.
+//
+// Follows, in order: the scene clip + tile DDA of tracing_tiles_kernel /
+// voxel_traversal (rendering/src/raytile_tracing.cu:32-56,
+// rendering/src/include/cuda_utils.h:158-238), the per-tile AABB clip of
+// rendering_diffuse_octree_fp16_kernel (raydiffuse_render_octree_fp16.cu:
+// 202-214), the voxel DDA of Sample_sparse_cuda_kernel
+// (training/src/Sample_kernel.cu:228-283) and the fixed-step march of
+// block_traversal_rendering (raydiffuse_render_octree_fp16.cu:67-106),
+// applied per occupied voxel instead of per 4^3 block.
+struct RayState {
+  float o[3], d[3];
+  float t_start;
+  // tile DDA (relative to the scene entry point)
+  int tc[3], tstep[3];
+  float tmax[3], tdelta[3];
+  bool tile_live;     // tile DDA still inside the grid
+  bool pending_tile;  // current tile-DDA cell not yet opened
+  // voxel DDA inside the current tile
+  int tile;        // sparse id, -1 when no tile is open
+  float t_in, q[3];
+  int vc[3], vstep[3];
+  float vmax[3], vdelta[3];
+  float near_, far_;
+  // current occupied voxel
+  uint32_t rec;
+  float z;         // next sample position (relative to t_in)
+  bool in_voxel;
+
+  __device__ bool init(const SceneDev& S, const float* oo, const float* dd, float ts) {
+    for (int a = 0; a < 3; ++a) { o[a] = oo[a]; d[a] = dd[a]; }
+    t_start = ts;
+    tile = -1;
+    in_voxel = false;
+    tile_live = false;
+    const int g[3] = {S.gx, S.gy, S.gz};
+    float size[3], half[3], cen[3];
+    for (int a = 0; a < 3; ++a) {
+      size[a] = fmul((float)g[a], S.tile_size);
+      half[a] = fmul(size[a], 0.5f);
+      cen[a] = fadd(S.smin[a], half[a]);
+    }
+    float2 b = slab(o, d, cen, half);
+    if (b.x == -1.0f) return false;
+    float t0 = fmaxf(b.x, t_start);
+    if (!(t0 < b.y)) return false;
+    float p[3];
+    for (int a = 0; a < 3; ++a) {
+      p[a] = fsub(fadd(o[a], fmul(t0, d[a])), S.smin[a]);
+      p[a] = fminf(fmaxf(p[a], 0.0f), fsub(size[a], 0.000001f));
+      int c = (int)floorf(fdiv(p[a], S.tile_size));
+      tc[a] = min(max(c, 0), g[a] - 1);
+      tstep[a] = d[a] >= 0.0f ? 1 : -1;
+      float nb = fmul((float)(tc[a] + tstep[a]), S.tile_size);
+      if (tstep[a] < 0) nb = fadd(nb, S.tile_size);
+      tmax[a] = d[a] != 0.0f ? fdiv(fsub(nb, p[a]), d[a]) : SNISR_INF;
+      tdelta[a] = d[a] != 0.0f ? fmul(fdiv(S.tile_size, d[a]), (float)tstep[a]) : SNISR_INF;
+    }
+    tile_live = true;
+    pending_tile = true;
+    return true;
+  }
+
+  // Opens the current tile of the tile DDA if it is non-empty and the ray
+  // overlaps it; returns false if nothing to march in it.
+  __device__ bool open_tile(const SceneDev& S) {
+    int dense = (tc[0] * S.gy + tc[1]) * S.gz + tc[2];
+    int id = __ldg(S.tile_index + dense);
+    if (id < 0) return false;
+    float c[3], h[3];
+    for (int a = 0; a < 3; ++a) { c[a] = __ldg(S.tile_center + 3 * id + a); h[a] = fmul(S.tile_size, 0.5f); }
+    float2 b = slab(o, d, c, h);
+    if (b.x == -1.0f) return false;
+    float ti = fmaxf(b.x, t_start);
+    if (!(ti < b.y)) return false;
+    t_in = ti;
+    const int N = S.res;
+    for (int a = 0; a < 3; ++a) {
+      float corner = fsub(c[a], h[a]);
+      q[a] = fsub(fadd(o[a], fmul(ti, d[a])), corner);
+      q[a] = fminf(fmaxf(q[a], 0.0f), fsub(S.tile_size, 0.00001f));
+      int v = (int)fdiv(q[a], S.voxel);
+      vc[a] = min(max(v, 0), N - 1);
+      vstep[a] = d[a] >= 0.0f ? 1 : -1;
+      float nb = fmul((float)(vc[a] + vstep[a]), S.voxel);
+      if (vstep[a] < 0) nb = fadd(nb, S.voxel);
+      vmax[a] = safe_div(fsub(nb, q[a]), d[a]);
+      vdelta[a] = safe_div(fmul((float)vstep[a], S.voxel), d[a]);
+    }
+    near_ = 0.0f;
+    tile = id;
+    return true;
+  }
+
+  // One Amanatides-Woo step with the reference tie rule: x only when strictly
+  // smallest, then y only when strictly smaller than z, otherwise z.
+  __device__ __forceinline__ int dda_axis(const float* m) const {
+    if (m[0] < m[1]) return (m[0] < m[2]) ? 0 : 2;
+    return (m[1] < m[2]) ? 1 : 2;
+  }
+
+  // Advances the tile DDA to the next tile; false when it leaves the grid.
+  __device__ bool step_tile(const SceneDev& S) {
+    int a = dda_axis(tmax);
+    tc[a] += tstep[a];
+    tmax[a] = fadd(tmax[a], tdelta[a]);
+    const int g[3] = {S.gx, S.gy, S.gz};
+    if (tc[a] < 0 || tc[a] >= g[a]) { tile_live = false; return false; }
+    return true;
+  }
+
+  // Moves to the next occupied voxel along the ray, crossing tiles as
+  // needed.  Sets rec, near_, far_.  Returns false when the ray has left the
+  // scene.  Every iteration moves one DDA coordinate by one cell, so the loop
+  // ends after at most (grid + tile) extent steps.
+  __device__ bool next_voxel(const SceneDev& S) {
+    const int N = S.res;
+    for (;;) {
+      if (tile < 0) {
+        if (!tile_live) return false;
+        if (!pending_tile && !step_tile(S)) return false;
+        pending_tile = false;
+        if (!open_tile(S)) continue;
+        // the entry voxel of the freshly opened tile
+        far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
+        int vid = (vc[0] * N + vc[1]) * N + vc[2];
+        uint32_t r;
+        if (block_occupied(S, tile, vc[0] >> 2, vc[1] >> 2, vc[2] >> 2) && occupied(S, tile, vid, r)) {
+          rec = r;
+          return true;
+        }
+      }
+      int a = dda_axis(vmax);
+      vc[a] += vstep[a];
+      vmax[a] = fadd(vmax[a], vdelta[a]);
+      near_ = far_;
+      if (vc[a] < 0 || vc[a] >= N) { tile = -1; continue; }
+      far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
+      if (!block_occupied(S, tile, vc[0] >> 2, vc[1] >> 2, vc[2] >> 2)) continue;
+      int vid = (vc[0] * N + vc[1]) * N + vc[2];
+      uint32_t r;
+      if (occupied(S, tile, vid, r)) { rec = r; return true; }
+    }
+  }
+};
+
+// One sample inside an occupied voxel.
+struct Sample {
+  uint32_t rec;
+  int tile;
+  float f[3];      // position inside the voxel, clamped to [0,1]
+  float interval;  // world length represented by the sample
+  float t;         // world distance from the ray origin
+};
+
+// Produces the next sample of the ray; false when the ray left the scene.
+__device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Sample& s) {
+  for (;;) {
+    if (R.in_voxel && R.z < R.far_) {
+      s.rec = R.rec;
+      s.tile = R.tile;
+      for (int a = 0; a < 3; ++a) {
+        float pos = fadd(R.q[a], fmul(R.z, R.d[a]));
+        float f = fsub(fmul(pos, S.inv_voxel), (float)R.vc[a]);
+        s.f[a] = fminf(fmaxf(f, 0.0f), 1.0f);
+      }
+      s.interval = fminf(S.step_len, fsub(R.far_, R.z));
+      s.t = fadd(R.t_in, R.z);
+      R.z = fadd(R.z, S.step_len);
+      return true;
+    }
+    if (!R.next_voxel(S)) return false;
+    R.in_voxel = true;
+    R.z = R.near_;
+  }
+}
+
+__device__ __forceinline__ void trilinear_weights(const float f[3], float w[8]) {
+  float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) w[k] = wx[(k >> 2) & 1] * wy[(k >> 1) & 1] * wz[k & 1];
+}
+
+__device__ __forceinline__ float softplusf(float x) { return fmaxf(x, 0.0f) + log1pf(expf(-fabsf(x))); }
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
+
+// Density of a sample: softplus of the trilinear density logit, per voxel length.
+__device__ __forceinline__ float sample_sigma(const SceneDev& S, const Sample& s, float w[8]) {
+  trilinear_weights(s.f, w);
+  const float4* dp = reinterpret_cast<const float4*>(S.dens + (size_t)s.rec * 8);
+  float4 a = __ldg(dp), b = __ldg(dp + 1);
+  float g = w[0] * a.x + w[1] * a.y + w[2] * a.z + w[3] * a.w + w[4] * b.x + w[5] * b.y + w[6] * b.z + w[7] * b.w;
+  return softplusf(g);
+}
+
+// View-direction encoding: [d, sin(2^0 d), cos(2^0 d), ..., sin(2^{L-1} d), cos(2^{L-1} d)]
+// (reference Positional_Encoding, training/scripts/networks.py:4-15).
+__device__ __forceinline__ void dir_encoding(const float d[3], int L, float* out) {
+  out[0] = d[0]; out[1] = d[1]; out[2] = d[2];
+  float scale = 1.0f;
+  for (int i = 0; i < L; ++i) {
+    for (int a = 0; a < 3; ++a) {
+      float s, c;
+      sincosf(scale * d[a], &s, &c);
+      out[3 + 6 * i + a] = s;
+      out[3 + 6 * i + 3 + a] = c;
+    }
+    scale *= 2.0f;
+  }
+}
+
+// Ray direction of a pixel (reference get_direction, rendering/src/compute_rays.cu:7-17),
+// normalised.
+__device__ __forceinline__ void camera_dir(const float* c2w, float cx, float cy, float inv_f, int px, int py, float d[3]) {
+  float x = fmul(fsub((float)px, cx), inv_f);
+  float y = fmul(fsub((float)py, cy), inv_f);
+  float r[3];
+  for (int a = 0; a < 3; ++a) r[a] = fadd(fadd(fmul(c2w[4 * a + 0], x), fmul(c2w[4 * a + 1], y)), c2w[4 * a + 2]);
+  float n = __fsqrt_rn(fadd(fadd(fmul(r[0], r[0]), fmul(r[1], r[1])), fmul(r[2], r[2])));
+  for (int a = 0; a < 3; ++a) d[a] = fdiv(r[a], n);
+}
+
+}  // namespace snisr

@@ -1,0 +1,50 @@
+// Host-side launchers of the GB300 kernels (implemented in *.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "scene_dev.h"
+
+namespace snisr {
+
+struct CamDev {
+  int W, H;
+  float cx, cy, inv_f;
+  float c2w[12];
+};
+
+// Per-scene workspace, sized at creation; nothing is allocated per frame.
+struct Workspace {
+  float4* ray_o = nullptr;     // [max_rays] origin
+  float4* ray_d = nullptr;     // [max_rays] direction, w = start distance
+  uint4* enc = nullptr;        // [max_rays][4] FP16 view encoding (32 halves)
+  SampleRec* recs = nullptr;   // [cap] compacted samples
+  SampleRec* sorted = nullptr; // [cap] samples grouped by tile
+  uint32_t cap = 0;
+  int* ctrl = nullptr;         // frame control words
+  int ctrl_words = 0;
+  int64_t max_rays = 0;
+  const uint8_t* wimg = nullptr;  // per-tile tensor-core weight images
+  int wimg_stride = 0;            // bytes per tile image
+  int wimg_bytes = 0;             // bytes copied per tile
+};
+
+// Shape of a supported MLP instantiation.
+bool mlp_shape_supported(int F, int H, int L);
+// Bytes of one tile's tensor-core weight image (see build in api.cpp).
+int tc_image_bytes(int H, int L);
+
+cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* origins, const float* dirs,
+                          int64_t n, const Workspace& ws, bool want_enc, cudaStream_t st);
+cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
+                                float* opac, cudaStream_t st);
+cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
+                             float* opac, int num_sms, cudaStream_t st);
+cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int K, int32_t* visited,
+                         int32_t* count, cudaStream_t st);
+cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t,
+                         int32_t* tri, cudaStream_t st);
+cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, cudaStream_t st);
+
+}  // namespace snisr

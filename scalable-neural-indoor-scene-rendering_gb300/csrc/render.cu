@@ -1,0 +1,703 @@
+// Render kernels: ray generation with the proxy-mesh start, the plain FP32
+// form (one thread per ray, CUDA-core MLP) and the batched tensor-core form
+// (warp-compacted traversal -> per-tile bucketing -> tcgen05 MLP).
+#include <cuda_fp16.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "proxy.cuh"
+#include "tc_ptx.cuh"
+
+namespace snisr {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// Ray generation: direction, proxy-mesh start distance, FP16 view encoding.
+// ---------------------------------------------------------------------------
+__global__ void raygen_kernel(SceneDev S, CamDev cam, const float* __restrict__ origins,
+                              const float* __restrict__ dirs, int64_t n, float4* ray_o, float4* ray_d,
+                              uint4* enc, int want_enc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float o[3], d[3];
+    if (dirs) {
+      for (int a = 0; a < 3; ++a) { o[a] = origins[3 * i + a]; d[a] = dirs[3 * i + a]; }
+    } else {
+      int py = (int)(i / cam.W), px = (int)(i - (int64_t)py * cam.W);
+      camera_dir(cam.c2w, cam.cx, cam.cy, cam.inv_f, px, py, d);
+      o[0] = cam.c2w[3]; o[1] = cam.c2w[7]; o[2] = cam.c2w[11];
+    }
+    float ts = 0.0f;
+    if (S.has_mesh) {
+      int tri;
+      float th = bvh_nearest(S, o, d, tri);
+      if (th >= 0.0f) ts = fmaxf(fsub(th, S.start_offset), 0.0f);
+    }
+    ray_o[i] = make_float4(o[0], o[1], o[2], 0.0f);
+    ray_d[i] = make_float4(d[0], d[1], d[2], ts);
+    if (want_enc) {
+      float e[27];
+      dir_encoding(d, 4, e);
+      __align__(16) __half h[32];
+      for (int k = 0; k < 32; ++k) h[k] = __float2half_rn(k < 27 ? e[k] : 0.0f);
+      const uint4* src = reinterpret_cast<const uint4*>(h);
+      for (int k = 0; k < 4; ++k) enc[4 * i + k] = src[k];
+    }
+  }
+}
+
+__global__ void proxy_kernel(SceneDev S, const float* __restrict__ origins, const float* __restrict__ dirs,
+                             int64_t n, float* t_out, int32_t* tri_out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float o[3] = {origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]};
+    float d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+    int tri = -1;
+    float t = S.has_mesh ? bvh_nearest(S, o, d, tri) : -1.0f;
+    t_out[i] = t;
+    tri_out[i] = tri;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Occupied-voxel sequences (no transmittance), for parity checks.
+// ---------------------------------------------------------------------------
+__global__ void trace_kernel(SceneDev S, const float4* __restrict__ ray_o, const float4* __restrict__ ray_d,
+                             int64_t n, int K, int32_t* visited, int32_t* count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 o4 = ray_o[i], d4 = ray_d[i];
+    float o[3] = {o4.x, o4.y, o4.z}, d[3] = {d4.x, d4.y, d4.z};
+    RayState R;
+    int c = 0;
+    if (R.init(S, o, d, d4.w)) {
+      while (R.next_voxel(S)) {
+        if (c < K) visited[i * K + c] = (int32_t)R.rec;
+        ++c;
+      }
+    }
+    for (int k = c; k < K; ++k) visited[i * K + k] = -1;
+    count[i] = c;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP32 form: one thread per ray, FP32 features/weights, CUDA-core MLP.
+// Weight layout per tile: for each Linear, W[out][round4(in)] then b[round4(out)].
+// ---------------------------------------------------------------------------
+template <int KIN, int H, int L>
+__device__ __forceinline__ void mlp_plain(const float* __restrict__ P, const float* x, float out[3]) {
+  constexpr int KP = (KIN + 3) & ~3;
+  float h[H];
+  {
+    const float4* W = reinterpret_cast<const float4*>(P);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int i = 0; i < KP / 4; ++i) {
+        float4 w = __ldg(W + j * (KP / 4) + i);
+        acc = fmaf(w.x, x[4 * i], acc);
+        acc = fmaf(w.y, x[4 * i + 1], acc);
+        acc = fmaf(w.z, x[4 * i + 2], acc);
+        acc = fmaf(w.w, x[4 * i + 3], acc);
+      }
+      h[j] = acc;
+    }
+    P += H * KP;
+#pragma unroll
+    for (int j = 0; j < H; ++j) h[j] = fmaxf(h[j] + __ldg(P + j), 0.0f);
+    P += H;
+  }
+#pragma unroll
+  for (int l = 1; l < L; ++l) {
+    float g[H];
+    const float4* W = reinterpret_cast<const float4*>(P);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int i = 0; i < H / 4; ++i) {
+        float4 w = __ldg(W + j * (H / 4) + i);
+        acc = fmaf(w.x, h[4 * i], acc);
+        acc = fmaf(w.y, h[4 * i + 1], acc);
+        acc = fmaf(w.z, h[4 * i + 2], acc);
+        acc = fmaf(w.w, h[4 * i + 3], acc);
+      }
+      g[j] = acc;
+    }
+    P += H * H;
+#pragma unroll
+    for (int j = 0; j < H; ++j) h[j] = fmaxf(g[j] + __ldg(P + j), 0.0f);
+    P += H;
+  }
+  const float4* W = reinterpret_cast<const float4*>(P);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < H / 4; ++i) {
+      float4 w = __ldg(W + c * (H / 4) + i);
+      acc = fmaf(w.x, h[4 * i], acc);
+      acc = fmaf(w.y, h[4 * i + 1], acc);
+      acc = fmaf(w.z, h[4 * i + 2], acc);
+      acc = fmaf(w.w, h[4 * i + 3], acc);
+    }
+    out[c] = acc;
+  }
+  P += 3 * H;
+  for (int c = 0; c < 3; ++c) out[c] += __ldg(P + c);
+}
+
+template <int F, int H, int L>
+__global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const float4* __restrict__ ray_o,
+                                                           const float4* __restrict__ ray_d, int64_t n,
+                                                           float* rgb, float* depth, float* opac) {
+  constexpr int KIN = F + 27;
+  constexpr int KP = (KIN + 3) & ~3;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 o4 = ray_o[i], d4 = ray_d[i];
+    float o[3] = {o4.x, o4.y, o4.z}, d[3] = {d4.x, d4.y, d4.z};
+    float x[KP];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) x[k] = 0.0f;
+    dir_encoding(d, 4, x + F);
+    float C[3] = {0.f, 0.f, 0.f}, D = 0.f, T = 1.f;
+    RayState R;
+    if (R.init(S, o, d, d4.w)) {
+      Sample s;
+      while (next_sample(S, R, s)) {
+        float w[8];
+        float sig = sample_sigma(S, s, w);
+        float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
+        float wt = T * alpha;
+        const float4* fp = S.feat32 + (size_t)s.rec * (F / 4) * 8;
+#pragma unroll
+        for (int g = 0; g < F / 4; ++g) {
+          float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            float4 v = __ldg(fp + g * 8 + k);
+            acc.x = fmaf(w[k], v.x, acc.x); acc.y = fmaf(w[k], v.y, acc.y);
+            acc.z = fmaf(w[k], v.z, acc.z); acc.w = fmaf(w[k], v.w, acc.w);
+          }
+          x[4 * g] = acc.x; x[4 * g + 1] = acc.y; x[4 * g + 2] = acc.z; x[4 * g + 3] = acc.w;
+        }
+        float out[3];
+        mlp_plain<KIN, H, L>(S.mlp_plain + (size_t)s.tile * S.plain_stride, x, out);
+        for (int c = 0; c < 3; ++c) C[c] += wt * sigmoidf_(out[c]);
+        D += wt * s.t;
+        T *= (1.0f - alpha);
+        if (T < S.early_stop) break;
+      }
+    }
+    rgb[3 * i] = C[0]; rgb[3 * i + 1] = C[1]; rgb[3 * i + 2] = C[2];
+    depth[i] = D;
+    opac[i] = 1.0f - T;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched tensor-core form, stage 1: traversal with per-warp compaction.
+// Each lane marches one ray; every round the warp converges, ballots the
+// lanes that produced a sample and writes them to consecutive slots of a
+// per-warp block of the sample buffer (one global atomic per 256 samples).
+// Depth and opacity are final here: density comes from the voxel data, so
+// transmittance and early stop do not wait for the MLP.
+// ---------------------------------------------------------------------------
+constexpr int kTravThreads = 128;
+constexpr uint32_t kBlk = 256;
+
+__global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
+                                                                const float4* __restrict__ ray_d, int64_t n,
+                                                                SampleRec* recs, uint32_t cap, int* ctrl,
+                                                                float* depth, float* opac) {
+  extern __shared__ uint32_t hist[];
+  for (int t = threadIdx.x; t < S.num_tiles; t += blockDim.x) hist[t] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  RayState R;
+  bool live = false;
+  float T = 1.0f, D = 0.0f;
+  if (i < n) {
+    float4 o4 = ray_o[i], d4 = ray_d[i];
+    float o[3] = {o4.x, o4.y, o4.z}, d[3] = {d4.x, d4.y, d4.z};
+    live = R.init(S, o, d, d4.w);
+  }
+  uint32_t cur = 0, end = 0;  // warp-uniform block cursor
+  for (;;) {
+    Sample s;
+    bool have = false;
+    float wt = 0.0f;
+    if (live) {
+      have = next_sample(S, R, s);
+      if (!have) {
+        live = false;
+      } else {
+        float w[8];
+        float sig = sample_sigma(S, s, w);
+        float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
+        wt = T * alpha;
+        D += wt * s.t;
+        T *= (1.0f - alpha);
+        if (T < S.early_stop) live = false;
+      }
+    }
+    unsigned m = __ballot_sync(kFull, have);
+    if (m == 0) break;
+    uint32_t cnt = __popc(m), idx = __popc(m & lanemask_lt());
+    uint32_t slot;
+    if (cur + cnt > end) {
+      uint32_t nb = 0;
+      if (lane == 0) nb = (uint32_t)atomicAdd(ctrl + CTRL_RESERVED, (int)kBlk);
+      nb = __shfl_sync(kFull, nb, 0);
+      uint32_t rem = end - cur;
+      slot = idx < rem ? cur + idx : nb + (idx - rem);
+      cur = nb + (cnt - rem);
+      end = nb + kBlk;
+    } else {
+      slot = cur + idx;
+      cur += cnt;
+    }
+    bool wrote = have && slot < cap;
+    if (have && !wrote) atomicOr(S.err, ERR_OVERFLOW);
+    unsigned m2 = __ballot_sync(kFull, wrote);
+    if (wrote) {
+      uint4* dst = reinterpret_cast<uint4*>(recs + slot);
+      dst[0] = make_uint4(s.rec, (uint32_t)i, __float_as_uint(wt), (uint32_t)s.tile);
+      dst[1] = make_uint4(__float_as_uint(s.f[0]), __float_as_uint(s.f[1]), __float_as_uint(s.f[2]), 0u);
+      unsigned g = __match_any_sync(m2, s.tile);
+      if (lane == __ffs(g) - 1) atomicAdd(hist + s.tile, (uint32_t)__popc(g));
+    }
+  }
+  for (uint32_t sl = cur + lane; sl < end; sl += 32)
+    if (sl < cap) recs[sl].rec = kInvalid;
+  if (i < n) {
+    depth[i] = D;
+    opac[i] = 1.0f - T;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < S.num_tiles; t += blockDim.x)
+    if (hist[t]) atomicAdd(ctrl + CTRL_HEADER + t, (int)hist[t]);
+}
+
+// Stage 2: per-tile offsets and 128-sample chunk offsets (one thread; the
+// tile count is small).  Layout after the header: count[NT], off[NT+1],
+// coff[NT+1], cursor[NT].
+__global__ void scan_kernel(int* ctrl, int NT) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int* cnt = ctrl + CTRL_HEADER;
+  int* off = cnt + NT;
+  int* coff = off + NT + 1;
+  int* cursor = coff + NT + 1;
+  int o = 0, c = 0;
+  for (int t = 0; t < NT; ++t) {
+    off[t] = o;
+    coff[t] = c;
+    o += cnt[t];
+    c += (cnt[t] + 127) / 128;
+    cursor[t] = 0;
+  }
+  off[NT] = o;
+  coff[NT] = c;
+  ctrl[CTRL_CHUNKS] = c;
+  ctrl[CTRL_SAMPLES] = o;
+}
+
+// Stage 3: move samples into per-tile order (warp-aggregated cursors).
+__global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap, int* ctrl, int NT,
+                               SampleRec* sorted) {
+  const int lane = threadIdx.x & 31;
+  uint32_t total = min((uint32_t)ctrl[CTRL_RESERVED], cap);
+  const int* off = ctrl + CTRL_HEADER + NT;
+  int* cursor = ctrl + CTRL_HEADER + NT + (NT + 1) + (NT + 1);
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < total; base += warps * 32) {
+    uint32_t s = base + lane;
+    uint4 a = make_uint4(kInvalid, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+    if (s < total) {
+      const uint4* src = reinterpret_cast<const uint4*>(recs + s);
+      a = src[0];
+      b = src[1];
+    }
+    bool valid = a.x != kInvalid;
+    unsigned m = __ballot_sync(kFull, valid);
+    if (valid) {
+      unsigned g = __match_any_sync(m, a.w);
+      int leader = __ffs(g) - 1;
+      int pos = 0;
+      if (lane == leader) pos = atomicAdd(cursor + a.w, __popc(g));
+      pos = __shfl_sync(g, pos, leader);
+      pos += __popc(g & lanemask_lt());
+      uint4* dst = reinterpret_cast<uint4*>(sorted + off[a.w] + pos);
+      dst[0] = a;
+      dst[1] = b;
+    }
+  }
+}
+
+// Stage 4: per-tile MLP on tcgen05.  One CTA = 4 warps; each chunk is 128
+// samples of one tile.  A operands (gathered trilinear features + view
+// encoding, hidden activations) are written by the threads in the 128-byte
+// swizzled K-major layout; weights arrive by bulk copy (TMA) once per tile
+// change; accumulators live in tensor memory (H columns x 128 lanes).
+// Hidden layers: FP16 x FP16 -> FP32.  The last Linear (H -> 3) runs on
+// CUDA cores in FP32 from the accumulator registers.
+template <int F, int H, int L>
+__global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec* __restrict__ sorted, int* ctrl,
+                                                     int NT, const uint4* __restrict__ enc,
+                                                     const uint8_t* __restrict__ wimg, int img_stride, int img_bytes,
+                                                     float* rgb) {
+  constexpr int G = F / 8;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* A0 = base;
+  uint8_t* A1 = base + 16384;
+  uint8_t* Wsm = base + 32768;
+  const float* Wlast = reinterpret_cast<const float*>(Wsm + L * H * 128);
+  const float* bhid = Wlast + 3 * H;
+  const float* blast = bhid + L * H;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Wsm + ((img_bytes + 15) & ~15));
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
+  const uint32_t wbar = tc::smem_addr(bars), mbar = tc::smem_addr(bars + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    tc::mbar_init(wbar, 1);
+    tc::mbar_init(mbar, 1);
+    tc::fence_mbar_init();
+  }
+  for (int k = tid; k < 16384 / 16; k += blockDim.x) reinterpret_cast<uint4*>(A1)[k] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), H);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = tc::idesc_f16(H, 0);
+  const int* off = ctrl + CTRL_HEADER + NT;
+  const int* coff = off + NT + 1;
+  const int total_chunks = ctrl[CTRL_CHUNKS];
+  int cur_tile = -1;
+  uint32_t wphase = 0, mphase = 0;
+  bool failed = false;
+
+  for (;;) {
+    if (tid == 0) *chunk_slot = atomicAdd(ctrl + CTRL_WORK, 1);
+    __syncthreads();
+    const int c = *chunk_slot;
+    if (c >= total_chunks) break;
+    int lo = 0, hi = NT;  // largest t with coff[t] <= c
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (__ldg(coff + mid) <= c) lo = mid; else hi = mid;
+    }
+    const int tile = lo;
+    const int row0 = __ldg(off + tile) + (c - __ldg(coff + tile)) * 128;
+    const int cnt = min(128, __ldg(off + tile + 1) - row0);
+    const bool new_w = tile != cur_tile;
+    if (new_w && tid == 0) {
+      tc::mbar_arrive_expect_tx(wbar, (uint32_t)img_bytes);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)tile * img_stride, (uint32_t)img_bytes, wbar);
+    }
+    cur_tile = tile;
+
+    // gather: warp w fills rows 32w .. 32w+31, four rows in flight
+#pragma unroll 1
+    for (int rr = 0; rr < 32; rr += 4) {
+      uint4 ra[4], rb[4], fv[4], ev[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int r = warp * 32 + rr + j;
+        if (r < cnt) {
+          const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + r);
+          ra[j] = src[0];
+          rb[j] = src[1];
+        } else {
+          ra[j] = make_uint4(kInvalid, 0, 0, 0);
+          rb[j] = make_uint4(0, 0, 0, 0);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        fv[j] = make_uint4(0, 0, 0, 0);
+        ev[j] = make_uint4(0, 0, 0, 0);
+        if (ra[j].x != kInvalid) {
+          if (lane < 8 * G) {
+            int k = lane / G, g = lane % G;
+            fv[j] = __ldg(S.feat16 + ((size_t)ra[j].x * G + g) * 8 + k);
+          }
+          if (lane >= 16 && lane < 20) ev[j] = __ldg(enc + (size_t)ra[j].y * 4 + (lane - 16));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = warp * 32 + rr + j;
+        const int k = lane / G;
+        float fx = __uint_as_float(rb[j].x), fy = __uint_as_float(rb[j].y), fz = __uint_as_float(rb[j].z);
+        float wk = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
+        const __half2* hv = reinterpret_cast<const __half2*>(&fv[j]);
+        float acc[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float2 p = __half22float2(hv[q]);
+          acc[2 * q] = wk * p.x;
+          acc[2 * q + 1] = wk * p.y;
+        }
+#pragma unroll
+        for (int sh = G; sh < 8 * G; sh <<= 1)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[q] += __shfl_xor_sync(kFull, acc[q], sh);
+        if (lane < G) {
+          __align__(16) __half2 o[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) o[q] = __floats2half2_rn(acc[2 * q], acc[2 * q + 1]);
+          *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, lane)) = *reinterpret_cast<const uint4*>(o);
+        }
+        if (lane >= 16 && lane < 24) {
+          int ch = G + lane - 16;
+          if (ch < 8) *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = (ch - G < 4) ? ev[j] : make_uint4(0, 0, 0, 0);
+        }
+      }
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (new_w) {
+      bool ok = tc::mbar_wait(wbar, wphase);
+      wphase ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+    }
+
+    float v[H];
+#pragma unroll 1
+    for (int l = 0; l < L; ++l) {
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t a_base = tc::smem_addr(l == 0 ? A0 : A1);
+        const uint32_t b_base = tc::smem_addr(Wsm + l * H * 128);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), idesc, kk > 0);
+        tc::mma_commit(mbar);
+      }
+      bool ok = tc::mbar_wait(mbar, mphase);
+      mphase ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+      tc::fence_after_sync();
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+      for (int cc = 0; cc < H; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
+      tc::tmem_wait_ld();
+      const float* b = bhid + l * H;
+#pragma unroll
+      for (int j = 0; j < H; ++j) v[j] = fmaxf(v[j] + b[j], 0.0f);
+      if (l + 1 < L) {
+#pragma unroll
+        for (int ch = 0; ch < H / 8; ++ch) {
+          __align__(16) __half2 o[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) o[q] = __floats2half2_rn(v[8 * ch + 2 * q], v[8 * ch + 2 * q + 1]);
+          *reinterpret_cast<uint4*>(A1 + tc::sw128_offset(tid, ch)) = *reinterpret_cast<const uint4*>(o);
+        }
+        tc::fence_proxy_async();
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (failed) break;
+    if (tid < cnt) {
+      const uint4 ra = *reinterpret_cast<const uint4*>(sorted + row0 + tid);
+      const float wt = __uint_as_float(ra.z);
+#pragma unroll
+      for (int c3 = 0; c3 < 3; ++c3) {
+        float acc = blast[c3];
+#pragma unroll
+        for (int j = 0; j < H; ++j) acc = fmaf(Wlast[c3 * H + j], v[j], acc);
+        atomicAdd(rgb + 3 * (size_t)ra.y + c3, wt * sigmoidf_(acc));
+      }
+    }
+  }
+  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, H);
+}
+
+// Diagnostic: one 128 x N x 64 MMA through the same descriptors as the MLP
+// kernel.  A [128][64], B [N][64] row-major 16-bit, D [128][N] FP32.
+__global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const uint16_t* B, float* D, int N,
+                                                       int bf16, int* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* As = base;
+  uint8_t* Bs = base + 16384;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 16384 + 8192);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int c = 0; c < 8; ++c) {
+    *reinterpret_cast<uint4*>(As + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(A + tid * 64 + 8 * c);
+    if (tid < N)
+      *reinterpret_cast<uint4*>(Bs + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(B + tid * 64 + 8 * c);
+  }
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_addr(bar), 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(slot), 64);
+    tc::tmem_relinquish();
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *slot;
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_f16(N, bf16);
+    for (int kk = 0; kk < 4; ++kk)
+      tc::mma_f16(tmem, tc::sdesc_sw128(tc::smem_addr(As) + 32 * kk), tc::sdesc_sw128(tc::smem_addr(Bs) + 32 * kk),
+                  idesc, kk > 0);
+    tc::mma_commit(tc::smem_addr(bar));
+  }
+  bool ok = tc::mbar_wait(tc::smem_addr(bar), 0);
+  tc::fence_after_sync();
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) *status = 1;
+  } else {
+    float v[64];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int cc = 0; cc < N; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
+    tc::tmem_wait_ld();
+    for (int j = 0; j < N; ++j) D[tid * N + j] = v[j];
+    if (tid == 0) *status = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+inline int grid_for(int64_t n, int threads, int cap_blocks) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap_blocks) b = cap_blocks;
+  return (int)b;
+}
+
+template <int F, int H, int L>
+cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth, float* opac,
+                           cudaStream_t st) {
+  render_plain_kernel<F, H, L><<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, ws.ray_o, ws.ray_d, n, rgb, depth, opac);
+  return cudaGetLastError();
+}
+
+template <int F, int H, int L>
+cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num_sms, cudaStream_t st) {
+  const int smem = 1024 + 32768 + ((ws.wimg_bytes + 15) & ~15) + 64;
+  static bool configured = false;  // attribute set once per process (idempotent)
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_tc_kernel<F, H, L>, 128, smem);
+  if (e != cudaSuccess) return e;
+  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+  // each CTA holds H tensor-memory columns; keep the total within 512
+  while (per_sm * H > 512) --per_sm;
+  mlp_tc_kernel<F, H, L><<<num_sms * per_sm, 128, smem, st>>>(S, ws.sorted, ws.ctrl, S.num_tiles, ws.enc, ws.wimg,
+                                                             ws.wimg_stride, ws.wimg_bytes, rgb);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool mlp_shape_supported(int F, int H, int L) {
+  return (F == 16 && H == 32 && L == 2) || (F == 32 && H == 64 && L == 3) || (F == 16 && H == 64 && L == 3) ||
+         (F == 32 && H == 32 && L == 2);
+}
+
+int tc_image_bytes(int H, int L) { return L * H * 128 + (3 * H + L * H + 4) * 4; }
+
+cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* origins, const float* dirs, int64_t n,
+                          const Workspace& ws, bool want_enc, cudaStream_t st) {
+  CamDev c{};
+  if (cam) c = *cam;
+  raygen_kernel<<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, c, origins, dirs, n, ws.ray_o, ws.ray_d, ws.enc,
+                                                           want_enc ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t, int32_t* tri,
+                         cudaStream_t st) {
+  proxy_kernel<<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, origins, dirs, n, t, tri);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int K, int32_t* visited, int32_t* count,
+                         cudaStream_t st) {
+  trace_kernel<<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, ws.ray_o, ws.ray_d, n, K, visited, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
+                                float* opac, cudaStream_t st) {
+  const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
+  if (F == 16 && H == 32 && L == 2) return render_plain_t<16, 32, 2>(S, ws, n, rgb, depth, opac, st);
+  if (F == 32 && H == 64 && L == 3) return render_plain_t<32, 64, 3>(S, ws, n, rgb, depth, opac, st);
+  if (F == 16 && H == 64 && L == 3) return render_plain_t<16, 64, 3>(S, ws, n, rgb, depth, opac, st);
+  if (F == 32 && H == 32 && L == 2) return render_plain_t<32, 32, 2>(S, ws, n, rgb, depth, opac, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth, float* opac,
+                             int num_sms, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(ws.ctrl, 0, sizeof(int) * ws.ctrl_words, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(rgb, 0, sizeof(float) * 3 * n, st);
+  if (e != cudaSuccess) return e;
+  traverse_kernel<<<grid_for(n, kTravThreads, 1 << 24), kTravThreads, sizeof(uint32_t) * S.num_tiles, st>>>(
+      S, ws.ray_o, ws.ray_d, n, ws.recs, ws.cap, ws.ctrl, depth, opac);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  scatter_kernel<<<num_sms * 8, 256, 0, st>>>(ws.recs, ws.cap, ws.ctrl, S.num_tiles, ws.sorted);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
+  if (F == 16 && H == 32 && L == 2) return mlp_tc_t<16, 32, 2>(S, ws, rgb, num_sms, st);
+  if (F == 32 && H == 64 && L == 3) return mlp_tc_t<32, 64, 3>(S, ws, rgb, num_sms, st);
+  if (F == 16 && H == 64 && L == 3) return mlp_tc_t<16, 64, 3>(S, ws, rgb, num_sms, st);
+  if (F == 32 && H == 32 && L == 2) return mlp_tc_t<32, 32, 2>(S, ws, rgb, num_sms, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, cudaStream_t st) {
+  int* status = nullptr;
+  cudaError_t e = cudaMallocAsync(&status, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int smem = 1024 + 16384 + 8192 + 64;
+  e = cudaFuncSetAttribute(diag_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) {
+    diag_mma_kernel<<<1, 128, smem, st>>>(A, B, D, N, bf16, status);
+    e = cudaGetLastError();
+  }
+  int h = -1;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(status, st);
+  if (e == cudaSuccess && h != 0) e = cudaErrorLaunchTimeout;
+  return e;
+}
+
+}  // namespace snisr
