@@ -51,10 +51,11 @@ def test_diag_mma_fp16_bf16(cuda):
             B = torch.randn(N, 64, generator=g)
             dt = torch.bfloat16 if bf16 else torch.float16
             Ah, Bh = A.to(dt), B.to(dt)
+            # keep the device copies referenced for the duration of the call
+            Ad, Bd = Ah.cuda().view(torch.int16), Bh.cuda().view(torch.int16)
             D = torch.empty(128, N, device=cuda)
-            snisr._lib.check(snisr.lib().snisr_diag_mma(Ah.cuda().view(torch.int16).data_ptr(),
-                                                        Bh.cuda().view(torch.int16).data_ptr(), D.data_ptr(), N,
-                                                        bf16, torch.cuda.current_stream().cuda_stream))
+            snisr._lib.check(snisr.lib().snisr_diag_mma(Ad.data_ptr(), Bd.data_ptr(), D.data_ptr(), N, bf16,
+                                                        torch.cuda.current_stream().cuda_stream))
             ref = Ah.double() @ Bh.double().T
             err = (D.cpu().double() - ref).abs().max().item()
             assert err < 1e-4, (bf16, N, err)
