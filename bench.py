@@ -1,0 +1,357 @@
+"""Benchmark: Mrays/s of the sparse-voxel tile renderer on one GB300.
+
+Workload (one step = one full frame): the 1280x720 full-frame render of a
+4x4x1-tile scene (128^3 voxels per 3 m tile, FP16 32-dim corner features,
+per-tile MLP 59 -> 64x3 -> 3, ~207k-triangle proxy mesh in a BVH), cycling
+through 8 seeded interior camera poses.  Seeded synthetic data stands in for
+the reference's captured scenes, which are not distributed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device-timed throughput (CUDA events per step, L2 flushed between
+steps); `e2e` is the same metric through snisr_render_host (host output
+buffers, device->host copies inside the timed region).  With N > 1 (torchrun)
+every rank renders its own frames: rays are independent, so ranks are
+replicas with no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "scalable-neural-indoor-scene-rendering_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mrays/s render & fwd+bwd train, BF16-TC vs plain FP32 on GB300 @ RMSE≤1e-3"
+UNIT = "Mrays/s"
+WORKLOAD = ("cfg2 full-frame render 1280x720: 4x4x1 tiles of 128^3 over 3 m, ~3.7% occupied, FP16 32-dim "
+            "corner features, per-tile FP16 MLP 59-64x3-3, 207k-triangle proxy BVH, 8 seeded poses")
+MLP_FLOP_PER_SAMPLE = 2 * (59 * 64 + 64 * 64 + 64 * 64 + 64 * 3)  # 24,320
+GATHER_BYTES_PER_SAMPLE = 8 * (32 + 1) * 2                         # 528 (FP16 features + density)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(ws, v: float) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_run(synth, steps: int, target_s: float, threads: int):
+    """The reference's method as a scalar host path (the oracle port, FP32,
+    no proxy start as in the reference renderer), all host threads, on a
+    bounded random sample of each pose's pixels."""
+    import numpy as np
+
+    import oracle
+    osc = oracle.OracleScene(synth.desc)
+    cam = synth.camera(0)
+    d_all = oracle.camera_dirs(cam)
+    rng = np.random.default_rng(0)
+    # calibrate the sample so that all steps take about target_s seconds
+    probe = 4096
+    idx = rng.choice(d_all.shape[0], probe, replace=False)
+    d = np.ascontiguousarray(d_all[idx])
+    o = oracle.camera_origins(cam, probe)
+    t0 = time.perf_counter()
+    osc.render(o, d, None, 0, threads)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(d_all.shape[0], max(probe, rate * target_s / max(steps, 1))))
+    total_rays, total_t = 0, 0.0
+    for s in range(steps):
+        cam = synth.camera(s % synth.cfg.poses)
+        d_all = oracle.camera_dirs(cam)
+        idx = np.sort(rng.choice(d_all.shape[0], n, replace=False))
+        d = np.ascontiguousarray(d_all[idx])
+        o = oracle.camera_origins(cam, n)
+        t0 = time.perf_counter()
+        osc.render(o, d, None, 0, threads)
+        total_t += time.perf_counter() - t0
+        total_rays += n
+    return {"value": total_rays / total_t / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} random pixels per pose x {steps} poses of the 1280x720 frame, FP32 scalar oracle, "
+                      f"{threads} threads, rays start at the scene entry (no proxy mesh, as the reference renderer)"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import snisr
+    snisr.lib()
+    synth = snisr.SynthScene(snisr.CFG2)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        pass
+    cb = cpu_baseline_run(synth, args.steps, 20.0, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "scalar CPU path (oracle port of the reference method)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=24)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--max-samples-per-ray", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="only render a few frames of both forms (small workspace; for ncu captures)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import snisr
+    snisr.build()
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = snisr.CFG2
+    synth = snisr.SynthScene(cfg, max_samples_per_ray=args.max_samples_per_ray)
+    scene = snisr.Scene(synth.desc, local)
+    W, H = cfg.width, cfg.height
+    n = W * H
+    cams = [synth.camera((rank * 3 + p) % cfg.poses) for p in range(cfg.poses)]
+    stream = torch.cuda.current_stream()
+    out = (torch.empty(n, 3, device=dev), torch.empty(n, device=dev), torch.empty(n, device=dev))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    if args.profile_run:
+        for i in range(args.warmup + args.steps):
+            scene.render(cams[i % len(cams)], snisr.FORM_TC, out)
+        scene.render(cams[0], snisr.FORM_PLAIN_FP32, out)
+        scene.check()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": "ok", "frames": args.warmup + args.steps}))
+        scene.close()
+        return
+
+    def timed(form, steps, warmup):
+        for i in range(warmup):
+            scene.render(cams[i % len(cams)], form, out)
+        scene.check()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        _barrier(ws)
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            scene.render(cams[i % len(cams)], form, out)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        _barrier(ws)
+        scene.check()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    # headline: tensor-core batched form
+    with ClockSampler(local) as clk:
+        ms_tc = timed(snisr.FORM_TC, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_tc = _max_over_ranks(ws, ms_tc)
+    value = ws * n * args.steps / (ms_tc * 1e-3) / 1e6
+    # plain FP32 form (the >= 2x target's denominator)
+    ms_plain = _max_over_ranks(ws, timed(snisr.FORM_PLAIN_FP32, max(4, args.steps // 3), 3))
+    plain_value = ws * n * max(4, args.steps // 3) / (ms_plain * 1e-3) / 1e6
+
+    # stages and counters of the TC form, averaged over the poses
+    scene.set_profiling(True)
+    stage_sum = None
+    stats_sum = {"samples": 0, "voxel_steps": 0, "chunks": 0}
+    for i in range(len(cams)):
+        flush.zero_()
+        scene.render(cams[i], snisr.FORM_TC, out)
+        st = scene.stage_times()
+        stage_sum = st if stage_sum is None else [a + b for a, b in zip(stage_sum, st)]
+        fs = scene.frame_stats()
+        for k in stats_sum:
+            stats_sum[k] += fs[k]
+    scene.set_profiling(False)
+    npose = len(cams)
+    stages = dict(zip(["raygen_proxy", "traverse", "scan", "scatter", "mlp_tc", "total"],
+                      [round(v / npose, 4) for v in stage_sum]))
+    samples = stats_sum["samples"] / npose
+    vsteps = stats_sum["voxel_steps"] / npose
+    chunks = stats_sum["chunks"] / npose
+
+    hbm, tc_peak, peak_kind = _peaks()
+    # algorithmic work per launch (per frame)
+    img = 26128  # bytes of one tile's weight image
+    mlp_bytes = samples * (GATHER_BYTES_PER_SAMPLE + 32 + 64 + 12) + chunks * img
+    mlp_flop = samples * MLP_FLOP_PER_SAMPLE
+    trav_bytes = vsteps * 8 + samples * (32 + 32) + n * (32 + 8)
+    t_mlp = stages["mlp_tc"] * 1e-3
+    t_trav = stages["traverse"] * 1e-3
+    dom = "mlp_tc" if t_mlp >= t_trav else "traverse"
+    if dom == "mlp_tc":
+        f_hbm = mlp_bytes / t_mlp / 1e9 / hbm
+        f_tc = mlp_flop / t_mlp / 1e12 / tc_peak
+        if f_tc >= f_hbm:
+            roof = {"bound": "tensor", "achieved": mlp_flop / t_mlp / 1e12, "peak": tc_peak, "unit": "TFLOP/s"}
+        else:
+            roof = {"bound": "hbm", "achieved": mlp_bytes / t_mlp / 1e9, "peak": hbm, "unit": "GB/s"}
+    else:
+        roof = {"bound": "hbm", "achieved": trav_bytes / t_trav / 1e9, "peak": hbm, "unit": "GB/s"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["kernel"] = dom
+    roof["peak_source"] = f"{peak_kind} (MEASURED_PEAKS.json burst)" if peak_kind == "measured" else "fallback"
+    roof["traffic"] = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                tj = json.load(f)
+            roof["traffic"] = tj.get(dom)
+        except Exception:
+            pass
+    for k in ("achieved", "frac"):
+        roof[k] = round(roof[k], 4)
+
+    # end to end through the C ABI with host (pinned) output buffers
+    e2e = None
+    if not args.no_e2e:
+        rgb_h = torch.empty(n, 3, pin_memory=True)
+        dep_h = torch.empty(n, pin_memory=True)
+        op_h = torch.empty(n, pin_memory=True)
+        for i in range(3):
+            scene.render_host(cams[i], snisr.FORM_TC, rgb_h, dep_h, op_h)
+        _barrier(ws)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            scene.render_host(cams[i % len(cams)], snisr.FORM_TC, rgb_h, dep_h, op_h)
+        t_e2e = _max_over_ranks(ws, time.perf_counter() - t0)
+        _barrier(ws)
+        e2e = {"value": round(ws * n * args.steps / t_e2e / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 68, "d2h_bytes_per_step": n * 20,
+               "path": "snisr_render_host (camera by value -> device; rgb/depth/opacity -> pinned host)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_run(synth, 8, 15.0, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_tc / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "tensor-core batched (tcgen05 FP16, FP32 accumulate)",
+                       "l2": "flushed between steps (256 MB write)", "poses": cfg.poses,
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "fps": round(value / (n / 1e6) / ws, 2),
+            "plain_fp32": {"value": round(plain_value, 3), "unit": UNIT,
+                           "ms_per_step": round(ms_plain / max(4, args.steps // 3), 4)},
+            "speedup_vs_plain": round(value / plain_value, 3),
+            "stages_ms": stages,
+            "frame_counters": {"samples": int(samples), "voxel_steps": int(vsteps), "mlp_chunks": int(chunks)},
+            "roofline": roof,
+            "clocks": clocks,
+            "gpu_launches": 5 * args.steps,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    scene.close()
+
+
+if __name__ == "__main__":
+    main()

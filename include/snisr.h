@@ -269,6 +269,16 @@ snisr_status snisr_synth_camera(const snisr_synth_scene* s, uint64_t pose_seed,
                                 int32_t width, int32_t height, float fov_x_deg,
                                 snisr_camera* cam);
 
+/* Stage timing: when enabled, render calls record CUDA events between
+ * stages.  stage_times synchronises on the last frame and returns, in ms:
+ * TC form [ray setup + proxy, traverse, scan, scatter, MLP, total];
+ * plain form [ray setup + proxy, render, total]. */
+snisr_status snisr_scene_set_profiling(snisr_scene* scene, int32_t enable);
+snisr_status snisr_scene_stage_times(snisr_scene* scene, float* ms, int32_t cap, int32_t* n);
+/* Counters of the last TC-form frame (synchronises `stream`): out[0] samples,
+ * out[1] voxel DDA steps, out[2] sample slots reserved, out[3] MLP chunks. */
+snisr_status snisr_scene_frame_stats(snisr_scene* scene, int64_t* out, void* stream);
+
 /* Diagnostics: one 128 x N x 64 tcgen05 MMA (N = 32 or 64) through the
  * descriptors of the tensor-core MLP.  A [128][64], B [N][64] row-major FP16
  * (bf16 = 0) or BF16 (bf16 = 1) bit patterns, D [128][N] FP32 = A * B^T.

@@ -48,6 +48,9 @@ struct snisr_scene {
   int F = 0, H = 0, L = 0, NT = 0, in = 0, P = 0;
   uint32_t* err_host = nullptr;  // pinned mirror of the device error word
   const int32_t* corners = nullptr;  // [NVOX][8] vertex ids on the device
+  bool profiling = false;
+  int last_form = -1;
+  cudaEvent_t ev[8] = {};
   float* out_bufs = nullptr;          // staging for render_host
 };
 
@@ -90,6 +93,8 @@ void free_scene(snisr_scene* sc) {
   for (void* p : sc->allocs) cudaFree(p);
   if (sc->train_ws) cudaFree(sc->train_ws);
   if (sc->err_host) cudaFreeHost(sc->err_host);
+  for (cudaEvent_t e : sc->ev)
+    if (e) cudaEventDestroy(e);
   cudaSetDevice(prev);
   delete sc;
 }
@@ -238,11 +243,17 @@ snisr_status render_impl(snisr_scene* sc, const CamDev* cam, const float* origin
   if (form != SNISR_FORM_PLAIN_FP32 && form != SNISR_FORM_TC) return set_error(SNISR_INVALID_ARG, "render: bad form");
   DeviceGuard guard(sc->device);
   cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t* ev = sc->profiling ? sc->ev : nullptr;
+  if (ev) CUDA_TRY(cudaEventRecord(ev[5], st), "render: event");
   CUDA_TRY(launch_raygen(sc->S, cam, origins, dirs, n, sc->ws, form == SNISR_FORM_TC, st), "render: ray generation");
-  if (form == SNISR_FORM_PLAIN_FP32)
+  if (ev) CUDA_TRY(cudaEventRecord(ev[6], st), "render: event");
+  if (form == SNISR_FORM_PLAIN_FP32) {
     CUDA_TRY(launch_render_plain(sc->S, sc->ws, n, rgb, depth, opac, st), "render: plain kernel");
-  else
-    CUDA_TRY(launch_render_tc(sc->S, sc->ws, n, rgb, depth, opac, sc->num_sms, st), "render: batched kernels");
+    if (ev) CUDA_TRY(cudaEventRecord(ev[7], st), "render: event");
+  } else {
+    CUDA_TRY(launch_render_tc(sc->S, sc->ws, n, rgb, depth, opac, sc->num_sms, st, ev), "render: batched kernels");
+  }
+  sc->last_form = form;
   return SNISR_OK;
 }
 
@@ -541,6 +552,57 @@ snisr_status snisr_trace_voxels(snisr_scene* sc, const float* origins, const flo
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(launch_raygen(sc->S, nullptr, origins, dirs, n, sc->ws, false, st), "trace_voxels: ray setup");
   CUDA_TRY(launch_trace(sc->S, sc->ws, n, K, visited, count, st), "trace_voxels");
+  return SNISR_OK;
+}
+
+snisr_status snisr_scene_set_profiling(snisr_scene* sc, int32_t enable) {
+  if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;
+  DeviceGuard guard(sc->device);
+  if (enable && !sc->ev[0])
+    for (cudaEvent_t& e : sc->ev) CUDA_TRY(cudaEventCreate(&e), "set_profiling: event");
+  sc->profiling = enable != 0;
+  return SNISR_OK;
+}
+
+snisr_status snisr_scene_stage_times(snisr_scene* sc, float* ms, int32_t cap, int32_t* n_out) {
+  if (check_scene(sc) != SNISR_OK || !ms || !n_out) return set_error(SNISR_INVALID_ARG, "stage_times: null argument");
+  if (!sc->profiling || sc->last_form < 0) return set_error(SNISR_INVALID_ARG, "stage_times: profiling is off or nothing rendered");
+  DeviceGuard guard(sc->device);
+  float v[6] = {0, 0, 0, 0, 0, 0};
+  int n = 0;
+  auto el = [&](int a, int b) -> snisr_status {
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, sc->ev[a], sc->ev[b]), "stage_times");
+    v[n++] = t;
+    return SNISR_OK;
+  };
+  if (sc->last_form == SNISR_FORM_TC) {
+    CUDA_TRY(cudaEventSynchronize(sc->ev[4]), "stage_times");
+    snisr_status s;
+    if ((s = el(5, 6)) || (s = el(0, 1)) || (s = el(1, 2)) || (s = el(2, 3)) || (s = el(3, 4)) || (s = el(5, 4))) return s;
+  } else {
+    CUDA_TRY(cudaEventSynchronize(sc->ev[7]), "stage_times");
+    snisr_status s;
+    if ((s = el(5, 6)) || (s = el(6, 7)) || (s = el(5, 7))) return s;
+  }
+  for (int i = 0; i < n && i < cap; ++i) ms[i] = v[i];
+  *n_out = n;
+  return SNISR_OK;
+}
+
+snisr_status snisr_scene_frame_stats(snisr_scene* sc, int64_t* out, void* stream) {
+  if (check_scene(sc) != SNISR_OK || !out) return set_error(SNISR_INVALID_ARG, "frame_stats: null argument");
+  DeviceGuard guard(sc->device);
+  int32_t w[6];
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemcpyAsync(w, sc->ws.ctrl, sizeof(w), cudaMemcpyDeviceToHost, st), "frame_stats");
+  CUDA_TRY(cudaStreamSynchronize(st), "frame_stats");
+  uint64_t steps;
+  std::memcpy(&steps, w + CTRL_STEPS, 8);
+  out[0] = w[CTRL_SAMPLES];
+  out[1] = (int64_t)steps;
+  out[2] = w[CTRL_RESERVED];
+  out[3] = w[CTRL_CHUNKS];
   return SNISR_OK;
 }
 

@@ -89,6 +89,7 @@ struct RayState {
   uint32_t rec;
   float z;         // next sample position (relative to t_in)
   bool in_voxel;
+  uint32_t steps;  // voxel cells examined (for traffic accounting)
 
   __device__ bool init(const SceneDev& S, const float* oo, const float* dd, float ts) {
     for (int a = 0; a < 3; ++a) { o[a] = oo[a]; d[a] = dd[a]; }
@@ -96,6 +97,7 @@ struct RayState {
     tile = -1;
     in_voxel = false;
     tile_live = false;
+    steps = 0;
     const int g[3] = {S.gx, S.gy, S.gz};
     float size[3], half[3], cen[3];
     for (int a = 0; a < 3; ++a) {
@@ -162,14 +164,27 @@ struct RayState {
     return (m[1] < m[2]) ? 1 : 2;
   }
 
+  template <int A>
+  __device__ __forceinline__ bool tile_axis_step(int g) {
+    tc[A] += tstep[A];
+    tmax[A] = fadd(tmax[A], tdelta[A]);
+    return tc[A] >= 0 && tc[A] < g;
+  }
   // Advances the tile DDA to the next tile; false when it leaves the grid.
+  // Same axis choice as dda_axis(), written with compile-time indices so the
+  // state stays in registers.
   __device__ bool step_tile(const SceneDev& S) {
-    int a = dda_axis(tmax);
-    tc[a] += tstep[a];
-    tmax[a] = fadd(tmax[a], tdelta[a]);
-    const int g[3] = {S.gx, S.gy, S.gz};
-    if (tc[a] < 0 || tc[a] >= g[a]) { tile_live = false; return false; }
-    return true;
+    bool in;
+    if (tmax[0] < tmax[1]) in = (tmax[0] < tmax[2]) ? tile_axis_step<0>(S.gx) : tile_axis_step<2>(S.gz);
+    else in = (tmax[1] < tmax[2]) ? tile_axis_step<1>(S.gy) : tile_axis_step<2>(S.gz);
+    if (!in) tile_live = false;
+    return in;
+  }
+  template <int A>
+  __device__ __forceinline__ bool voxel_axis_step(int N) {
+    vc[A] += vstep[A];
+    vmax[A] = fadd(vmax[A], vdelta[A]);
+    return vc[A] >= 0 && vc[A] < N;
   }
 
   // Moves to the next occupied voxel along the ray, crossing tiles as
@@ -185,6 +200,7 @@ struct RayState {
         pending_tile = false;
         if (!open_tile(S)) continue;
         // the entry voxel of the freshly opened tile
+        ++steps;
         far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
         int vid = (vc[0] * N + vc[1]) * N + vc[2];
         uint32_t r;
@@ -193,11 +209,12 @@ struct RayState {
           return true;
         }
       }
-      int a = dda_axis(vmax);
-      vc[a] += vstep[a];
-      vmax[a] = fadd(vmax[a], vdelta[a]);
+      bool in;
+      if (vmax[0] < vmax[1]) in = (vmax[0] < vmax[2]) ? voxel_axis_step<0>(N) : voxel_axis_step<2>(N);
+      else in = (vmax[1] < vmax[2]) ? voxel_axis_step<1>(N) : voxel_axis_step<2>(N);
       near_ = far_;
-      if (vc[a] < 0 || vc[a] >= N) { tile = -1; continue; }
+      if (!in) { tile = -1; continue; }
+      ++steps;
       far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
       if (!block_occupied(S, tile, vc[0] >> 2, vc[1] >> 2, vc[2] >> 2)) continue;
       int vid = (vc[0] * N + vc[1]) * N + vc[2];

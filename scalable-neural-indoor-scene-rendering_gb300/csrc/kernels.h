@@ -39,8 +39,10 @@ cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* ori
                           int64_t n, const Workspace& ws, bool want_enc, cudaStream_t st);
 cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
                                 float* opac, cudaStream_t st);
+// ev (optional, 5 events): recorded before traverse, after traverse, scan,
+// scatter and the MLP.
 cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
-                             float* opac, int num_sms, cudaStream_t st);
+                             float* opac, int num_sms, cudaStream_t st, cudaEvent_t* ev = nullptr);
 cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int K, int32_t* visited,
                          int32_t* count, cudaStream_t st);
 cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t,

@@ -15,6 +15,19 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 
+// {lo, hi} -> packed FP16 pair (round to nearest)
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+// {max(lo,0), max(hi,0)} -> packed FP16 pair
+__device__ __forceinline__ uint32_t pack_relu_h2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -284,6 +297,10 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, cons
     depth[i] = D;
     opac[i] = 1.0f - T;
   }
+  unsigned long long st = (i < n) ? R.steps : 0u;
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) st += __shfl_xor_sync(kFull, st, sh);
+  if (lane == 0 && st) atomicAdd(reinterpret_cast<unsigned long long*>(ctrl + CTRL_STEPS), st);
   __syncthreads();
   for (int t = threadIdx.x; t < S.num_tiles; t += blockDim.x)
     if (hist[t]) atomicAdd(ctrl + CTRL_HEADER + t, (int)hist[t]);
@@ -413,62 +430,58 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
     }
     cur_tile = tile;
 
-    // gather: warp w fills rows 32w .. 32w+31, four rows in flight
-#pragma unroll 1
-    for (int rr = 0; rr < 32; rr += 4) {
-      uint4 ra[4], rb[4], fv[4], ev[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        int r = warp * 32 + rr + j;
-        if (r < cnt) {
-          const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + r);
-          ra[j] = src[0];
-          rb[j] = src[1];
-        } else {
-          ra[j] = make_uint4(kInvalid, 0, 0, 0);
-          rb[j] = make_uint4(0, 0, 0, 0);
-        }
+    // gather: lane = row.  Each lane reads its sample's 8-corner FP16 record
+    // (G x 8 x 16 bytes, one voxel), interpolates in FP32 and writes the
+    // swizzled A row: chunks [0,G) features, [G,G+4) view encoding, rest 0.
+    {
+      const int r = tid;
+      uint4 ra = make_uint4(kInvalid, 0, 0, 0), rb = make_uint4(0, 0, 0, 0);
+      if (r < cnt) {
+        const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + r);
+        ra = src[0];
+        rb = src[1];
       }
+      uint8_t* arow = A0;
+      if (ra.x != kInvalid) {
+        const float fx = __uint_as_float(rb.x), fy = __uint_as_float(rb.y), fz = __uint_as_float(rb.z);
+        float w[8];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        fv[j] = make_uint4(0, 0, 0, 0);
-        ev[j] = make_uint4(0, 0, 0, 0);
-        if (ra[j].x != kInvalid) {
-          if (lane < 8 * G) {
-            int k = lane / G, g = lane % G;
-            fv[j] = __ldg(S.feat16 + ((size_t)ra[j].x * G + g) * 8 + k);
+        for (int k = 0; k < 8; ++k)
+          w[k] = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
+        const uint4* fp = S.feat16 + (size_t)ra.x * G * 8;
+        uint4 ev[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ev[j] = __ldg(enc + (size_t)ra.y * 4 + j);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          uint4 cv[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) cv[k] = __ldg(fp + g * 8 + k);
+          float acc[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const __half2* hv = reinterpret_cast<const __half2*>(&cv[k]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float2 p = __half22float2(hv[q]);
+              acc[2 * q] = fmaf(w[k], p.x, acc[2 * q]);
+              acc[2 * q + 1] = fmaf(w[k], p.y, acc[2 * q + 1]);
+            }
           }
-          if (lane >= 16 && lane < 20) ev[j] = __ldg(enc + (size_t)ra[j].y * 4 + (lane - 16));
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int r = warp * 32 + rr + j;
-        const int k = lane / G;
-        float fx = __uint_as_float(rb[j].x), fy = __uint_as_float(rb[j].y), fz = __uint_as_float(rb[j].z);
-        float wk = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
-        const __half2* hv = reinterpret_cast<const __half2*>(&fv[j]);
-        float acc[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float2 p = __half22float2(hv[q]);
-          acc[2 * q] = wk * p.x;
-          acc[2 * q + 1] = wk * p.y;
+          uint4 o;
+          o.x = pack_h2(acc[0], acc[1]); o.y = pack_h2(acc[2], acc[3]);
+          o.z = pack_h2(acc[4], acc[5]); o.w = pack_h2(acc[6], acc[7]);
+          *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, g)) = o;
         }
 #pragma unroll
-        for (int sh = G; sh < 8 * G; sh <<= 1)
+        for (int j = 0; j < 4; ++j) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, G + j)) = ev[j];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) acc[q] += __shfl_xor_sync(kFull, acc[q], sh);
-        if (lane < G) {
-          __align__(16) __half2 o[4];
+        for (int ch = G + 4; ch < 8; ++ch) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
+      } else {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) o[q] = __floats2half2_rn(acc[2 * q], acc[2 * q + 1]);
-          *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, lane)) = *reinterpret_cast<const uint4*>(o);
-        }
-        if (lane >= 16 && lane < 24) {
-          int ch = G + lane - 16;
-          if (ch < 8) *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = (ch - G < 4) ? ev[j] : make_uint4(0, 0, 0, 0);
-        }
+        for (int ch = 0; ch < 8; ++ch) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
       }
     }
     tc::fence_proxy_async();
@@ -501,16 +514,21 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
       tc::tmem_wait_ld();
       const float* b = bhid + l * H;
 #pragma unroll
-      for (int j = 0; j < H; ++j) v[j] = fmaxf(v[j] + b[j], 0.0f);
+      for (int j = 0; j < H; ++j) v[j] += b[j];
       if (l + 1 < L) {
 #pragma unroll
         for (int ch = 0; ch < H / 8; ++ch) {
-          __align__(16) __half2 o[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) o[q] = __floats2half2_rn(v[8 * ch + 2 * q], v[8 * ch + 2 * q + 1]);
-          *reinterpret_cast<uint4*>(A1 + tc::sw128_offset(tid, ch)) = *reinterpret_cast<const uint4*>(o);
+          uint4 o;
+          o.x = pack_relu_h2(v[8 * ch + 0], v[8 * ch + 1]);
+          o.y = pack_relu_h2(v[8 * ch + 2], v[8 * ch + 3]);
+          o.z = pack_relu_h2(v[8 * ch + 4], v[8 * ch + 5]);
+          o.w = pack_relu_h2(v[8 * ch + 6], v[8 * ch + 7]);
+          *reinterpret_cast<uint4*>(A1 + tc::sw128_offset(tid, ch)) = o;
         }
         tc::fence_proxy_async();
+      } else {
+#pragma unroll
+        for (int j = 0; j < H; ++j) v[j] = fmaxf(v[j], 0.0f);
       }
       tc::fence_before_sync();
       __syncthreads();
@@ -608,6 +626,9 @@ cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
     configured = true;
   }
   int per_sm = 0;
@@ -662,24 +683,31 @@ cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t 
 }
 
 cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth, float* opac,
-                             int num_sms, cudaStream_t st) {
+                             int num_sms, cudaStream_t st, cudaEvent_t* ev) {
   cudaError_t e = cudaMemsetAsync(ws.ctrl, 0, sizeof(int) * ws.ctrl_words, st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(rgb, 0, sizeof(float) * 3 * n, st);
   if (e != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
   traverse_kernel<<<grid_for(n, kTravThreads, 1 << 24), kTravThreads, sizeof(uint32_t) * S.num_tiles, st>>>(
       S, ws.ray_o, ws.ray_d, n, ws.recs, ws.cap, ws.ctrl, depth, opac);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
   scatter_kernel<<<num_sms * 8, 256, 0, st>>>(ws.recs, ws.cap, ws.ctrl, S.num_tiles, ws.sorted);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[3], st)) != cudaSuccess) return e;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
-  if (F == 16 && H == 32 && L == 2) return mlp_tc_t<16, 32, 2>(S, ws, rgb, num_sms, st);
-  if (F == 32 && H == 64 && L == 3) return mlp_tc_t<32, 64, 3>(S, ws, rgb, num_sms, st);
-  if (F == 16 && H == 64 && L == 3) return mlp_tc_t<16, 64, 3>(S, ws, rgb, num_sms, st);
-  if (F == 32 && H == 32 && L == 2) return mlp_tc_t<32, 32, 2>(S, ws, rgb, num_sms, st);
-  return cudaErrorInvalidValue;
+  if (F == 16 && H == 32 && L == 2) e = mlp_tc_t<16, 32, 2>(S, ws, rgb, num_sms, st);
+  else if (F == 32 && H == 64 && L == 3) e = mlp_tc_t<32, 64, 3>(S, ws, rgb, num_sms, st);
+  else if (F == 16 && H == 64 && L == 3) e = mlp_tc_t<16, 64, 3>(S, ws, rgb, num_sms, st);
+  else if (F == 32 && H == 32 && L == 2) e = mlp_tc_t<32, 32, 2>(S, ws, rgb, num_sms, st);
+  else e = cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[4], st)) != cudaSuccess) return e;
+  return cudaSuccess;
 }
 
 cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, cudaStream_t st) {

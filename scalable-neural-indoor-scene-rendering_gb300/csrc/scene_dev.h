@@ -63,6 +63,7 @@ enum : int {
   CTRL_WORK = 1,       // MLP work-queue head
   CTRL_CHUNKS = 2,     // total 128-sample chunks
   CTRL_SAMPLES = 3,    // total valid samples
+  CTRL_STEPS = 4,      // u64 (words 4-5): voxel DDA steps of the frame
   CTRL_HEADER = 8,     // per-tile arrays follow: count, offset, chunk offset, cursor
 };
 

@@ -115,6 +115,21 @@ class Scene:
     def check(self, stream=None):
         _lib.check(_lib.lib().snisr_scene_check(self._h, _stream(stream)))
 
+    def set_profiling(self, enable: bool):
+        _lib.check(_lib.lib().snisr_scene_set_profiling(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        """Per-stage ms of the last frame (see snisr_scene_stage_times)."""
+        buf = (C.c_float * 8)()
+        n = C.c_int32()
+        _lib.check(_lib.lib().snisr_scene_stage_times(self._h, buf, 8, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def frame_stats(self, stream=None):
+        out = (C.c_int64 * 4)()
+        _lib.check(_lib.lib().snisr_scene_frame_stats(self._h, out, _stream(stream)))
+        return {"samples": out[0], "voxel_steps": out[1], "reserved": out[2], "chunks": out[3]}
+
     def render(self, cam: _lib.Camera, form: int = _lib.FORM_TC, out=None, stream=None):
         import torch
         n = cam.width * cam.height
