@@ -66,6 +66,9 @@ def lib() -> C.CDLL:
             "oracle_voxel_traversal": (C.c_int, [P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float]),
             "oracle_ray_triangle_onesided": (C.c_float, [P, P, P, P, P]),
             "oracle_trilinear_base": (None, [P, C.c_int, C.c_int, C.c_int, P, P]),
+            "oracle_volume_rendering": (None, [P, P, P, C.c_int64, C.c_int, C.c_float, P, P, P]),
+            "oracle_positional_encoding": (None, [P, C.c_int64, C.c_int, P]),
+            "oracle_grid_sample": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -174,3 +177,32 @@ def op_integrate(rgba, dz, early, frame, trans):
     n = frame.shape[0]
     lib().oracle_op_integrate(_p(rgba), _p(dz), n, early, _p(frame), _p(trans))
     return frame, trans
+
+
+def volume_rendering(rgb, sigma, dists, init_T=1.0):
+    """rgb [B,ns,3], sigma/dists [B,ns] float32 -> out [B,3], T [B,ns], alpha [B,ns] (float64)."""
+    B, ns = sigma.shape
+    out = np.zeros((B, 3))
+    trans = np.zeros((B, ns))
+    alpha = np.zeros((B, ns))
+    lib().oracle_volume_rendering(_p(np.ascontiguousarray(rgb, np.float32)), _p(np.ascontiguousarray(sigma, np.float32)),
+                                  _p(np.ascontiguousarray(dists, np.float32)), B, ns, init_T, _p(out), _p(trans),
+                                  _p(alpha))
+    return out, trans, alpha
+
+
+def positional_encoding(x, L):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros((x.shape[0], 3 + 6 * L))
+    lib().oracle_positional_encoding(_p(x), x.shape[0], L, _p(out))
+    return out
+
+
+def grid_sample(vol, idx):
+    """vol [C,D,H,W] float32, idx [n,3] (x,y,z) index-space points -> [n,C] float64."""
+    vol = np.ascontiguousarray(vol, np.float32)
+    idx = np.ascontiguousarray(idx, np.float32)
+    C_, D, H, W = vol.shape
+    out = np.zeros((idx.shape[0], C_))
+    lib().oracle_grid_sample(_p(vol), C_, D, H, W, _p(idx), idx.shape[0], _p(out))
+    return out

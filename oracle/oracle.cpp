@@ -715,6 +715,65 @@ void oracle_op_integrate(const float* rgba, const float* dz, int64_t npix, float
   }
 }
 
+// Compositing of the training graph (training/scripts/utils.py:823-837):
+// alpha = 1 - exp(-sigma*dist); T = cumprod([init_T, 1 - alpha + 1e-10])[:-1];
+// out = sum(alpha * T * rgb).  Double precision.
+void oracle_volume_rendering(const float* rgb, const float* sigma, const float* dists, int64_t B, int ns, float init_T,
+                             double* out, double* trans, double* alpha) {
+  for (int64_t b = 0; b < B; ++b) {
+    double T = init_T, c[3] = {0, 0, 0};
+    for (int i = 0; i < ns; ++i) {
+      int64_t k = b * ns + i;
+      double a = 1.0 - std::exp(-(double)sigma[k] * (double)dists[k]);
+      alpha[k] = a;
+      trans[k] = T;
+      for (int j = 0; j < 3; ++j) c[j] += a * T * (double)rgb[3 * k + j];
+      T *= (1.0 - a + 1e-10);
+    }
+    for (int j = 0; j < 3; ++j) out[3 * b + j] = c[j];
+  }
+}
+
+// Positional encoding [x, sin(2^i x), cos(2^i x)] (training/scripts/networks.py:4-15),
+// applied to n 3-vectors with L frequencies; out [n][3 + 6L].  Double precision.
+void oracle_positional_encoding(const float* x, int64_t n, int L, double* out) {
+  const int W = 3 + 6 * L;
+  for (int64_t i = 0; i < n; ++i) {
+    double* o = out + i * W;
+    for (int a = 0; a < 3; ++a) o[a] = x[3 * i + a];
+    for (int l = 0; l < L; ++l) {
+      double sc = std::ldexp(1.0, l);
+      for (int a = 0; a < 3; ++a) {
+        o[3 + 6 * l + a] = std::sin(sc * (double)x[3 * i + a]);
+        o[3 + 6 * l + 3 + a] = std::cos(sc * (double)x[3 * i + a]);
+      }
+    }
+  }
+}
+
+// Trilinear lookup of query_voxel (training/scripts/tile/tile.py:225-236):
+// grid_sample(align_corners=True, zeros padding) of a [C][D][H][W] volume
+// (x indexes W) at index-space points (x - min_corner)/voxel - 0.5.
+void oracle_grid_sample(const float* vol, int C, int D, int H, int W, const float* idx, int64_t n, double* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    double p[3] = {idx[3 * i], idx[3 * i + 1], idx[3 * i + 2]};  // (x->W, y->H, z->D)
+    int i0[3];
+    double f[3];
+    for (int a = 0; a < 3; ++a) { double fl = std::floor(p[a]); i0[a] = (int)fl; f[a] = p[a] - fl; }
+    for (int c = 0; c < C; ++c) {
+      double acc = 0;
+      for (int k = 0; k < 8; ++k) {
+        int dx = (k >> 2) & 1, dy = (k >> 1) & 1, dz = k & 1;
+        int x = i0[0] + dx, y = i0[1] + dy, z = i0[2] + dz;
+        if (x < 0 || x >= W || y < 0 || y >= H || z < 0 || z >= D) continue;
+        double w = (dx ? f[0] : 1 - f[0]) * (dy ? f[1] : 1 - f[1]) * (dz ? f[2] : 1 - f[2]);
+        acc += w * (double)vol[(((int64_t)c * D + z) * H + y) * W + x];
+      }
+      out[i * C + c] = acc;
+    }
+  }
+}
+
 // Pieces exposed for the reference-harness cross-check.
 void oracle_ray_aabb(const float* o, const float* d, const float* c, float h, float* out) {
   const float hh[3] = {h, h, h};

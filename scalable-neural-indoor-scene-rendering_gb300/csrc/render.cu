@@ -369,16 +369,15 @@ __global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap,
 // Hidden layers: FP16 x FP16 -> FP32.  The last Linear (H -> 3) runs on
 // CUDA cores in FP32 from the accumulator registers.
 template <int F, int H, int L>
-__global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec* __restrict__ sorted, int* ctrl,
+__global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const SampleRec* __restrict__ sorted, int* ctrl,
                                                      int NT, const uint4* __restrict__ enc,
                                                      const uint8_t* __restrict__ wimg, int img_stride, int img_bytes,
                                                      float* rgb) {
   constexpr int G = F / 8;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* A0 = base;
-  uint8_t* A1 = base + 16384;
-  uint8_t* Wsm = base + 32768;
+  uint8_t* A0 = base;            // layer input: features+encoding, then hidden activations
+  uint8_t* Wsm = base + 16384;
   const float* Wlast = reinterpret_cast<const float*>(Wsm + L * H * 128);
   const float* bhid = Wlast + 3 * H;
   const float* blast = bhid + L * H;
@@ -393,7 +392,6 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
     tc::mbar_init(mbar, 1);
     tc::fence_mbar_init();
   }
-  for (int k = tid; k < 16384 / 16; k += blockDim.x) reinterpret_cast<uint4*>(A1)[k] = make_uint4(0, 0, 0, 0);
   if (warp == 0) {
     tc::tmem_alloc(tc::smem_addr(tmem_slot), H);
     tc::tmem_relinquish();
@@ -492,15 +490,15 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
       if (__syncthreads_or(!ok)) { failed = true; break; }
     }
 
-    float v[H];
+    float out3[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
     for (int l = 0; l < L; ++l) {
       if (tid == 0) {
         tc::fence_after_sync();
-        const uint32_t a_base = tc::smem_addr(l == 0 ? A0 : A1);
+        const uint32_t a_base = tc::smem_addr(A0);
         const uint32_t b_base = tc::smem_addr(Wsm + l * H * 128);
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
+        const int ksteps = l == 0 ? 4 : H / 16;  // K = 64 (padded input) or H
+        for (int kk = 0; kk < ksteps; ++kk)
           tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), idesc, kk > 0);
         tc::mma_commit(mbar);
       }
@@ -509,26 +507,44 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
       if (__syncthreads_or(!ok)) { failed = true; break; }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-      for (int cc = 0; cc < H; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
-      tc::tmem_wait_ld();
       const float* b = bhid + l * H;
-#pragma unroll
-      for (int j = 0; j < H; ++j) v[j] += b[j];
       if (l + 1 < L) {
+        // bias + ReLU + FP16 pack of 32 columns at a time into the A tile
 #pragma unroll
-        for (int ch = 0; ch < H / 8; ++ch) {
-          uint4 o;
-          o.x = pack_relu_h2(v[8 * ch + 0], v[8 * ch + 1]);
-          o.y = pack_relu_h2(v[8 * ch + 2], v[8 * ch + 3]);
-          o.z = pack_relu_h2(v[8 * ch + 4], v[8 * ch + 5]);
-          o.w = pack_relu_h2(v[8 * ch + 6], v[8 * ch + 7]);
-          *reinterpret_cast<uint4*>(A1 + tc::sw128_offset(tid, ch)) = o;
+        for (int half = 0; half < H / 32; ++half) {
+          float v[32];
+          tc::tmem_ld16(taddr + 32 * half, v);
+          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c0 = 32 * half + 8 * q;
+            uint4 o;
+            o.x = pack_relu_h2(v[8 * q + 0] + b[c0 + 0], v[8 * q + 1] + b[c0 + 1]);
+            o.y = pack_relu_h2(v[8 * q + 2] + b[c0 + 2], v[8 * q + 3] + b[c0 + 3]);
+            o.z = pack_relu_h2(v[8 * q + 4] + b[c0 + 4], v[8 * q + 5] + b[c0 + 5]);
+            o.w = pack_relu_h2(v[8 * q + 6] + b[c0 + 6], v[8 * q + 7] + b[c0 + 7]);
+            *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(tid, 4 * half + q)) = o;
+          }
         }
         tc::fence_proxy_async();
       } else {
+        // last hidden layer: bias + ReLU in FP32, then the H -> 3 Linear
+        out3[0] = blast[0]; out3[1] = blast[1]; out3[2] = blast[2];
 #pragma unroll
-        for (int j = 0; j < H; ++j) v[j] = fmaxf(v[j], 0.0f);
+        for (int half = 0; half < H / 32; ++half) {
+          float v[32];
+          tc::tmem_ld16(taddr + 32 * half, v);
+          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float h = fmaxf(v[j] + b[32 * half + j], 0.0f);
+            out3[0] = fmaf(Wlast[32 * half + j], h, out3[0]);
+            out3[1] = fmaf(Wlast[H + 32 * half + j], h, out3[1]);
+            out3[2] = fmaf(Wlast[2 * H + 32 * half + j], h, out3[2]);
+          }
+        }
       }
       tc::fence_before_sync();
       __syncthreads();
@@ -538,12 +554,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(SceneDev S, const SampleRec
       const uint4 ra = *reinterpret_cast<const uint4*>(sorted + row0 + tid);
       const float wt = __uint_as_float(ra.z);
 #pragma unroll
-      for (int c3 = 0; c3 < 3; ++c3) {
-        float acc = blast[c3];
-#pragma unroll
-        for (int j = 0; j < H; ++j) acc = fmaf(Wlast[c3 * H + j], v[j], acc);
-        atomicAdd(rgb + 3 * (size_t)ra.y + c3, wt * sigmoidf_(acc));
-      }
+      for (int c3 = 0; c3 < 3; ++c3) atomicAdd(rgb + 3 * (size_t)ra.y + c3, wt * sigmoidf_(out3[c3]));
     }
   }
   if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
@@ -621,22 +632,27 @@ cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, fl
 
 template <int F, int H, int L>
 cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num_sms, cudaStream_t st) {
-  const int smem = 1024 + 32768 + ((ws.wimg_bytes + 15) & ~15) + 64;
-  static bool configured = false;  // attribute set once per process (idempotent)
-  if (!configured) {
+  const int smem = 1024 + 16384 + ((ws.wimg_bytes + 15) & ~15) + 64;
+  static int per_sm = 0;  // resident CTAs per SM, computed once per process
+  if (per_sm == 0) {
     cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
-    configured = true;
+    int dev = 0, smem_sm = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaFuncAttributes fa{};
+    e = cudaFuncGetAttributes(&fa, mlp_tc_kernel<F, H, L>);
+    if (e != cudaSuccess) return e;
+    const int regs_cta = ((fa.numRegs + 7) & ~7) * 128;
+    int n = smem_sm / (smem + reserved);
+    n = min(n, 65536 / max(regs_cta, 1));
+    n = min(n, 512 / H);  // tensor-memory columns per SM
+    per_sm = max(1, min(n, 8));
   }
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_tc_kernel<F, H, L>, 128, smem);
-  if (e != cudaSuccess) return e;
-  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
-  // each CTA holds H tensor-memory columns; keep the total within 512
-  while (per_sm * H > 512) --per_sm;
   mlp_tc_kernel<F, H, L><<<num_sms * per_sm, 128, smem, st>>>(S, ws.sorted, ws.ctrl, S.num_tiles, ws.enc, ws.wimg,
                                                              ws.wimg_stride, ws.wimg_bytes, rgb);
   return cudaGetLastError();
