@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
             "oracle_volume_rendering": (None, [P, P, P, C.c_int64, C.c_int, C.c_float, P, P, P]),
             "oracle_positional_encoding": (None, [P, C.c_int64, C.c_int, P]),
             "oracle_grid_sample": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]),
+            "oracle_train_forward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, C.c_int]),
+            "oracle_train_backward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -117,6 +119,30 @@ class OracleScene:
         cnt = np.zeros(n, np.int32)
         lib().oracle_trace(self._h, _p(o), _p(d), _p(t_start), n, K, _p(vis), _p(cnt), nthreads or threads())
         return vis, cnt
+
+    def train_forward(self, vfeat, vdens, mlp, o, d, ray_tile, nthreads: int | None = None):
+        """FP64 colours [n,3] and sample counts [n] of ray segments (ray i inside tile ray_tile[i])."""
+        n = o.shape[0]
+        rgb = np.zeros((n, 3))
+        cnt = np.zeros(n, np.int32)
+        args = [np.ascontiguousarray(a, np.float32) for a in (vfeat, vdens, mlp)]
+        rt = np.ascontiguousarray(ray_tile, np.int32)
+        lib().oracle_train_forward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(rgb), _p(cnt),
+                                   nthreads or threads())
+        return rgb, cnt
+
+    def train_backward(self, vfeat, vdens, mlp, o, d, ray_tile, grad_rgb):
+        """FP64 gradients of sum(grad_rgb * rgb): (d vfeat, d vdens, d mlp)."""
+        n = o.shape[0]
+        args = [np.ascontiguousarray(a, np.float32) for a in (vfeat, vdens, mlp)]
+        gF = np.zeros(args[0].shape)
+        gG = np.zeros(args[1].shape)
+        gW = np.zeros(args[2].shape)
+        rt = np.ascontiguousarray(ray_tile, np.int32)
+        g = np.ascontiguousarray(grad_rgb, np.float64)
+        lib().oracle_train_backward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(g), _p(gF), _p(gG),
+                                    _p(gW))
+        return gF, gG, gW
 
     def render(self, o, d, t_start, form: int, nthreads: int | None = None):
         """form: 0 plain FP32, 1 FP64, 2 tensor-core emulation (FP16 MLP inputs, FP64 math)."""

@@ -535,6 +535,176 @@ void oracle_render(const oracle_scene* os, const float* o, const float* d, const
 }
 
 // ---------------------------------------------------------------------------
+// Training: forward and adjoint of one ray segment inside one tile, FP64.
+// Replaces the autograd graph of Tile.train_batch (training/scripts/tile/
+// tile.py:667-704: sparse sampling, query_voxel, volume_rendering) for the
+// per-corner feature model: rgb = sigmoid(MLP([trilinear F, enc(d)])),
+// sigma = softplus(trilinear G), alpha = 1 - exp(-sigma * delta / voxel).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+namespace {
+struct TrainSample {
+  int32_t corners[8];
+  double w[8];
+  double s;            // density logit
+  double sigma, alpha, T, dv;  // dv = delta / voxel
+  double c[3];
+  std::vector<double> x;             // MLP input
+  std::vector<std::vector<double>> h;  // hidden activations (post-ReLU)
+};
+
+// Occupied-voxel segments of a ray inside one tile (no tile DDA): the tile's
+// own slab clip and voxel DDA, as in march().
+template <class Visit>
+void march_one_tile(const Scene& s, int id, const float o[3], const float d[3], Visit&& visit) {
+  float c[3], h[3];
+  for (int a = 0; a < 3; ++a) { c[a] = s.centers[(size_t)id * 3 + a]; h[a] = s.tile * 0.5f; }
+  Bound tb = ray_aabb(o, d, c, h);
+  if (tb.lo == -1.0f || !(tb.lo < tb.hi)) return;
+  const float ti = tb.lo;
+  const int N = s.N;
+  float q[3], vmax[3], vdel[3];
+  int vc[3], vs[3];
+  for (int a = 0; a < 3; ++a) {
+    float corner = c[a] - h[a];
+    q[a] = (o[a] + ti * d[a]) - corner;
+    q[a] = std::min(std::max(q[a], 0.0f), s.tile - 0.00001f);
+    int v = (int)(q[a] / s.voxel);
+    vc[a] = std::min(std::max(v, 0), N - 1);
+    vs[a] = d[a] >= 0.0f ? 1 : -1;
+    float nb = (float)(vc[a] + vs[a]) * s.voxel;
+    if (vs[a] < 0) nb = nb + s.voxel;
+    vmax[a] = safe_divide(nb - q[a], d[a]);
+    vdel[a] = safe_divide((float)vs[a] * s.voxel, d[a]);
+  }
+  float near_ = 0.0f;
+  for (;;) {
+    float far_ = std::min(std::min(vmax[0], vmax[1]), vmax[2]);
+    int vid = (vc[0] * N + vc[1]) * N + vc[2];
+    uint32_t rec;
+    if (occupied(s, id, vid, rec))
+      if (!visit(id, rec, vc, near_, far_, ti, q)) return;
+    int a = dda_axis(vmax);
+    vc[a] += vs[a];
+    vmax[a] = vmax[a] + vdel[a];
+    near_ = far_;
+    if (vc[a] < 0 || vc[a] >= N) return;
+  }
+}
+
+struct TrainParams {
+  const float* vfeat;  // [NV][F]
+  const float* vdens;  // [NV]
+  const float* mlp;    // [NT][P]
+};
+
+// Forward of one segment; returns the samples (with activations) and colour.
+void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const float o[3], const float d[3],
+                       std::vector<TrainSample>& out, double C[3]) {
+  out.clear();
+  C[0] = C[1] = C[2] = 0;
+  double T = 1.0;
+  std::vector<double> enc(27);
+  dir_enc<double>(d, enc.data());
+  const float* W = p.mlp + (int64_t)tile * s.P;
+  march_one_tile(s, tile, o, d, [&](int, uint32_t rec, const int* vc, float nr, float fr, float ti, const float* q) {
+    return voxel_samples(s, vc, nr, fr, ti, q, d, [&](const SampleGeom& g) {
+      TrainSample ts;
+      trilinear_w<double>(g.f, ts.w);
+      const int32_t* cn = s.d->voxel_corners + (int64_t)rec * 8;
+      ts.s = 0;
+      for (int k = 0; k < 8; ++k) {
+        ts.corners[k] = cn[k];
+        ts.s += ts.w[k] * (double)p.vdens[cn[k]];
+      }
+      ts.sigma = softplus<double>(ts.s);
+      ts.dv = (double)(g.interval * s.inv_voxel);
+      ts.alpha = 1.0 - std::exp(-ts.sigma * ts.dv);
+      ts.T = T;
+      ts.x.assign((size_t)s.in, 0.0);
+      for (int c = 0; c < s.F; ++c)
+        for (int k = 0; k < 8; ++k) ts.x[(size_t)c] += ts.w[k] * (double)p.vfeat[(int64_t)cn[k] * s.F + c];
+      for (int i = 0; i < 27; ++i) ts.x[(size_t)(s.F + i)] = enc[(size_t)i];
+      // MLP with stored activations
+      std::vector<double> cur = ts.x;
+      int64_t off = 0;
+      for (int l = 0; l <= s.L; ++l) {
+        int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
+        std::vector<double> nx((size_t)fo);
+        for (int oo = 0; oo < fo; ++oo) {
+          double acc = W[off + (int64_t)fi * fo + oo];
+          for (int i = 0; i < fi; ++i) acc += (double)W[off + (int64_t)oo * fi + i] * cur[(size_t)i];
+          nx[(size_t)oo] = l < s.L ? std::max(acc, 0.0) : acc;
+        }
+        off += (int64_t)fi * fo + fo;
+        if (l < s.L) ts.h.push_back(nx);
+        cur.swap(nx);
+      }
+      for (int c = 0; c < 3; ++c) {
+        ts.c[c] = sigmoid<double>(cur[(size_t)c]);
+        C[c] += T * ts.alpha * ts.c[c];
+      }
+      T *= (1.0 - ts.alpha);
+      out.push_back(std::move(ts));
+      return !(T < (double)s.early);
+    });
+  });
+}
+
+// Adjoint of one segment given dL/dC (g); accumulates into the gradients.
+void train_backward_ray(const Scene& s, const TrainParams& p, int tile, const std::vector<TrainSample>& S,
+                        const double g[3], double* gF, double* gG, double* gW) {
+  const float* W = p.mlp + (int64_t)tile * s.P;
+  double* GW = gW + (int64_t)tile * s.P;
+  const int n = (int)S.size();
+  std::vector<double> suffix((size_t)n * 3 + 3, 0.0);  // S_i = sum_{j>i} T_j alpha_j c_j
+  for (int i = n - 1; i >= 0; --i)
+    for (int c = 0; c < 3; ++c) {
+      double next = (i + 1 < n) ? S[(size_t)i + 1].T * S[(size_t)i + 1].alpha * S[(size_t)i + 1].c[c] : 0.0;
+      suffix[(size_t)i * 3 + c] = suffix[(size_t)(i + 1) * 3 + c] + next;
+    }
+  for (int i = 0; i < n; ++i) {
+    const TrainSample& t = S[(size_t)i];
+    double gc = 0, gs = 0;
+    for (int c = 0; c < 3; ++c) { gc += g[c] * t.c[c]; gs += g[c] * suffix[(size_t)i * 3 + c]; }
+    double dsigma = t.dv * ((1.0 - t.alpha) * t.T * gc - gs);
+    double ds = sigmoid<double>(t.s) * dsigma;
+    for (int k = 0; k < 8; ++k) gG[t.corners[k]] += t.w[k] * ds;
+    // MLP backward
+    std::vector<double> delta(3);
+    for (int c = 0; c < 3; ++c) delta[(size_t)c] = g[c] * t.T * t.alpha * t.c[c] * (1.0 - t.c[c]);
+    // layer offsets
+    std::vector<int64_t> offs;
+    int64_t off = 0;
+    for (int l = 0; l <= s.L; ++l) {
+      int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
+      offs.push_back(off);
+      off += (int64_t)fi * fo + fo;
+    }
+    for (int l = s.L; l >= 0; --l) {
+      int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
+      const std::vector<double>& in = l == 0 ? t.x : t.h[(size_t)l - 1];
+      for (int oo = 0; oo < fo; ++oo) {
+        GW[offs[(size_t)l] + (int64_t)fi * fo + oo] += delta[(size_t)oo];
+        for (int ii = 0; ii < fi; ++ii) GW[offs[(size_t)l] + (int64_t)oo * fi + ii] += delta[(size_t)oo] * in[(size_t)ii];
+      }
+      std::vector<double> prev((size_t)fi, 0.0);
+      for (int ii = 0; ii < fi; ++ii) {
+        double acc = 0;
+        for (int oo = 0; oo < fo; ++oo) acc += (double)W[offs[(size_t)l] + (int64_t)oo * fi + ii] * delta[(size_t)oo];
+        if (l > 0) acc = t.h[(size_t)l - 1][(size_t)ii] > 0.0 ? acc : 0.0;
+        prev[(size_t)ii] = acc;
+      }
+      delta.swap(prev);
+    }
+    for (int c = 0; c < s.F; ++c)
+      for (int k = 0; k < 8; ++k) gF[(int64_t)t.corners[k] * s.F + c] += t.w[k] * delta[(size_t)c];
+  }
+}
+}  // namespace
+extern "C" {
+
+// ---------------------------------------------------------------------------
 // Reference-op restatements (bit-exact specification of the drop-in ops).
 // ---------------------------------------------------------------------------
 void oracle_op_compute_rays(const float* intr, const float* rot, int H, int W, float* rays_d) {
@@ -712,6 +882,36 @@ void oracle_op_integrate(const float* rgba, const float* dz, int64_t npix, float
     }
     trans[i] = T;
     for (int a = 0; a < 3; ++a) frame[3 * i + a] = frame[3 * i + a] + c[a];
+  }
+}
+
+// Training forward (FP64): rgb [n][3] of ray segments (ray i inside tile
+// ray_tile[i]); counts [n] (optional) = samples per segment.
+void oracle_train_forward(const oracle_scene* os, const float* vfeat, const float* vdens, const float* mlp,
+                          const float* o, const float* d, const int32_t* ray_tile, int64_t n, double* rgb,
+                          int32_t* counts, int threads) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  TrainParams p{vfeat, vdens, mlp};
+  parallel_for(n, threads, [&](int64_t i) {
+    std::vector<TrainSample> S;
+    train_forward_ray(s, p, ray_tile[i], o + 3 * i, d + 3 * i, S, rgb + 3 * i);
+    if (counts) counts[i] = (int32_t)S.size();
+  });
+}
+
+// Training adjoint (FP64): gradients of L = sum(grad_rgb * rgb) accumulated
+// into gF [NV][F], gG [NV], gW [NT][P] (zero them first).  Single-threaded
+// (deterministic accumulation order).
+void oracle_train_backward(const oracle_scene* os, const float* vfeat, const float* vdens, const float* mlp,
+                           const float* o, const float* d, const int32_t* ray_tile, int64_t n,
+                           const double* grad_rgb, double* gF, double* gG, double* gW) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  TrainParams p{vfeat, vdens, mlp};
+  std::vector<TrainSample> S;
+  for (int64_t i = 0; i < n; ++i) {
+    double C[3];
+    train_forward_ray(s, p, ray_tile[i], o + 3 * i, d + 3 * i, S, C);
+    train_backward_ray(s, p, ray_tile[i], S, grad_rgb + 3 * i, gF, gG, gW);
   }
 }
 
