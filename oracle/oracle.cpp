@@ -223,8 +223,9 @@ void dir_enc(const float d[3], T* out) {
 }
 
 // MLP of one tile: Linear -> ReLU (L times) -> Linear; layout per Linear
-// W[out][in] then b[out].  `half_inputs`: round every Linear input to FP16
-// (tensor-core form) for the hidden layers.
+// W[out][in] then b[out].  `half_inputs`: emulate the tensor-core form --
+// every Linear's weights, inputs and bias rounded to FP16, products summed
+// exactly (FP32 accumulation in hardware; the oracle sums in T).
 template <class T>
 void mlp(const Scene& s, int tile, const T* x, T out[3], bool half_inputs = false) {
   const float* p = s.d->mlp_params + (int64_t)tile * s.P;
@@ -238,10 +239,12 @@ void mlp(const Scene& s, int tile, const T* x, T out[3], bool half_inputs = fals
       for (int i = 0; i < fi; ++i) {
         T w = (T)p[off + (int64_t)o * fi + i];
         T xi = cur[(size_t)i];
-        if (half_inputs && l < s.L) { w = (T)round_f16((float)w); xi = (T)round_f16((float)xi); }
+        if (half_inputs) { w = (T)round_f16((float)w); xi = (T)round_f16((float)xi); }
         acc += w * xi;
       }
-      nxt[(size_t)o] = acc + (T)p[off + (int64_t)fi * fo + o];
+      T bias = (T)p[off + (int64_t)fi * fo + o];
+      if (half_inputs) bias = (T)round_f16((float)bias);
+      nxt[(size_t)o] = acc + bias;
     }
     off += (int64_t)fi * fo + fo;
     if (l < s.L)

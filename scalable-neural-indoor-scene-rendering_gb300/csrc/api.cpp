@@ -116,36 +116,30 @@ std::vector<float> plain_layout(const float* p, int in, int H, int L, int& strid
   return out;
 }
 
-// Tensor-core image of one tile: L FP16 B tiles [H][64] in the 128-byte
-// swizzled K-major layout, then FP32 Wlast[3][H], b_hidden[L][H], b_last[4].
+// Tensor-core image of one tile (layout in tc_image_bytes): FP16 weights
+// and biases in 128-byte swizzled K-major tiles.
 void tc_image(const float* p, int in, int H, int L, uint8_t* img) {
   const int bytes = tc_image_bytes(H, L);
   std::memset(img, 0, (size_t)bytes);
+  auto put = [&](uint8_t* tile, int row, int k, float v) {
+    uint16_t h = f32_to_f16(v);
+    uint32_t o = ((uint32_t)row >> 3) * 1024u + ((uint32_t)row & 7u) * 128u +
+                 ((((uint32_t)k >> 3) ^ ((uint32_t)row & 7u)) << 4) + (((uint32_t)k & 7u) << 1);
+    std::memcpy(tile + o, &h, 2);
+  };
+  uint8_t* wout = img + L * H * 128;
+  uint8_t* bhid = wout + 2048;
+  uint8_t* bout = bhid + H * 128;
   int64_t off = 0;
-  float* tail = reinterpret_cast<float*>(img + L * H * 128);
-  float* wlast = tail;
-  float* bhid = tail + 3 * H;
-  float* blast = bhid + L * H;
   for (int l = 0; l <= L; ++l) {
     int fi = l == 0 ? in : H, fo = l == L ? 3 : H;
-    if (l < L) {
-      uint8_t* tile = img + l * H * 128;
-      for (int n = 0; n < fo; ++n)
-        for (int k = 0; k < fi; ++k) {
-          uint16_t h = f32_to_f16(p[off + (int64_t)n * fi + k]);
-          uint32_t o = ((uint32_t)n >> 3) * 1024u + ((uint32_t)n & 7u) * 128u + ((((uint32_t)k >> 3) ^ ((uint32_t)n & 7u)) << 4) + (((uint32_t)k & 7u) << 1);
-          std::memcpy(tile + o, &h, 2);
-        }
-      off += (int64_t)fi * fo;
-      for (int n = 0; n < fo; ++n) bhid[l * H + n] = p[off + n];
-      off += fo;
-    } else {
-      for (int c = 0; c < 3; ++c)
-        for (int j = 0; j < H; ++j) wlast[c * H + j] = p[off + (int64_t)c * H + j];
-      off += 3 * (int64_t)H;
-      for (int c = 0; c < 3; ++c) blast[c] = p[off + c];
-      off += 3;
-    }
+    uint8_t* wt = l < L ? img + l * H * 128 : wout;
+    for (int n = 0; n < fo; ++n)
+      for (int k = 0; k < fi; ++k) put(wt, n, k, p[off + (int64_t)n * fi + k]);
+    off += (int64_t)fi * fo;
+    for (int n = 0; n < fo; ++n)
+      for (int k = 0; k < 16; ++k) put(l < L ? bhid : bout, n, (l < L ? 16 * l : 0) + k, p[off + n]);
+    off += fo;
   }
 }
 
@@ -434,6 +428,7 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
   ws.cap = (uint32_t)cap;
   if ((st = dev_alloc(sc, &ws.recs, (size_t)cap * sizeof(SampleRec), "sample buffer")) != SNISR_OK) return fail(st);
   if ((st = dev_alloc(sc, &ws.sorted, (size_t)cap * sizeof(SampleRec), "sorted samples")) != SNISR_OK) return fail(st);
+  if ((st = dev_alloc(sc, &ws.blk_count, (size_t)(cap / 256 + 2) * 4, "block counts")) != SNISR_OK) return fail(st);
   ws.ctrl_words = std::max(CTRL_HEADER + 4 * NT + 2, train_ctrl_words(NT));
   if ((st = dev_alloc(sc, &ws.ctrl, (size_t)ws.ctrl_words * 4, "control words")) != SNISR_OK) return fail(st);
 

@@ -21,6 +21,7 @@ struct Workspace {
   uint4* enc = nullptr;        // [max_rays][4] FP16 view encoding (32 halves)
   SampleRec* recs = nullptr;   // [cap] compacted samples
   SampleRec* sorted = nullptr; // [cap] samples grouped by tile
+  uint32_t* blk_count = nullptr;  // [cap/256 + 1] valid samples per 256-slot block
   uint32_t cap = 0;
   int* ctrl = nullptr;         // frame control words
   int ctrl_words = 0;

@@ -230,12 +230,14 @@ constexpr uint32_t kBlk = 256;
 
 __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
                                                                 const float4* __restrict__ ray_d, int64_t n,
-                                                                SampleRec* recs, uint32_t cap, int* ctrl,
-                                                                float* depth, float* opac) {
-  extern __shared__ uint32_t hist[];
-  for (int t = threadIdx.x; t < S.num_tiles; t += blockDim.x) hist[t] = 0;
-  __syncthreads();
+                                                                SampleRec* recs, uint32_t cap, uint32_t* blk_count,
+                                                                int* ctrl, float* depth, float* opac) {
+  // per-warp tile histogram (no CTA-wide barrier: warps finish independently)
+  extern __shared__ uint32_t hist_all[];
   const int lane = threadIdx.x & 31;
+  uint32_t* hist = hist_all + (threadIdx.x >> 5) * S.num_tiles;
+  for (int t = lane; t < S.num_tiles; t += 32) hist[t] = 0;
+  __syncwarp();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   RayState R;
   bool live = false;
@@ -245,6 +247,7 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, cons
     float o[3] = {o4.x, o4.y, o4.z}, d[3] = {d4.x, d4.y, d4.z};
     live = R.init(S, o, d, d4.w);
   }
+  const uint32_t ray_id = (uint32_t)i;
   uint32_t cur = 0, end = 0;  // warp-uniform block cursor
   for (;;) {
     Sample s;
@@ -270,6 +273,8 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, cons
     uint32_t slot;
     if (cur + cnt > end) {
       uint32_t nb = 0;
+      // the open block (if any) is filled to the end by this round
+      if (lane == 0 && end != 0 && (end - kBlk) / kBlk < (cap + kBlk - 1) / kBlk) blk_count[(end - kBlk) / kBlk] = kBlk;
       if (lane == 0) nb = (uint32_t)atomicAdd(ctrl + CTRL_RESERVED, (int)kBlk);
       nb = __shfl_sync(kFull, nb, 0);
       uint32_t rem = end - cur;
@@ -285,14 +290,14 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, cons
     unsigned m2 = __ballot_sync(kFull, wrote);
     if (wrote) {
       uint4* dst = reinterpret_cast<uint4*>(recs + slot);
-      dst[0] = make_uint4(s.rec, (uint32_t)i, __float_as_uint(wt), (uint32_t)s.tile);
+      dst[0] = make_uint4(s.rec, ray_id, __float_as_uint(wt), (uint32_t)s.tile);
       dst[1] = make_uint4(__float_as_uint(s.f[0]), __float_as_uint(s.f[1]), __float_as_uint(s.f[2]), 0u);
       unsigned g = __match_any_sync(m2, s.tile);
       if (lane == __ffs(g) - 1) atomicAdd(hist + s.tile, (uint32_t)__popc(g));
     }
   }
-  for (uint32_t sl = cur + lane; sl < end; sl += 32)
-    if (sl < cap) recs[sl].rec = kInvalid;
+  if (lane == 0 && end != 0 && (end - kBlk) / kBlk < (cap + kBlk - 1) / kBlk)
+    blk_count[(end - kBlk) / kBlk] = cur - (end - kBlk);
   if (i < n) {
     depth[i] = D;
     opac[i] = 1.0f - T;
@@ -301,8 +306,8 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, cons
 #pragma unroll
   for (int sh = 16; sh > 0; sh >>= 1) st += __shfl_xor_sync(kFull, st, sh);
   if (lane == 0 && st) atomicAdd(reinterpret_cast<unsigned long long*>(ctrl + CTRL_STEPS), st);
-  __syncthreads();
-  for (int t = threadIdx.x; t < S.num_tiles; t += blockDim.x)
+  __syncwarp();
+  for (int t = lane; t < S.num_tiles; t += 32)
     if (hist[t]) atomicAdd(ctrl + CTRL_HEADER + t, (int)hist[t]);
 }
 
@@ -330,33 +335,43 @@ __global__ void scan_kernel(int* ctrl, int NT) {
 }
 
 // Stage 3: move samples into per-tile order (warp-aggregated cursors).
-__global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap, int* ctrl, int NT,
-                               SampleRec* sorted) {
+// Slot s is valid iff s % 256 < blk_count[s / 256] (per-warp blocks are
+// filled in order; only each warp's last block is partial).
+__global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap, const uint32_t* __restrict__ blk_count,
+                               int* ctrl, int NT, SampleRec* sorted) {
   const int lane = threadIdx.x & 31;
-  uint32_t total = min((uint32_t)ctrl[CTRL_RESERVED], cap);
+  const uint32_t total = min((uint32_t)ctrl[CTRL_RESERVED], cap);
   const int* off = ctrl + CTRL_HEADER + NT;
   int* cursor = ctrl + CTRL_HEADER + NT + (NT + 1) + (NT + 1);
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < total; base += warps * 32) {
-    uint32_t s = base + lane;
-    uint4 a = make_uint4(kInvalid, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-    if (s < total) {
-      const uint4* src = reinterpret_cast<const uint4*>(recs + s);
-      a = src[0];
-      b = src[1];
+  constexpr int U = 2;  // records per lane in flight
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * U; base < total; base += warps * 32 * U) {
+    uint4 a[U], b[U];
+    bool valid[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t s = base + u * 32 + lane;
+      valid[u] = s < total && (s % kBlk) < __ldg(blk_count + s / kBlk);
+      if (valid[u]) {
+        const uint4* src = reinterpret_cast<const uint4*>(recs + s);
+        a[u] = src[0];
+        b[u] = src[1];
+      }
     }
-    bool valid = a.x != kInvalid;
-    unsigned m = __ballot_sync(kFull, valid);
-    if (valid) {
-      unsigned g = __match_any_sync(m, a.w);
-      int leader = __ffs(g) - 1;
-      int pos = 0;
-      if (lane == leader) pos = atomicAdd(cursor + a.w, __popc(g));
-      pos = __shfl_sync(g, pos, leader);
-      pos += __popc(g & lanemask_lt());
-      uint4* dst = reinterpret_cast<uint4*>(sorted + off[a.w] + pos);
-      dst[0] = a;
-      dst[1] = b;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      unsigned m = __ballot_sync(kFull, valid[u]);
+      if (valid[u]) {
+        unsigned g = __match_any_sync(m, a[u].w);
+        int leader = __ffs(g) - 1;
+        int pos = 0;
+        if (lane == leader) pos = atomicAdd(cursor + a[u].w, __popc(g));
+        pos = __shfl_sync(g, pos, leader);
+        pos += __popc(g & lanemask_lt());
+        uint4* dst = reinterpret_cast<uint4*>(sorted + off[a[u].w] + pos);
+        dst[0] = a[u];
+        dst[1] = b[u];
+      }
     }
   }
 }
@@ -376,12 +391,11 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   constexpr int G = F / 8;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  // shared memory: A tile (16 KB) | weight image of the current tile | ones atom | barriers
   uint8_t* A0 = base;            // layer input: features+encoding, then hidden activations
-  uint8_t* Wsm = base + 16384;
-  const float* Wlast = reinterpret_cast<const float*>(Wsm + L * H * 128);
-  const float* bhid = Wlast + 3 * H;
-  const float* blast = bhid + L * H;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(Wsm + ((img_bytes + 15) & ~15));
+  uint8_t* Wsm = base + 16384;   // tc_image layout (see tc_image_bytes)
+  uint8_t* ones = Wsm + ((img_bytes + 1023) & ~1023);  // 1 KB atom of 1/16 (8 rows x 128 B)
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 1024);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
   const uint32_t wbar = tc::smem_addr(bars), mbar = tc::smem_addr(bars + 1);
@@ -396,11 +410,18 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     tc::tmem_alloc(tc::smem_addr(tmem_slot), H);
     tc::tmem_relinquish();
   }
+  // every fp16 of the atom is 1/16: D += (1/16) * sum_{k<16} bias = bias (exact)
+  for (int k = tid; k < 1024 / 16; k += blockDim.x)
+    reinterpret_cast<uint4*>(ones)[k] = make_uint4(0x2C002C00u, 0x2C002C00u, 0x2C002C00u, 0x2C002C00u);
+  tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = tc::idesc_f16(H, 0);
+  const uint32_t idesc_out = tc::idesc_f16(16, 0);
+  // A operand of the bias step: the 1 KB atom for all 16 row groups (stride 0)
+  const uint64_t ones_desc = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
   const int* off = ctrl + CTRL_HEADER + NT;
   const int* coff = off + NT + 1;
   const int total_chunks = ctrl[CTRL_CHUNKS];
@@ -428,88 +449,114 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     }
     cur_tile = tile;
 
-    // gather: lane = row.  Each lane reads its sample's 8-corner FP16 record
-    // (G x 8 x 16 bytes, one voxel), interpolates in FP32 and writes the
-    // swizzled A row: chunks [0,G) features, [G,G+4) view encoding, rest 0.
+    // gather: per warp iteration RPI = 32/G rows; lane (g = lane / RPI,
+    // row = lane % RPI) owns channel group g of one row.  The FP16 cache is
+    // corner-major ([voxel][corner][group] x 16 B), so for each corner the G
+    // lanes of a row read one contiguous G*16-byte slice: a load instruction
+    // touches RPI cache lines, not 32.  Each lane interpolates its 8 channels
+    // over the 8 corners in FP32 and writes one 16-byte chunk of the
+    // swizzled A row (8 consecutive rows per 8-lane phase: conflict-free).
+    // A row holds chunks [0,G) features, [G,G+4) view encoding, the rest 0.
     {
-      const int r = tid;
-      uint4 ra = make_uint4(kInvalid, 0, 0, 0), rb = make_uint4(0, 0, 0, 0);
-      if (r < cnt) {
-        const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + r);
-        ra = src[0];
-        rb = src[1];
-      }
-      uint8_t* arow = A0;
-      if (ra.x != kInvalid) {
-        const float fx = __uint_as_float(rb.x), fy = __uint_as_float(rb.y), fz = __uint_as_float(rb.z);
-        float w[8];
+      constexpr int RPI = 32 / G;
+      const int my_g = lane / RPI, my_row = lane % RPI;
+#pragma unroll 1
+      for (int it = 0; it < G; it += 2) {
+        uint32_t rec[2], ray[2];
+        float fx[2], fy[2], fz[2];
+        uint4 cv[2][8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-          w[k] = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
-        const uint4* fp = S.feat16 + (size_t)ra.x * G * 8;
-        uint4 ev[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) ev[j] = __ldg(enc + (size_t)ra.y * 4 + j);
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-          uint4 cv[8];
-#pragma unroll
-          for (int k = 0; k < 8; ++k) cv[k] = __ldg(fp + g * 8 + k);
-          float acc[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const __half2* hv = reinterpret_cast<const __half2*>(&cv[k]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float2 p = __half22float2(hv[q]);
-              acc[2 * q] = fmaf(w[k], p.x, acc[2 * q]);
-              acc[2 * q + 1] = fmaf(w[k], p.y, acc[2 * q + 1]);
-            }
+        for (int u = 0; u < 2; ++u) {
+          const int rbase = warp * 32 + (it + u) * RPI;
+          uint4 ra = make_uint4(kInvalid, 0, 0, 0), rb = make_uint4(0, 0, 0, 0);
+          if (lane < RPI && rbase + lane < cnt) {
+            const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + rbase + lane);
+            ra = src[0];
+            rb = src[1];
           }
-          uint4 o;
-          o.x = pack_h2(acc[0], acc[1]); o.y = pack_h2(acc[2], acc[3]);
-          o.z = pack_h2(acc[4], acc[5]); o.w = pack_h2(acc[6], acc[7]);
-          *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, g)) = o;
+          rec[u] = __shfl_sync(kFull, ra.x, my_row);
+          ray[u] = __shfl_sync(kFull, ra.y, my_row);
+          fx[u] = __uint_as_float(__shfl_sync(kFull, rb.x, my_row));
+          fy[u] = __uint_as_float(__shfl_sync(kFull, rb.y, my_row));
+          fz[u] = __uint_as_float(__shfl_sync(kFull, rb.z, my_row));
+          if (rec[u] != kInvalid) {
+            const uint4* fp = S.feat16 + (size_t)rec[u] * 8 * G + my_g;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cv[u][k] = __ldg(fp + k * G);
+          }
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, G + j)) = ev[j];
+        for (int u = 0; u < 2; ++u) {
+          const int r = warp * 32 + (it + u) * RPI + my_row;
+          if (rec[u] != kInvalid) {
+            float acc[8];
 #pragma unroll
-        for (int ch = G + 4; ch < 8; ++ch) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
-      } else {
+            for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
 #pragma unroll
-        for (int ch = 0; ch < 8; ++ch) *reinterpret_cast<uint4*>(arow + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
+            for (int k = 0; k < 8; ++k) {
+              const float wk = ((k & 4) ? fx[u] : 1.0f - fx[u]) * ((k & 2) ? fy[u] : 1.0f - fy[u]) *
+                               ((k & 1) ? fz[u] : 1.0f - fz[u]);
+              const __half2* hv = reinterpret_cast<const __half2*>(&cv[u][k]);
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                float2 pp = __half22float2(hv[q]);
+                acc[2 * q] = fmaf(wk, pp.x, acc[2 * q]);
+                acc[2 * q + 1] = fmaf(wk, pp.y, acc[2 * q + 1]);
+              }
+            }
+            uint4 o;
+            o.x = pack_h2(acc[0], acc[1]); o.y = pack_h2(acc[2], acc[3]);
+            o.z = pack_h2(acc[4], acc[5]); o.w = pack_h2(acc[6], acc[7]);
+            *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, my_g)) = o;
+#pragma unroll
+            for (int e = my_g; e < 4; e += G)
+              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)ray[u] * 4 + e);
+#pragma unroll
+            for (int ch = G + 4 + my_g; ch < 8; ch += G)
+              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
+          } else {
+#pragma unroll
+            for (int ch = my_g; ch < 8; ch += G)
+              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
+          }
+        }
       }
     }
     tc::fence_proxy_async();
     __syncthreads();
     if (new_w) {
-      bool ok = tc::mbar_wait(wbar, wphase);
+      // one thread polls the barrier; the others wait at bar.sync, which
+      // keeps the shared-memory pipe free for the gathers of other CTAs
+      bool ok = tid == 0 ? tc::mbar_wait(wbar, wphase) : true;
       wphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; break; }
     }
 
+    // L hidden Linear layers and the output Linear (N = 16, 3 used), all on
+    // the tensor core; each layer's bias enters as one extra K = 16 step.
     float out3[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
-    for (int l = 0; l < L; ++l) {
+    for (int l = 0; l <= L; ++l) {
       if (tid == 0) {
         tc::fence_after_sync();
         const uint32_t a_base = tc::smem_addr(A0);
-        const uint32_t b_base = tc::smem_addr(Wsm + l * H * 128);
+        const bool last = l == L;
+        const uint32_t b_base = tc::smem_addr(Wsm + (last ? L * H * 128 : l * H * 128));
         const int ksteps = l == 0 ? 4 : H / 16;  // K = 64 (padded input) or H
+        const uint32_t id = last ? idesc_out : idesc;
         for (int kk = 0; kk < ksteps; ++kk)
-          tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), idesc, kk > 0);
+          tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), id, kk > 0);
+        const uint32_t bias_tile = tc::smem_addr(Wsm + (last ? L * H * 128 + 2048 + H * 128 : L * H * 128 + 2048));
+        tc::mma_f16(tmem, ones_desc, tc::sdesc_sw128(bias_tile + (last ? 0 : 32 * l)), id, 1);
         tc::mma_commit(mbar);
       }
-      bool ok = tc::mbar_wait(mbar, mphase);
+      bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
       mphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; break; }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-      const float* b = bhid + l * H;
-      if (l + 1 < L) {
-        // bias + ReLU + FP16 pack of 32 columns at a time into the A tile
+      if (l < L) {
+        // ReLU + FP16 pack of 32 columns at a time into the A tile
 #pragma unroll
         for (int half = 0; half < H / 32; ++half) {
           float v[32];
@@ -518,33 +565,20 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
           tc::tmem_wait_ld();
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int c0 = 32 * half + 8 * q;
             uint4 o;
-            o.x = pack_relu_h2(v[8 * q + 0] + b[c0 + 0], v[8 * q + 1] + b[c0 + 1]);
-            o.y = pack_relu_h2(v[8 * q + 2] + b[c0 + 2], v[8 * q + 3] + b[c0 + 3]);
-            o.z = pack_relu_h2(v[8 * q + 4] + b[c0 + 4], v[8 * q + 5] + b[c0 + 5]);
-            o.w = pack_relu_h2(v[8 * q + 6] + b[c0 + 6], v[8 * q + 7] + b[c0 + 7]);
+            o.x = pack_relu_h2(v[8 * q + 0], v[8 * q + 1]);
+            o.y = pack_relu_h2(v[8 * q + 2], v[8 * q + 3]);
+            o.z = pack_relu_h2(v[8 * q + 4], v[8 * q + 5]);
+            o.w = pack_relu_h2(v[8 * q + 6], v[8 * q + 7]);
             *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(tid, 4 * half + q)) = o;
           }
         }
         tc::fence_proxy_async();
       } else {
-        // last hidden layer: bias + ReLU in FP32, then the H -> 3 Linear
-        out3[0] = blast[0]; out3[1] = blast[1]; out3[2] = blast[2];
-#pragma unroll
-        for (int half = 0; half < H / 32; ++half) {
-          float v[32];
-          tc::tmem_ld16(taddr + 32 * half, v);
-          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
-          tc::tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float h = fmaxf(v[j] + b[32 * half + j], 0.0f);
-            out3[0] = fmaf(Wlast[32 * half + j], h, out3[0]);
-            out3[1] = fmaf(Wlast[H + 32 * half + j], h, out3[1]);
-            out3[2] = fmaf(Wlast[2 * H + 32 * half + j], h, out3[2]);
-          }
-        }
+        float v[4];
+        tc::tmem_ld4(taddr, v);
+        tc::tmem_wait_ld();
+        out3[0] = v[0]; out3[1] = v[1]; out3[2] = v[2];
       }
       tc::fence_before_sync();
       __syncthreads();
@@ -632,7 +666,7 @@ cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, fl
 
 template <int F, int H, int L>
 cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num_sms, cudaStream_t st) {
-  const int smem = 1024 + 16384 + ((ws.wimg_bytes + 15) & ~15) + 64;
+  const int smem = 1024 + 16384 + ((ws.wimg_bytes + 1023) & ~1023) + 1024 + 64;
   static int per_sm = 0;  // resident CTAs per SM, computed once per process
   if (per_sm == 0) {
     cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -665,7 +699,12 @@ bool mlp_shape_supported(int F, int H, int L) {
          (F == 32 && H == 32 && L == 2);
 }
 
-int tc_image_bytes(int H, int L) { return L * H * 128 + (3 * H + L * H + 4) * 4; }
+// Per-tile tensor-core image (all tiles 128-byte swizzled, K-major, FP16):
+//   [0, L*H*128)               hidden-layer weights W_l [H rows][K <= 64]
+//   [+0, +2048)                output weights [16 rows (3 used)][H]
+//   [+2048, +2048 + H*128)     hidden biases: row n, K-slice l = 16 x b_l[n]
+//   [.., +2048)                output bias: row c, K-slice 0 = 16 x b_out[c]
+int tc_image_bytes(int H, int L) { return L * H * 128 + 2048 + H * 128 + 2048; }
 
 cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* origins, const float* dirs, int64_t n,
                           const Workspace& ws, bool want_enc, cudaStream_t st) {
@@ -705,14 +744,16 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   e = cudaMemsetAsync(rgb, 0, sizeof(float) * 3 * n, st);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
-  traverse_kernel<<<grid_for(n, kTravThreads, 1 << 24), kTravThreads, sizeof(uint32_t) * S.num_tiles, st>>>(
-      S, ws.ray_o, ws.ray_d, n, ws.recs, ws.cap, ws.ctrl, depth, opac);
+  const int hist_bytes = (int)sizeof(uint32_t) * S.num_tiles * (kTravThreads / 32);
+  traverse_kernel<<<grid_for(n, kTravThreads, 1 << 24), kTravThreads, hist_bytes, st>>>(S, ws.ray_o, ws.ray_d, n, ws.recs,
+                                                                                ws.cap, ws.blk_count, ws.ctrl,
+                                                                                depth, opac);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
-  scatter_kernel<<<num_sms * 8, 256, 0, st>>>(ws.recs, ws.cap, ws.ctrl, S.num_tiles, ws.sorted);
+  scatter_kernel<<<num_sms * 16, 256, 0, st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl, S.num_tiles, ws.sorted);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[3], st)) != cudaSuccess) return e;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;

@@ -3,10 +3,9 @@
 //
 //   dens   [NVOX][8]        FP32 density logits per corner
 //   feat32 [NVOX][F/4][8]   float4 = 4 channels of one corner
-//   feat16 [NVOX][F/8][8]   uint4  = 8 FP16 channels of one corner
-//
-// The FP16 record of one voxel (F=32: 512 bytes) is read by one warp with a
-// single coalesced 16-byte-per-lane load.
+//   feat16 [NVOX][8][F/8]   uint4  = 8 FP16 channels of one corner,
+//                           corner-major: the F/8 lanes that interpolate one
+//                           sample read one contiguous F*2-byte slice per corner
 #include <cuda_fp16.h>
 
 #include "scene_dev.h"
@@ -37,7 +36,7 @@ __global__ void expand_kernel(const int32_t* __restrict__ corners, const void* v
       for (int g = 0; g < G8; ++g) {
         __align__(16) __half h[8];
         for (int c = 0; c < 8; ++c) h[c] = __float2half_rn(load_val(vfeat, vid * F + 8 * g + c, f16));
-        feat16[(v * G8 + g) * 8 + k] = *reinterpret_cast<const uint4*>(h);
+        feat16[(v * 8 + k) * G8 + g] = *reinterpret_cast<const uint4*>(h);
       }
     }
   }

@@ -105,6 +105,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+// 32 lanes x 32 bits, 4 consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -128,6 +138,13 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
          | ((uint64_t)(1024u >> 4) << 32)       // stride byte offset
          | ((uint64_t)1u << 46)                 // descriptor version
          | ((uint64_t)2u << 61);                // 128-byte swizzle
+}
+
+// Same layout with an explicit stride byte offset between 8-row groups
+// (0 = every group reads the same 1 KB atom).
+__device__ __forceinline__ uint64_t sdesc_sw128_sbo(uint32_t saddr, uint32_t sbo_bytes) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32) |
+         ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
 }
 
 // Byte offset of the 16-byte chunk `c` (0..7) of row `r` in a 128-byte

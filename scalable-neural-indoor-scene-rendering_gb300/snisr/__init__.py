@@ -8,6 +8,7 @@ from . import _lib
 from ._lib import FORM_PLAIN_FP32, FORM_TC, F16, F32, SnisrError, lib
 from .configs import ALL as CONFIGS, CFG1, CFG2, CFG3, CFG4, CFG5, Config
 from .scene import Scene, SynthScene, camera_rays
+from . import ops
 
 __all__ = [
     "FORM_PLAIN_FP32", "FORM_TC", "F16", "F32", "SnisrError", "lib", "CONFIGS", "CFG1", "CFG2", "CFG3",

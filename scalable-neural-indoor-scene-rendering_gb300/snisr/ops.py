@@ -1,0 +1,122 @@
+"""Reference-op mirrors: the FASTRENDERING (rendering/src/binding.cpp:13-27)
+and CUDA_EXT (training/src/binding.cpp:4-12) entry points for this path, with
+the reference's names, argument order and in-place outputs, implemented by
+libsnisr's sm_103a kernels.
+
+Inputs are checked like the reference's CHECK_INPUT (CUDA, contiguous) plus
+dtype/shape checks; failures raise RuntimeError as TORCH_CHECK does.  The
+`num_thread` arguments are accepted for signature compatibility; launch
+shapes are chosen by the library.
+"""
+from __future__ import annotations
+
+from . import _lib
+
+
+def _check(t, name, dtype=None, dim=None):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise RuntimeError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise RuntimeError(f"{name} must be {dtype}, got {t.dtype}")
+    if dim is not None and t.dim() != dim:
+        raise RuntimeError(f"{name} must have {dim} dims, got {t.dim()}")
+
+
+def _stream():
+    import torch
+    return torch.cuda.current_stream().cuda_stream
+
+
+def compute_rays(intrinsic, c2w_rotation, num_thread, rays_d):
+    """rays_d[H,W,3] = R @ [(x-cx)/f, (y-cy)/f, 1] (rendering/src/compute_rays.cu:46-68)."""
+    import torch
+    _check(intrinsic, "intrinsic", torch.float32)
+    _check(c2w_rotation, "c2w_rotation", torch.float32)
+    _check(rays_d, "rays_d", torch.float32, 3)
+    H, W = rays_d.shape[0], rays_d.shape[1]
+    _lib.check(_lib.lib().snisr_op_compute_rays(intrinsic.data_ptr(), c2w_rotation.data_ptr(), H, W,
+                                                rays_d.data_ptr(), _stream()))
+
+
+def tracing_tiles(rays_d, IndexMap, origin, tile_shape, scene_min_corner, scene_size, tile_size, num_thread,
+                  visitedTiles):
+    """Visited non-empty tiles per pixel, -1 padded (rendering/src/raytile_tracing.cu:63-95)."""
+    import torch
+    _check(rays_d, "rays_d", torch.float32)
+    _check(IndexMap, "IndexMap", torch.int32)
+    _check(origin, "origin", torch.float32)
+    _check(tile_shape, "tile_shape", torch.int32)
+    _check(scene_min_corner, "scene_min_corner", torch.float32)
+    _check(scene_size, "scene_size", torch.float32)
+    _check(visitedTiles, "visitedTiles", torch.int32, 3)
+    npix = visitedTiles.shape[0] * visitedTiles.shape[1]
+    if rays_d.numel() != npix * 3:
+        raise RuntimeError("rays_d and visitedTiles disagree on the pixel count")
+    _lib.check(_lib.lib().snisr_op_tracing_tiles(rays_d.data_ptr(), npix, IndexMap.data_ptr(), origin.data_ptr(),
+                                                 tile_shape.data_ptr(), scene_min_corner.data_ptr(),
+                                                 scene_size.data_ptr(), float(tile_size), visitedTiles.shape[2],
+                                                 visitedTiles.data_ptr(), _stream()))
+
+
+def inverse_z_sampling(origin, rays_d, inverse_near, inverse_bound, num_thread, offset, sample_per_ray,
+                       sample_points, integrate_steps):
+    """1/z-uniform samples (rendering/src/sampling.cu:48-81)."""
+    import torch
+    for t, n in ((origin, "origin"), (rays_d, "rays_d"), (inverse_near, "inverse_near"),
+                 (inverse_bound, "inverse_bound"), (sample_points, "sample_points"),
+                 (integrate_steps, "integrate_steps")):
+        _check(t, n, torch.float32)
+    npix = inverse_near.numel()
+    if rays_d.numel() != npix * 3 or inverse_bound.numel() != npix or sample_points.numel() != npix * sample_per_ray * 3:
+        raise RuntimeError("inverse_z_sampling: inconsistent sizes")
+    _lib.check(_lib.lib().snisr_op_inverse_z_sampling(rays_d.data_ptr(), origin.data_ptr(), inverse_near.data_ptr(),
+                                                      inverse_bound.data_ptr(), npix, int(offset), int(sample_per_ray),
+                                                      sample_points.data_ptr(), integrate_steps.data_ptr(),
+                                                      _stream()))
+
+
+def integrate_points(sample_results, integrate_steps, num_thread, early_step, transparency, colors_buffer):
+    """Front-to-back compositing of 16 samples per pixel, transmittance carried
+    across calls (rendering/src/volume_rendering.cu:60-87)."""
+    import torch
+    for t, n in ((sample_results, "sample_results"), (integrate_steps, "integrate_steps"),
+                 (transparency, "transparency"), (colors_buffer, "colors_buffer")):
+        _check(t, n, torch.float32)
+    npix = transparency.numel()
+    if sample_results.numel() != npix * 64 or integrate_steps.numel() != npix * 16 or colors_buffer.numel() != npix * 3:
+        raise RuntimeError("integrate_points: expects 16 samples of (rgb, sigma) per pixel")
+    _lib.check(_lib.lib().snisr_op_integrate_points(sample_results.data_ptr(), integrate_steps.data_ptr(), npix,
+                                                    float(early_step), colors_buffer.data_ptr(),
+                                                    transparency.data_ptr(), _stream()))
+
+
+def Sample_sparse(rays_start, rays_dir, node_flags, cx, cy, cz, tile_size, num_voxel, z_vals, dists):
+    """Samples only inside occupied voxels (training/src/Sample_kernel.cu:397-434).
+    node_flags: int16 [N][N][N] x-major (1 = occupied)."""
+    import torch
+    _check(rays_start, "rays_start", torch.float32, 2)
+    _check(rays_dir, "rays_dir", torch.float32, 2)
+    _check(node_flags, "node_flags", torch.int16, 3)
+    _check(z_vals, "z_vals", torch.float32, 2)
+    _check(dists, "dists", torch.float32, 2)
+    B, ns = z_vals.shape
+    if rays_start.shape[0] != B or rays_dir.shape[0] != B or dists.shape != z_vals.shape:
+        raise RuntimeError("Sample_sparse: inconsistent batch sizes")
+    if node_flags.numel() != num_voxel ** 3:
+        raise RuntimeError("Sample_sparse: node_flags must hold num_voxel^3 entries")
+    _lib.check(_lib.lib().snisr_op_sample_sparse(rays_start.data_ptr(), rays_dir.data_ptr(), B, node_flags.data_ptr(),
+                                                 float(cx), float(cy), float(cz), float(tile_size), int(num_voxel),
+                                                 ns, z_vals.data_ptr(), dists.data_ptr(), _stream()))
+
+
+def sparse_sampling(rays_o, rays_d, node_flags, num_voxel, center, size, nsamples):
+    """training/scripts/utils.py:797-805: node_flags given as D x H x W (z,y,x),
+    returns (z_vals, dists) pre-filled with -1."""
+    import torch
+    z = torch.full((rays_o.shape[0], nsamples), -1, dtype=torch.float32, device=rays_o.device)
+    d = torch.full((rays_o.shape[0], nsamples), -1, dtype=torch.float32, device=rays_o.device)
+    Sample_sparse(rays_o, rays_d, node_flags.permute(2, 1, 0).contiguous(), *center, size, num_voxel, z, d)
+    return z, d
