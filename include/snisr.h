@@ -149,6 +149,21 @@ snisr_status snisr_render_host(snisr_scene* scene, const snisr_camera* cam, int3
                                float* rgb_host, float* depth_host, float* opacity_host,
                                void* stream);
 
+/* Plain FP32 render of at most 32768 rays that allocates no device memory
+ * (no counterpart in the reference).  For callers that may not call
+ * cudaMalloc while rendering: hosts that own all device memory through a pool
+ * of their own, and real-time frame loops that must not block on the
+ * allocator.  Ray staging uses a 2 MiB file-scope __device__ array that every
+ * GPU loading the library holds until exit; the first call on a device looks
+ * up its address, so make that call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Results equal
+ * snisr_render_rays(..., SNISR_FORM_PLAIN_FP32, ...); n > 32768 is rejected
+ * with SNISR_INVALID_ARG. */
+snisr_status snisr_render_rays_noalloc(snisr_scene* scene, const float* origins_dev,
+                                       const float* dirs_dev, int64_t n, float* rgb_dev,
+                                       float* depth_dev, float* opacity_dev, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Per-stage entry points (parity harnesses and drop-in ops).               */
 /* ------------------------------------------------------------------------ */

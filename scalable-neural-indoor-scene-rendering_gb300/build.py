@@ -73,7 +73,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(len(srcs), max(2, os.cpu_count() or 2))) as ex:
         objs = list(ex.map(lambda s: _compile(s, cuda), srcs))
     tmp = OUT + ".tmp"
-    cmd = [os.path.join(cuda, "bin", "nvcc"), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
+    cmd = [os.path.join(cuda, "bin", "nvcc"), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread",
+           "-Xlinker", "--no-undefined"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

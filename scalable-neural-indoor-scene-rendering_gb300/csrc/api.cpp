@@ -228,6 +228,20 @@ snisr_status cam_to_dev(const snisr_camera* c, CamDev& out) {
   return SNISR_OK;
 }
 
+}  // namespace
+
+namespace snisr {
+snisr_status scene_views(snisr_scene* sc, SceneDev* S, Workspace* ws, int* device) {
+  if (!sc) return set_error(SNISR_INVALID_ARG, "scene is null");
+  *S = sc->S;
+  *ws = sc->ws;
+  *device = sc->device;
+  return SNISR_OK;
+}
+}  // namespace snisr
+
+namespace {
+
 snisr_status render_impl(snisr_scene* sc, const CamDev* cam, const float* origins, const float* dirs, int64_t n,
                          int32_t form, float* rgb, float* depth, float* opac, void* stream) {
   if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;

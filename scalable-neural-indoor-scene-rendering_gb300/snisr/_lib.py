@@ -110,6 +110,7 @@ _SIGNATURES = {
     "snisr_proxy_hit": (C.c_int, [P, P, P, C.c_int64, P, P, P]),
     "snisr_trace_voxels": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P]),
     "snisr_render_rays": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P, P]),
+    "snisr_render_rays_noalloc": (C.c_int, [P, P, P, C.c_int64, P, P, P, P]),
     "snisr_train_forward": (C.c_int, [P, P, P, P, P, P, C.c_int64, C.c_int32, P, P]),
     "snisr_train_backward": (C.c_int, [P, P, P, P, P, P, C.c_int64, C.c_int32, P, P, P, P, P, P]),
     "snisr_op_compute_rays": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P]),
