@@ -197,21 +197,31 @@ snisr_status snisr_render_rays(snisr_scene* scene, const float* origins_dev,
 /* training/scripts/utils.py:823-837).  Parameters are passed explicitly so  */
 /* that an optimiser outside the library owns them.                          */
 /* ------------------------------------------------------------------------ */
-/* vfeat_dev [NV][F] FP32, vdens_dev [NV] FP32, mlp_dev [NT][P] FP32.
- * rgb_dev [n*3] out.  Rays must be normalised.  form: PLAIN_FP32 or TC
- * (TC = BF16 compute copies with FP32 accumulation). */
+/* Ray segments: ray i is marched inside sparse tile ray_tile_dev[i] only
+ * (rays split at tile faces, as per-tile training uses them); rays must be
+ * grouped by tile (non-decreasing ids).  vfeat_dev [NV][F] FP32 features,
+ * vdens_dev [NV] FP32 density logits, mlp_dev [NT][P] FP32 MLP parameters.
+ * Rays normalised.  rgb_dev [n*3] out.  form PLAIN_FP32: FP32 CUDA-core MLP;
+ * TC: tcgen05 BF16 MMAs with FP32 accumulation.  Sample records are kept in
+ * a per-scene training workspace (grown on the first call of a larger batch,
+ * n * max_samples_per_ray records) for the backward call. */
 snisr_status snisr_train_forward(snisr_scene* scene, const float* vfeat_dev,
                                  const float* vdens_dev, const float* mlp_dev,
                                  const float* origins_dev, const float* dirs_dev,
-                                 int64_t n, int32_t form, float* rgb_dev, void* stream);
-/* grad_rgb_dev [n*3] = dL/drgb, rgb_dev = the forward output.  Gradients are
+                                 const int32_t* ray_tile_dev, int64_t n, int32_t form,
+                                 float* rgb_dev, void* stream);
+/* Hand-written adjoint of the preceding snisr_train_forward call on the same
+ * scene and rays: per-ray reverse compositing with suffix sums, per-sample
+ * recomputation of features and MLP activations.  grad_rgb_dev [n*3] =
+ * dL/drgb; rgb_dev (the forward output) may be NULL.  Gradients are
  * ACCUMULATED (+=) into gvfeat_dev [NV][F], gvdens_dev [NV], gmlp_dev [NT][P]. */
 snisr_status snisr_train_backward(snisr_scene* scene, const float* vfeat_dev,
                                   const float* vdens_dev, const float* mlp_dev,
                                   const float* origins_dev, const float* dirs_dev,
-                                  int64_t n, int32_t form, const float* rgb_dev,
-                                  const float* grad_rgb_dev, float* gvfeat_dev,
-                                  float* gvdens_dev, float* gmlp_dev, void* stream);
+                                  const int32_t* ray_tile_dev, int64_t n, int32_t form,
+                                  const float* rgb_dev, const float* grad_rgb_dev,
+                                  float* gvfeat_dev, float* gvdens_dev, float* gmlp_dev,
+                                  void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Reference-op drop-ins (argument meaning as in the reference; device ptrs) */

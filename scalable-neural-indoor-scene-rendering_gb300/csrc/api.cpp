@@ -25,6 +25,9 @@ snisr_status set_error(snisr_status st, const std::string& msg) {
   return st;
 }
 
+struct TrainWS;
+TrainWS* train_ws_new();
+void train_ws_free(TrainWS* T);
 cudaError_t launch_expand(const int32_t* corners, const void* vfeat, const void* vdens, int f16, int F, int64_t nvox,
                           float* dens, float4* feat32, uint4* feat16, cudaStream_t st);
 int train_ctrl_words(int NT);
@@ -41,9 +44,8 @@ struct snisr_scene {
   snisr_scene_info info{};
   std::vector<void*> allocs;  // every device allocation of the scene
   // training workspace (allocated lazily at the first training call)
-  void* train_ws = nullptr;
-  size_t train_ws_bytes = 0;
-  int64_t train_rays = 0;
+  TrainWS* train = nullptr;
+  int max_samples_per_ray = 48;
   // host copies needed for MLP re-layout
   int F = 0, H = 0, L = 0, NT = 0, in = 0, P = 0;
   uint32_t* err_host = nullptr;  // pinned mirror of the device error word
@@ -91,7 +93,7 @@ void free_scene(snisr_scene* sc) {
   cudaGetDevice(&prev);
   cudaSetDevice(sc->device);
   for (void* p : sc->allocs) cudaFree(p);
-  if (sc->train_ws) cudaFree(sc->train_ws);
+  if (sc->train) train_ws_free(sc->train);
   if (sc->err_host) cudaFreeHost(sc->err_host);
   for (cudaEvent_t e : sc->ev)
     if (e) cudaEventDestroy(e);
@@ -231,6 +233,14 @@ snisr_status cam_to_dev(const snisr_camera* c, CamDev& out) {
 }  // namespace
 
 namespace snisr {
+snisr_status scene_train_ws(snisr_scene* sc, TrainWS** out, int* num_sms, int* msr) {
+  if (!sc) return set_error(SNISR_INVALID_ARG, "scene is null");
+  if (!sc->train) sc->train = train_ws_new();
+  *out = sc->train;
+  *num_sms = sc->num_sms;
+  *msr = sc->max_samples_per_ray;
+  return SNISR_OK;
+}
 snisr_status scene_views(snisr_scene* sc, SceneDev* S, Workspace* ws, int* device) {
   if (!sc) return set_error(SNISR_INVALID_ARG, "scene is null");
   *S = sc->S;
@@ -458,6 +468,8 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
   I.params_per_tile = sc->P;
   I.sample_capacity = cap;
   sc->corners = d_corners;
+  sc->S.corners = d_corners;
+  sc->max_samples_per_ray = std::max(d->max_samples_per_ray, 1);
   *out = sc;
   return SNISR_OK;
 }

@@ -79,6 +79,7 @@ struct RayState {
   float tmax[3], tdelta[3];
   bool tile_live;     // tile DDA still inside the grid
   bool pending_tile;  // current tile-DDA cell not yet opened
+  bool entry_pending; // tile opened, its entry voxel not yet examined
   // voxel DDA inside the current tile
   int tile;        // sparse id, -1 when no tile is open
   float t_in, q[3];
@@ -97,6 +98,7 @@ struct RayState {
     tile = -1;
     in_voxel = false;
     tile_live = false;
+    entry_pending = false;
     steps = 0;
     const int g[3] = {S.gx, S.gy, S.gz};
     float size[3], half[3], cen[3];
@@ -132,6 +134,11 @@ struct RayState {
     int dense = (tc[0] * S.gy + tc[1]) * S.gz + tc[2];
     int id = __ldg(S.tile_index + dense);
     if (id < 0) return false;
+    return open_tile_id(S, id);
+  }
+
+  // Per-tile AABB clip and voxel-DDA set-up for sparse tile `id`.
+  __device__ bool open_tile_id(const SceneDev& S, int id) {
     float c[3], h[3];
     for (int a = 0; a < 3; ++a) { c[a] = __ldg(S.tile_center + 3 * id + a); h[a] = fmul(S.tile_size, 0.5f); }
     float2 b = slab(o, d, c, h);
@@ -154,7 +161,22 @@ struct RayState {
     }
     near_ = 0.0f;
     tile = id;
+    entry_pending = true;
     return true;
+  }
+
+  // Ray segment restricted to sparse tile `id` (training rays split at tile
+  // faces): no tile DDA, the segment ends where the ray leaves the tile.
+  __device__ bool init_segment(const SceneDev& S, const float* oo, const float* dd, int id) {
+    for (int a = 0; a < 3; ++a) { o[a] = oo[a]; d[a] = dd[a]; }
+    t_start = 0.0f;
+    tile = -1;
+    in_voxel = false;
+    tile_live = false;
+    pending_tile = false;
+    entry_pending = false;
+    steps = 0;
+    return open_tile_id(S, id);
   }
 
   // One Amanatides-Woo step with the reference tie rule: x only when strictly
@@ -199,7 +221,10 @@ struct RayState {
         if (!pending_tile && !step_tile(S)) return false;
         pending_tile = false;
         if (!open_tile(S)) continue;
+      }
+      if (entry_pending) {
         // the entry voxel of the freshly opened tile
+        entry_pending = false;
         ++steps;
         far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
         int vid = (vc[0] * N + vc[1]) * N + vc[2];

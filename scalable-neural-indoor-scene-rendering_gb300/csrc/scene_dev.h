@@ -34,6 +34,7 @@ struct SceneDev {
   const OccWord* occ;            // [NT][words_per_tile]
   const uint32_t* block_mask;    // [NT][(N/4)^3 / 32] coarse 4^3-block occupancy
   const float* dens;             // [NVOX][8] density logits per corner
+  const int32_t* corners;        // [NVOX][8] vertex ids (training gathers/scatters)
   const float4* feat32;          // [NVOX][F/4][8] float4 per (channel group, corner)
   const uint4* feat16;           // [NVOX][8][F/8] 8 halves per (corner, channel group)
   const float* mlp_plain;        // [NT][plain stride] padded FP32 weights

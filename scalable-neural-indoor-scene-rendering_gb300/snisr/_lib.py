@@ -111,8 +111,8 @@ _SIGNATURES = {
     "snisr_trace_voxels": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P]),
     "snisr_render_rays": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P, P]),
     "snisr_render_rays_noalloc": (C.c_int, [P, P, P, C.c_int64, P, P, P, P]),
-    "snisr_train_forward": (C.c_int, [P, P, P, P, P, P, C.c_int64, C.c_int32, P, P]),
-    "snisr_train_backward": (C.c_int, [P, P, P, P, P, P, C.c_int64, C.c_int32, P, P, P, P, P, P]),
+    "snisr_train_forward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, P]),
+    "snisr_train_backward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, P, P, P, P, P]),
     "snisr_op_compute_rays": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P]),
     "snisr_op_tracing_tiles": (C.c_int, [P, C.c_int64, P, P, P, P, P, C.c_float, C.c_int32, P, P]),
     "snisr_op_sample_sparse": (C.c_int, [P, P, C.c_int64, P, C.c_float, C.c_float, C.c_float, C.c_float,
