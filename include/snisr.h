@@ -54,7 +54,10 @@ typedef enum snisr_dtype { SNISR_F32 = 0, SNISR_F16 = 1 } snisr_dtype;
  * math on CUDA cores.  TC: batched form — traversal emits compacted samples,
  * grouped by tile, and the per-tile MLP runs as tcgen05 FP16 MMAs with FP32
  * accumulation in tensor memory. */
-typedef enum snisr_form { SNISR_FORM_PLAIN_FP32 = 0, SNISR_FORM_TC = 1 } snisr_form;
+typedef enum snisr_form {
+  SNISR_FORM_PLAIN_FP32 = 0, /* CUDA cores, FP32                                        */
+  SNISR_FORM_TC = 1          /* tensor cores: render FP16 operands; training split BF16 */
+} snisr_form;
 
 /* ------------------------------------------------------------------------ */
 /* Scene description (host arrays, borrowed for the duration of create).     */
@@ -304,12 +307,15 @@ snisr_status snisr_scene_stage_times(snisr_scene* scene, float* ms, int32_t cap,
  * out[1] voxel DDA steps, out[2] sample slots reserved, out[3] MLP chunks. */
 snisr_status snisr_scene_frame_stats(snisr_scene* scene, int64_t* out, void* stream);
 
-/* Diagnostics: one 128 x N x 64 tcgen05 MMA (N = 32 or 64) through the
- * descriptors of the tensor-core MLP.  A [128][64], B [N][64] row-major FP16
- * (bf16 = 0) or BF16 (bf16 = 1) bit patterns, D [128][N] FP32 = A * B^T.
+/* Diagnostics of the tcgen05 operand layouts.  mode 0: one 128 x N x 64 MMA
+ * (N = 32 or 64) through the descriptors of the tensor-core MLP: A [128][64],
+ * B [N][64] row-major FP16 (bf16 = 0) or BF16 (bf16 = 1) bit patterns,
+ * D [128][N] FP32 = A * B^T.  mode 1/2 (N = 64): At [128][64], Bt [128][64]
+ * stored sample-major and consumed as MN-major operands, D [128][64] with
+ * D[m][n] = sum_k At[k][m] Bt[k][n] for m < 64 (two stride conventions).
  * Synchronises `stream`. */
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev,
-                            int32_t N, int32_t bf16, void* stream);
+                            int32_t N, int32_t bf16, int32_t mode, void* stream);
 
 const char* snisr_last_error_string(void);
 const char* snisr_version(void);

@@ -69,8 +69,8 @@ def lib() -> C.CDLL:
             "oracle_volume_rendering": (None, [P, P, P, C.c_int64, C.c_int, C.c_float, P, P, P]),
             "oracle_positional_encoding": (None, [P, C.c_int64, C.c_int, P]),
             "oracle_grid_sample": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]),
-            "oracle_train_forward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, C.c_int]),
-            "oracle_train_backward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
+            "oracle_train_forward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, C.c_int, C.c_int]),
+            "oracle_train_backward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -85,6 +85,9 @@ def _p(a: np.ndarray | None):
         return None
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.c_void_p)
+
+
+_EMUL = {None: 0, "tc": 1}
 
 
 def threads() -> int:
@@ -120,19 +123,21 @@ class OracleScene:
         lib().oracle_trace(self._h, _p(o), _p(d), _p(t_start), n, K, _p(vis), _p(cnt), nthreads or threads())
         return vis, cnt
 
-    def train_forward(self, vfeat, vdens, mlp, o, d, ray_tile, nthreads: int | None = None):
-        """FP64 colours [n,3] and sample counts [n] of ray segments (ray i inside tile ray_tile[i])."""
+    def train_forward(self, vfeat, vdens, mlp, o, d, ray_tile, nthreads: int | None = None, emulate: str | None = None):
+        """FP64 colours [n,3] and sample counts [n] of ray segments (ray i inside tile ray_tile[i]).
+        emulate: None (exact) or "tc" -- round the MLP operands as the tensor-core form does
+        (split BF16 hi+lo forward operands, BF16 backward operands)."""
         n = o.shape[0]
         rgb = np.zeros((n, 3))
         cnt = np.zeros(n, np.int32)
         args = [np.ascontiguousarray(a, np.float32) for a in (vfeat, vdens, mlp)]
         rt = np.ascontiguousarray(ray_tile, np.int32)
         lib().oracle_train_forward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(rgb), _p(cnt),
-                                   nthreads or threads())
+                                   nthreads or threads(), _EMUL[emulate])
         return rgb, cnt
 
-    def train_backward(self, vfeat, vdens, mlp, o, d, ray_tile, grad_rgb):
-        """FP64 gradients of sum(grad_rgb * rgb): (d vfeat, d vdens, d mlp)."""
+    def train_backward(self, vfeat, vdens, mlp, o, d, ray_tile, grad_rgb, emulate: str | None = None):
+        """FP64 gradients of sum(grad_rgb * rgb): (d vfeat, d vdens, d mlp).  emulate as in train_forward."""
         n = o.shape[0]
         args = [np.ascontiguousarray(a, np.float32) for a in (vfeat, vdens, mlp)]
         gF = np.zeros(args[0].shape)
@@ -141,7 +146,7 @@ class OracleScene:
         rt = np.ascontiguousarray(ray_tile, np.int32)
         g = np.ascontiguousarray(grad_rgb, np.float64)
         lib().oracle_train_backward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(g), _p(gF), _p(gG),
-                                    _p(gW))
+                                    _p(gW), _EMUL[emulate])
         return gF, gG, gW
 
     def render(self, o, d, t_start, form: int, nthreads: int | None = None):

@@ -595,10 +595,34 @@ void march_one_tile(const Scene& s, int id, const float o[3], const float d[3], 
   }
 }
 
+// round to nearest-even BF16, returned as float
+float round_bf16(float f) {
+  uint32_t x;
+  std::memcpy(&x, &f, 4);
+  if ((x & 0x7F800000u) == 0x7F800000u) return f;
+  x += 0x7FFFu + ((x >> 16) & 1u);
+  x &= 0xFFFF0000u;
+  std::memcpy(&f, &x, 4);
+  return f;
+}
+
 struct TrainParams {
   const float* vfeat;  // [NV][F]
   const float* vdens;  // [NV]
   const float* mlp;    // [NT][P]
+  // emul = 1: operand emulation of the tensor-core training form.  Forward
+  // products (and the backward's recomputation) use split BF16 operands,
+  // v = hi + lo with hi = bf16(v), lo = bf16(v - hi): MLP inputs, weights,
+  // biases and post-ReLU activations (rf).  Backward products use single
+  // BF16 operands (rb): the output-logit gradient, each hidden delta, W^T in
+  // the data gradient and the activation in the weight gradient.
+  int emul = 0;
+  double rf(double v) const {
+    if (emul == 0) return v;
+    const float hi = round_bf16((float)v);
+    return (double)hi + (double)round_bf16((float)v - hi);
+  }
+  double rb(double v) const { return emul == 0 ? v : (double)round_bf16((float)v); }
 };
 
 // Forward of one segment; returns the samples (with activations) and colour.
@@ -625,9 +649,11 @@ void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const flo
       ts.alpha = 1.0 - std::exp(-ts.sigma * ts.dv);
       ts.T = T;
       ts.x.assign((size_t)s.in, 0.0);
-      for (int c = 0; c < s.F; ++c)
+      for (int c = 0; c < s.F; ++c) {
         for (int k = 0; k < 8; ++k) ts.x[(size_t)c] += ts.w[k] * (double)p.vfeat[(int64_t)cn[k] * s.F + c];
-      for (int i = 0; i < 27; ++i) ts.x[(size_t)(s.F + i)] = enc[(size_t)i];
+        ts.x[(size_t)c] = p.rf(ts.x[(size_t)c]);
+      }
+      for (int i = 0; i < 27; ++i) ts.x[(size_t)(s.F + i)] = p.rf(enc[(size_t)i]);
       // MLP with stored activations
       std::vector<double> cur = ts.x;
       int64_t off = 0;
@@ -635,9 +661,9 @@ void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const flo
         int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
         std::vector<double> nx((size_t)fo);
         for (int oo = 0; oo < fo; ++oo) {
-          double acc = W[off + (int64_t)fi * fo + oo];
-          for (int i = 0; i < fi; ++i) acc += (double)W[off + (int64_t)oo * fi + i] * cur[(size_t)i];
-          nx[(size_t)oo] = l < s.L ? std::max(acc, 0.0) : acc;
+          double acc = p.rf(W[off + (int64_t)fi * fo + oo]);
+          for (int i = 0; i < fi; ++i) acc += p.rf(W[off + (int64_t)oo * fi + i]) * cur[(size_t)i];
+          nx[(size_t)oo] = l < s.L ? p.rf(std::max(acc, 0.0)) : acc;
         }
         off += (int64_t)fi * fo + fo;
         if (l < s.L) ts.h.push_back(nx);
@@ -675,7 +701,7 @@ void train_backward_ray(const Scene& s, const TrainParams& p, int tile, const st
     for (int k = 0; k < 8; ++k) gG[t.corners[k]] += t.w[k] * ds;
     // MLP backward
     std::vector<double> delta(3);
-    for (int c = 0; c < 3; ++c) delta[(size_t)c] = g[c] * t.T * t.alpha * t.c[c] * (1.0 - t.c[c]);
+    for (int c = 0; c < 3; ++c) delta[(size_t)c] = p.rb(g[c] * t.T * t.alpha * t.c[c] * (1.0 - t.c[c]));
     // layer offsets
     std::vector<int64_t> offs;
     int64_t off = 0;
@@ -689,13 +715,13 @@ void train_backward_ray(const Scene& s, const TrainParams& p, int tile, const st
       const std::vector<double>& in = l == 0 ? t.x : t.h[(size_t)l - 1];
       for (int oo = 0; oo < fo; ++oo) {
         GW[offs[(size_t)l] + (int64_t)fi * fo + oo] += delta[(size_t)oo];
-        for (int ii = 0; ii < fi; ++ii) GW[offs[(size_t)l] + (int64_t)oo * fi + ii] += delta[(size_t)oo] * in[(size_t)ii];
+        for (int ii = 0; ii < fi; ++ii) GW[offs[(size_t)l] + (int64_t)oo * fi + ii] += delta[(size_t)oo] * p.rb(in[(size_t)ii]);
       }
       std::vector<double> prev((size_t)fi, 0.0);
       for (int ii = 0; ii < fi; ++ii) {
         double acc = 0;
-        for (int oo = 0; oo < fo; ++oo) acc += (double)W[offs[(size_t)l] + (int64_t)oo * fi + ii] * delta[(size_t)oo];
-        if (l > 0) acc = t.h[(size_t)l - 1][(size_t)ii] > 0.0 ? acc : 0.0;
+        for (int oo = 0; oo < fo; ++oo) acc += p.rb(W[offs[(size_t)l] + (int64_t)oo * fi + ii]) * delta[(size_t)oo];
+        if (l > 0) acc = t.h[(size_t)l - 1][(size_t)ii] > 0.0 ? p.rb(acc) : 0.0;
         prev[(size_t)ii] = acc;
       }
       delta.swap(prev);
@@ -889,12 +915,13 @@ void oracle_op_integrate(const float* rgba, const float* dz, int64_t npix, float
 }
 
 // Training forward (FP64): rgb [n][3] of ray segments (ray i inside tile
-// ray_tile[i]); counts [n] (optional) = samples per segment.
+// ray_tile[i]); counts [n] (optional) = samples per segment.  emul: 1 =
+// operand emulation of the tensor-core form (TrainParams), 0 = exact.
 void oracle_train_forward(const oracle_scene* os, const float* vfeat, const float* vdens, const float* mlp,
                           const float* o, const float* d, const int32_t* ray_tile, int64_t n, double* rgb,
-                          int32_t* counts, int threads) {
+                          int32_t* counts, int threads, int emul) {
   const Scene& s = *reinterpret_cast<const Scene*>(os);
-  TrainParams p{vfeat, vdens, mlp};
+  TrainParams p{vfeat, vdens, mlp, emul};
   parallel_for(n, threads, [&](int64_t i) {
     std::vector<TrainSample> S;
     train_forward_ray(s, p, ray_tile[i], o + 3 * i, d + 3 * i, S, rgb + 3 * i);
@@ -907,9 +934,9 @@ void oracle_train_forward(const oracle_scene* os, const float* vfeat, const floa
 // (deterministic accumulation order).
 void oracle_train_backward(const oracle_scene* os, const float* vfeat, const float* vdens, const float* mlp,
                            const float* o, const float* d, const int32_t* ray_tile, int64_t n,
-                           const double* grad_rgb, double* gF, double* gG, double* gW) {
+                           const double* grad_rgb, double* gF, double* gG, double* gW, int emul) {
   const Scene& s = *reinterpret_cast<const Scene*>(os);
-  TrainParams p{vfeat, vdens, mlp};
+  TrainParams p{vfeat, vdens, mlp, emul};
   std::vector<TrainSample> S;
   for (int64_t i = 0; i < n; ++i) {
     double C[3];

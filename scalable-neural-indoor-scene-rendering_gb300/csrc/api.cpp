@@ -628,10 +628,11 @@ snisr_status snisr_scene_frame_stats(snisr_scene* sc, int64_t* out, void* stream
 }
 
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev, int32_t N, int32_t bf16,
-                            void* stream) {
-  if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1))
+                            int32_t mode, void* stream) {
+  if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1) || mode < 0 || mode > 2 ||
+      (mode != 0 && N != 64))
     return set_error(SNISR_INVALID_ARG, "diag_mma: bad argument");
-  cudaError_t e = launch_diag_mma(A_dev, B_dev, D_dev, N, bf16, (cudaStream_t)stream);
+  cudaError_t e = launch_diag_mma(A_dev, B_dev, D_dev, N, bf16, mode, (cudaStream_t)stream);
   if (e == cudaErrorLaunchTimeout) return set_error(SNISR_DEVICE_TIMEOUT, "diag_mma: MMA completion wait ran out");
   CUDA_TRY(e, "diag_mma");
   return SNISR_OK;

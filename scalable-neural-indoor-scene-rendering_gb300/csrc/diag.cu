@@ -1,0 +1,110 @@
+// Diagnostics of the tcgen05 operand layouts (used by the GPU tests).
+//
+// mode 0: A [128][64], B [N][64] K-major (the MLP's forward layout),
+//         D = A B^T (K = 64).
+// mode 1/2: At [128][64], Bt [128][64] stored sample-major (row = K index,
+//         the layout the epilogues write), consumed as MN-major operands,
+//         D[m][n] = sum_k At[k][m] Bt[k][n] for m < 64 (K = 128), the second
+//         64-row atom of A pointing at a zero tile.  Mode 1: leading byte
+//         offset = MN atom stride, stride byte offset = 8-row K group stride;
+//         mode 2: the two swapped.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+namespace snisr {
+namespace {
+
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+__global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const uint16_t* B, float* D, int N,
+                                                       int bf16, int mode, int* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* As = base;               // 16 KB
+  uint8_t* Zs = base + 16384;       // 16 KB zeros
+  uint8_t* Bs = base + 32768;       // 16 KB (+16 KB slack)
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 65536);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // zero [Zs, base + 64 KB): the zero tile, the B tile and its slack
+  for (int k = tid; k < (65536 - 16384) / 16; k += 128) reinterpret_cast<uint4*>(Zs)[k] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+  const int brows = mode == 0 ? N : 128;
+  for (int c = 0; c < 8; ++c) {
+    *reinterpret_cast<uint4*>(As + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(A + tid * 64 + 8 * c);
+    if (tid < brows)
+      *reinterpret_cast<uint4*>(Bs + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(B + tid * 64 + 8 * c);
+  }
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_addr(bar), 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(slot), 64);
+    tc::tmem_relinquish();
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *slot;
+  if (tid == 0) {
+    if (mode == 0) {
+      const uint32_t idesc = tc::idesc_f16(N, bf16);
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_f16(tmem, tc::sdesc_sw128(tc::smem_addr(As) + 32 * kk), tc::sdesc_sw128(tc::smem_addr(Bs) + 32 * kk),
+                    idesc, kk > 0);
+    } else {
+      const uint32_t idesc = tc::idesc_f16(64, bf16) | (1u << 15) | (1u << 16);  // A, B MN-major
+      const uint32_t lbo = mode == 1 ? 16384u : 1024u, sbo = mode == 1 ? 1024u : 16384u;
+      for (int kk = 0; kk < 8; ++kk)
+        tc::mma_f16(tmem, sdesc_sw128_mn(tc::smem_addr(As) + 2048 * kk, lbo, sbo),
+                    sdesc_sw128_mn(tc::smem_addr(Bs) + 2048 * kk, lbo, sbo), idesc, kk > 0);
+    }
+    tc::mma_commit(tc::smem_addr(bar));
+  }
+  bool ok = tid == 0 ? tc::mbar_wait(tc::smem_addr(bar), 0) : true;
+  tc::fence_after_sync();
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) *status = 1;
+  } else {
+    const int nc = mode == 0 ? N : 64;
+    float v[64];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int cc = 0; cc < nc; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
+    tc::tmem_wait_ld();
+    for (int j = 0; j < nc; ++j) D[tid * nc + j] = v[j];
+    if (tid == 0) *status = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+}  // namespace
+
+cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
+                            cudaStream_t st) {
+  int* status = nullptr;
+  cudaError_t e = cudaMallocAsync(&status, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int smem = 1024 + 65536 + 64;
+  e = cudaFuncSetAttribute(diag_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) {
+    diag_mma_kernel<<<1, 128, smem, st>>>(A, B, D, N, bf16, mode, status);
+    e = cudaGetLastError();
+  }
+  int h = -1;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(status, st);
+  if (e == cudaSuccess && h != 0) e = cudaErrorLaunchTimeout;
+  return e;
+}
+
+}  // namespace snisr

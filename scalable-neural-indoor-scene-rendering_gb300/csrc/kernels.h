@@ -48,6 +48,31 @@ cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int 
                          int32_t* count, cudaStream_t st);
 cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t,
                          int32_t* tri, cudaStream_t st);
-cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, cudaStream_t st);
+// Tensor-core training MLP (forward colours / backward with recomputation).
+struct TrainTcArgs {
+  const float* vfeat;
+  const float* mlp;
+  const float* dirs;
+  int64_t n;
+  const void* recs;
+  const int32_t* tstart;
+  int32_t* coff;
+  int* work;
+  uint4* enc;
+  uint8_t* wimg;
+  int img_stride;
+  float4* cout;
+  const float4* dout;
+  float* gvfeat;
+  float* gmlp;
+  int num_sms;
+};
+int train_tc_image_bytes(int H, int L);
+int train_tc_bwd_smem_bytes(int H, int L);
+// enc: [n][8] uint4 (BF16 hi / lo view encoding)
+cudaError_t launch_train_tc(const SceneDev& S, const TrainTcArgs& a, bool backward, cudaStream_t st);
+
+cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
+                            cudaStream_t st);
 
 }  // namespace snisr

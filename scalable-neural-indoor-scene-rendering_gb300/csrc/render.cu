@@ -597,59 +597,6 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   if (warp == 0) tc::tmem_dealloc(tmem, H);
 }
 
-// Diagnostic: one 128 x N x 64 MMA through the same descriptors as the MLP
-// kernel.  A [128][64], B [N][64] row-major 16-bit, D [128][N] FP32.
-__global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const uint16_t* B, float* D, int N,
-                                                       int bf16, int* status) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* As = base;
-  uint8_t* Bs = base + 16384;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 16384 + 8192);
-  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  for (int c = 0; c < 8; ++c) {
-    *reinterpret_cast<uint4*>(As + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(A + tid * 64 + 8 * c);
-    if (tid < N)
-      *reinterpret_cast<uint4*>(Bs + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(B + tid * 64 + 8 * c);
-  }
-  if (tid == 0) {
-    tc::mbar_init(tc::smem_addr(bar), 1);
-    tc::fence_mbar_init();
-  }
-  if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(slot), 64);
-    tc::tmem_relinquish();
-  }
-  tc::fence_proxy_async();
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = *slot;
-  if (tid == 0) {
-    const uint32_t idesc = tc::idesc_f16(N, bf16);
-    for (int kk = 0; kk < 4; ++kk)
-      tc::mma_f16(tmem, tc::sdesc_sw128(tc::smem_addr(As) + 32 * kk), tc::sdesc_sw128(tc::smem_addr(Bs) + 32 * kk),
-                  idesc, kk > 0);
-    tc::mma_commit(tc::smem_addr(bar));
-  }
-  bool ok = tc::mbar_wait(tc::smem_addr(bar), 0);
-  tc::fence_after_sync();
-  if (__syncthreads_or(!ok)) {
-    if (tid == 0) *status = 1;
-  } else {
-    float v[64];
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int cc = 0; cc < N; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
-    tc::tmem_wait_ld();
-    for (int j = 0; j < N; ++j) D[tid * N + j] = v[j];
-    if (tid == 0) *status = 0;
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
-}
-
 inline int grid_for(int64_t n, int threads, int cap_blocks) {
   int64_t b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -765,24 +712,6 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[4], st)) != cudaSuccess) return e;
   return cudaSuccess;
-}
-
-cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, cudaStream_t st) {
-  int* status = nullptr;
-  cudaError_t e = cudaMallocAsync(&status, sizeof(int), st);
-  if (e != cudaSuccess) return e;
-  const int smem = 1024 + 16384 + 8192 + 64;
-  e = cudaFuncSetAttribute(diag_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) {
-    diag_mma_kernel<<<1, 128, smem, st>>>(A, B, D, N, bf16, status);
-    e = cudaGetLastError();
-  }
-  int h = -1;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFreeAsync(status, st);
-  if (e == cudaSuccess && h != 0) e = cudaErrorLaunchTimeout;
-  return e;
 }
 
 }  // namespace snisr

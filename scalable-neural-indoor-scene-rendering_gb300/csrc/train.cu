@@ -153,14 +153,15 @@ __global__ void scan_pass3(const int32_t* cnt, int64_t n, const int32_t* bsum, i
 
 // per-tile sample ranges (rays sorted by tile): start[t] = off[first ray with tile >= t]
 __global__ void tile_ranges_kernel(const int32_t* __restrict__ ray_tile, const int32_t* __restrict__ off, int64_t n,
-                                   const int32_t* total, int NT, int32_t* start, uint32_t* err) {
+                                   const int32_t* total, int NT, int64_t cap, int32_t* start, uint32_t* err) {
   for (int t = threadIdx.x; t <= NT; t += blockDim.x) {
     int64_t lo = 0, hi = n;  // first index with ray_tile >= t
     while (lo < hi) {
       int64_t mid = (lo + hi) >> 1;
       if (ray_tile[mid] < t) lo = mid + 1; else hi = mid;
     }
-    start[t] = lo < n ? off[lo] : *total;
+    const int64_t v = lo < n ? off[lo] : *total;
+    start[t] = (int32_t)(v < cap ? v : cap);  // records beyond the capacity were not written
   }
   // rays must be grouped by tile (non-decreasing ids)
   for (int64_t i = threadIdx.x + 1; i < n; i += blockDim.x)
@@ -454,6 +455,11 @@ cudaError_t train_plain_mlp_bwd(const SceneDev& S, const float* vfeat, const flo
 // ---------------------------------------------------------------------------
 struct TrainWS {
   int64_t rays = 0, cap = 0;
+  int32_t* coff = nullptr;
+  int* work = nullptr;
+  uint4* enc = nullptr;
+  uint8_t* wimg = nullptr;
+  int img_stride = 0;
   int32_t *cnt = nullptr, *off = nullptr, *bsum = nullptr, *total = nullptr, *tstart = nullptr;
   TrainRec* recs = nullptr;
   float4 *c = nullptr, *dout = nullptr;
@@ -461,6 +467,7 @@ struct TrainWS {
   void* block = nullptr;
   size_t bytes = 0;
   int64_t last_n = -1;
+  int last_form = -1;
 };
 
 snisr_status scene_views(snisr_scene* scene, SceneDev* S, Workspace* ws, int* device);
@@ -472,8 +479,10 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT) {
   T->block = nullptr;
   const int64_t rays = n, cap = n * (int64_t)msr, nb = (rays + 1023) / 1024 + 2;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const int img_stride = (train_tc_image_bytes(64, 3) + 127) & ~127;
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
-              al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4);
+              al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al((NT + 2) * 4) + al(16) +
+              al(rays * 128) + al((size_t)img_stride * NT);
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, sz);
   if (e != cudaSuccess) return set_error(SNISR_OOM, std::string("train workspace: ") + cudaGetErrorString(e));
@@ -489,6 +498,11 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT) {
   T->dout = (float4*)take(cap * 16);
   T->act = (float*)take(cap * kActStride * 4);
   T->dlt = (float*)take(cap * kDltStride * 4);
+  T->coff = (int32_t*)take((NT + 2) * 4);
+  T->work = (int*)take(16);
+  T->enc = (uint4*)take(rays * 128);
+  T->wimg = (uint8_t*)take((size_t)img_stride * NT);
+  T->img_stride = img_stride;
   T->block = p;
   T->bytes = sz;
   T->rays = rays;
@@ -533,7 +547,7 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
   TR_TRY(cudaGetLastError(), "train: scan");
   tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, vdens, orig, dirs, ray_tile, n, T->cnt, T->off, T->recs, T->cap, 1);
   TR_TRY(cudaGetLastError(), "train: write");
-  tile_ranges_kernel<<<1, 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->tstart, S.err);
+  tile_ranges_kernel<<<1, 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->cap, T->tstart, S.err);
   TR_TRY(cudaGetLastError(), "train: tile ranges");
   return SNISR_OK;
 }
@@ -557,13 +571,19 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   if (s != SNISR_OK) return s;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
   cudaError_t e;
-  if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
+  if (form != SNISR_FORM_PLAIN_FP32) {
+    TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
+                  T->c, T->dout, nullptr, nullptr, num_sms};
+    e = launch_train_tc(S, a, false, st);
+    if (e == cudaErrorInvalidValue) return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
+  } else if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
   else if (F == 16 && H == 32 && L == 2) e = train_plain_mlp_fwd<16, 32, 2>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
   else return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
   TR_TRY(e, "train_forward: mlp");
   tr_composite_fwd<<<gridn(n, 128), 128, 0, st>>>(T->recs, T->c, T->cnt, T->off, n, T->cap, rgb);
   TR_TRY(cudaGetLastError(), "train_forward: composite");
   T->last_n = n;
+  T->last_form = form;
   return SNISR_OK;
 }
 
@@ -594,7 +614,12 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
   const int64_t max_tile = T->cap;  // upper bound; empty blocks exit at once
   cudaError_t e;
-  if (F == 32 && H == 64 && L == 3)
+  if (T->last_form != form) return set_error(SNISR_INVALID_ARG, "train_backward: the forward call used another form");
+  if (form != SNISR_FORM_PLAIN_FP32) {
+    TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
+                  T->c, T->dout, gvfeat, gmlp, num_sms};
+    e = launch_train_tc(S, a, true, st);
+  } else if (F == 32 && H == 64 && L == 3)
     e = train_plain_mlp_bwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->dout, T->act, T->dlt, gvfeat,
                                         T->tstart, max_tile, gmlp, num_sms, st);
   else if (F == 16 && H == 32 && L == 2)

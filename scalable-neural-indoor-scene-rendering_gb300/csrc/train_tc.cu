@@ -1,0 +1,667 @@
+// Tensor-core (tcgen05, BF16 operands, FP32 accumulation) form of the
+// training MLP: forward colours and the backward pass with per-chunk
+// recomputation of the activations.
+//
+// Samples are processed in chunks of 128 rows of one tile (chunk lists are
+// per tile).  Activation tiles are written by the epilogues in the 128-byte
+// swizzled layout with one sample per row; the same tiles serve as K-major
+// A operands (samples = M) of the forward/backward data GEMMs and as MN-major
+// operands (samples = K) of the weight-gradient GEMMs, whose accumulators
+// stay in tensor memory across all chunks of a tile and are flushed with
+// atomics when the CTA moves to another tile.
+//
+// Precision.  Forward products (and the backward's recomputation of them)
+// use split BF16 operands: v = hi + lo, hi = bf16(v), lo = bf16(v - hi), and
+// A.B = A_hi.B_hi + A_lo.B_hi + A_hi.B_lo, about 16 significant bits.  The
+// ReLU masks of the backward then follow an FP32 evaluation except within
+// ~2^-16 of a kink; with single BF16 operands the masks of units near a kink
+// flip and the feature gradients move by several percent.  Backward products
+// (hidden deltas, weight gradients) use single BF16 operands: their rounding
+// error is smooth (~2^-9 per operand).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+namespace snisr {
+
+namespace {
+
+struct __align__(16) TrainRecT {  // mirror of the record written by the march kernel
+  uint32_t rec, ray, tile, pad0;
+  float f[3], dv;
+  float T, alpha, s, pad1;
+};
+
+constexpr uint32_t kBf16Eighth = 0x3E003E00u;  // 1/8, two lanes
+constexpr uint32_t kBf16One = 0x3F803F80u;     // 1.0, two lanes
+
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xFFFF0000u); }
+// split of two values into BF16 hi and lo pairs
+__device__ __forceinline__ void split_bf2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  hi = pack_bf2(a, b);
+  lo = pack_bf2(a - bf_lo(hi), b - bf_hi(hi));
+}
+__device__ __forceinline__ void split_bf16(float v, uint16_t& hi, uint16_t& lo) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  hi = __bfloat16_as_ushort(h);
+  lo = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+}
+// positive BF16 value in the low / high half (sign clear, not zero)
+__device__ __forceinline__ bool pos_lo(uint32_t v) { return (v & 0x8000u) == 0 && (v & 0x7FFFu) != 0; }
+__device__ __forceinline__ bool pos_hi(uint32_t v) { return (v & 0x80000000u) == 0 && (v & 0x7FFF0000u) != 0; }
+
+// MN-major 128B-swizzled descriptor: lbo = stride between 64-element MN
+// atoms, sbo = stride between 8-row K groups (1024).
+__device__ __forceinline__ uint64_t sdesc_mn(uint32_t saddr, uint32_t lbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)(1024u >> 4) << 32) | ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+__device__ __forceinline__ uint32_t idesc_bf16(int n, bool a_mn, bool b_mn) {
+  return tc::idesc_f16(n, 1) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
+// ---- per-tile weight image -------------------------------------------------
+// All sub-tiles K-major, 128-byte swizzled, 64 K columns:
+//   hi part : W_l [H][64] (l < L), W_out [16][64]
+//   lo part : the same shapes holding bf16(w - hi)
+//   bias    : [H][64], K slice 16l..16l+15 of row o = 8 x hi(b_l[o]), 8 x lo(b_l[o])
+//   out bias: [16][64], K slice 0..15 likewise for the output layer
+//   W^T     : per layer l <= L, [64 rows = inputs of l][K = outputs] (hi only)
+struct ImageLayout {
+  int hi_part, lo_off, bias_off, obias_off, fwd_bytes, t_off, total;
+  __host__ __device__ ImageLayout(int H, int L) {
+    hi_part = L * H * 128 + 2048;
+    lo_off = hi_part;
+    bias_off = 2 * hi_part;
+    obias_off = bias_off + H * 128;
+    fwd_bytes = obias_off + 2048;
+    t_off = fwd_bytes;
+    total = t_off + (L + 1) * 8192;
+  }
+};
+
+__device__ __forceinline__ uint32_t sw_off(int row, int k) {
+  return (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u + ((uint32_t)((k >> 3) ^ (row & 7)) << 4) +
+         (uint32_t)((k & 7) << 1);
+}
+
+__global__ void pack_train_weights(const float* __restrict__ mlp, int P, int IN, int H, int L, int stride,
+                                   uint8_t* out) {
+  const ImageLayout lay(H, L);
+  const int tile = blockIdx.y;
+  uint8_t* img = out + (size_t)tile * stride;
+  const float* p = mlp + (size_t)tile * P;
+  // the image was zeroed by the caller; one thread per parameter
+  int64_t off = 0;
+  for (int l = 0; l <= L; ++l) {
+    const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
+    const int wofs = l < L ? l * H * 128 : L * H * 128;
+    uint8_t* whi = img + wofs;
+    uint8_t* wlo = img + lay.lo_off + wofs;
+    uint8_t* btile = img + (l < L ? lay.bias_off : lay.obias_off);
+    uint8_t* tt = img + lay.t_off + l * 8192;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * fi; e += gridDim.x * blockDim.x) {
+      const int o = e / fi, i = e % fi;
+      uint16_t h, lo;
+      split_bf16(p[off + e], h, lo);
+      *reinterpret_cast<uint16_t*>(whi + sw_off(o, i)) = h;
+      *reinterpret_cast<uint16_t*>(wlo + sw_off(o, i)) = lo;
+      *reinterpret_cast<uint16_t*>(tt + sw_off(i, o)) = h;
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * 16; e += gridDim.x * blockDim.x) {
+      const int o = e / 16, k = e % 16;
+      uint16_t h, lo;
+      split_bf16(p[off + (int64_t)fi * fo + o], h, lo);
+      *reinterpret_cast<uint16_t*>(btile + sw_off(o, (l < L ? 16 * l : 0) + k)) = k < 8 ? h : lo;
+    }
+    off += (int64_t)fi * fo + fo;
+  }
+}
+
+// per-ray view encoding (27 values + 5 zeros) as BF16 hi [0,4) and lo [4,8) uint4s
+__global__ void ray_enc_kernel(const float* __restrict__ dirs, int64_t n, uint4* enc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+    float e[32];
+    dir_encoding(d, 4, e);
+    for (int k = 27; k < 32; ++k) e[k] = 0.f;
+    for (int q = 0; q < 4; ++q) {
+      uint32_t h[4], l[4];
+      for (int j = 0; j < 4; ++j) split_bf2(e[8 * q + 2 * j], e[8 * q + 2 * j + 1], h[j], l[j]);
+      enc[8 * i + q] = make_uint4(h[0], h[1], h[2], h[3]);
+      enc[8 * i + 4 + q] = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
+// chunk lists: chunks of 128 samples never straddle tiles
+__global__ void train_chunks_kernel(const int32_t* __restrict__ tstart, int NT, int32_t* coff) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int c = 0;
+  for (int t = 0; t < NT; ++t) {
+    coff[t] = c;
+    c += (tstart[t + 1] - tstart[t] + 127) / 128;
+  }
+  coff[NT] = c;
+}
+
+struct ChunkPos {
+  int tile, row0, cnt;
+};
+__device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const int32_t* tstart, int NT) {
+  int lo = 0, hi = NT;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(coff + mid) <= c) lo = mid; else hi = mid;
+  }
+  ChunkPos p;
+  p.tile = lo;
+  p.row0 = __ldg(tstart + lo) + (c - __ldg(coff + lo)) * 128;
+  p.cnt = min(128, __ldg(tstart + lo + 1) - p.row0);
+  return p;
+}
+
+// Gather of the split input rows [0,128) of the chunk into Xhi / Xlo: lane
+// (g, row) interpolates 8 FP32 channels over the 8 corners; view encoding
+// copied from the per-ray split table.
+template <int F>
+__device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restrict__ vfeat,
+                                         const TrainRecT* __restrict__ recs, int row0, int cnt,
+                                         const uint4* __restrict__ enc, uint8_t* Xhi, uint8_t* Xlo, int warp, int lane) {
+  constexpr int G = F / 8, RPI = 32 / G;
+  const int my_g = lane / RPI, my_row = lane % RPI;
+  const uint4 z = make_uint4(0, 0, 0, 0);
+  for (int it = 0; it < G; ++it) {
+    const int r = warp * 32 + it * RPI + my_row;
+    if (r < cnt) {
+      const TrainRecT t = recs[row0 + r];
+      float w[8];
+      trilinear_weights(t.f, w);
+      const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)t.rec * 8);
+      const int4 a = __ldg(cn), b = __ldg(cn + 1);
+      const int c[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float4* src = reinterpret_cast<const float4*>(vfeat + (size_t)c[k] * F + 8 * my_g);
+        const float4 v0 = __ldg(src), v1 = __ldg(src + 1);
+        acc[0] = fmaf(w[k], v0.x, acc[0]); acc[1] = fmaf(w[k], v0.y, acc[1]);
+        acc[2] = fmaf(w[k], v0.z, acc[2]); acc[3] = fmaf(w[k], v0.w, acc[3]);
+        acc[4] = fmaf(w[k], v1.x, acc[4]); acc[5] = fmaf(w[k], v1.y, acc[5]);
+        acc[6] = fmaf(w[k], v1.z, acc[6]); acc[7] = fmaf(w[k], v1.w, acc[7]);
+      }
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) split_bf2(acc[2 * j], acc[2 * j + 1], h[j], l[j]);
+      *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, my_g)) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, my_g)) = make_uint4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+      for (int e = my_g; e < 4; e += G) {
+        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)t.ray * 8 + e);
+        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)t.ray * 8 + 4 + e);
+      }
+#pragma unroll
+      for (int ch = G + 4 + my_g; ch < 8; ch += G) {
+        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, ch)) = z;
+        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, ch)) = z;
+      }
+    } else {
+#pragma unroll
+      for (int ch = my_g; ch < 8; ch += G) {
+        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, ch)) = z;
+        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, ch)) = z;
+      }
+    }
+  }
+}
+
+// ReLU + split BF16 pack of a 128 x H accumulator into hi / lo activation
+// tiles (dst_lo may be null: hi only)
+template <int H>
+__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_lo, int row) {
+#pragma unroll
+  for (int half = 0; half < H / 32; ++half) {
+    float v[32];
+    tc::tmem_ld16(taddr + 32 * half, v);
+    tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], l[j]);
+      *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, 4 * half + q)) = make_uint4(h[0], h[1], h[2], h[3]);
+      if (dst_lo)
+        *reinterpret_cast<uint4*>(dst_lo + tc::sw128_offset(row, 4 * half + q)) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
+struct Bars {
+  uint32_t wbar, mbar;
+  uint32_t wphase, mphase;
+};
+
+__device__ __forceinline__ bool wait_mma(Bars& b, int tid) {
+  bool ok = tid == 0 ? tc::mbar_wait(b.mbar, b.mphase) : true;
+  b.mphase ^= 1u;
+  ok = !__syncthreads_or(!ok);
+  tc::fence_after_sync();
+  return ok;
+}
+
+// One split-precision forward layer: tmem = A.W^T + bias with N = n outputs,
+// K = 16 * ksteps.  A_hi.W_hi + A_lo.W_hi + A_hi.W_lo, then the bias step
+// (A = 1/8 everywhere, B slice = 8 x hi, 8 x lo of the bias).
+__device__ __forceinline__ void issue_split_layer(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t w_hi,
+                                                  uint32_t w_lo, uint32_t bias_slice, uint64_t ones8, int n,
+                                                  int ksteps) {
+  const uint32_t id = idesc_bf16(n, false, false);
+  for (int kk = 0; kk < ksteps; ++kk) {
+    const uint64_t ah = tc::sdesc_sw128(a_hi + 32 * kk), al = tc::sdesc_sw128(a_lo + 32 * kk);
+    const uint64_t wh = tc::sdesc_sw128(w_hi + 32 * kk), wl = tc::sdesc_sw128(w_lo + 32 * kk);
+    tc::mma_f16(tmem, ah, wh, id, kk > 0);
+    tc::mma_f16(tmem, al, wh, id, 1);
+    tc::mma_f16(tmem, ah, wl, id, 1);
+  }
+  tc::mma_f16(tmem, ones8, tc::sdesc_sw128(bias_slice), id, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Forward: per-sample colour c = sigmoid(MLP(x)) on tcgen05.
+// ---------------------------------------------------------------------------
+template <int F, int H, int L>
+__global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
+                                                        const TrainRecT* __restrict__ recs,
+                                                        const int32_t* __restrict__ tstart,
+                                                        const int32_t* __restrict__ coff, int* work,
+                                                        const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
+                                                        int img_stride, float4* cout) {
+  const ImageLayout lay(H, L);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* Ahi = base;
+  uint8_t* Alo = base + 16384;
+  uint8_t* Wsm = base + 32768;
+  uint8_t* ones = Wsm + ((lay.fwd_bytes + 1023) & ~1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 1024);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int NT = S.num_tiles;
+  Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
+  if (tid == 0) {
+    tc::mbar_init(B.wbar, 1);
+    tc::mbar_init(B.mbar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 64);
+    tc::tmem_relinquish();
+  }
+  for (int k = tid; k < 64; k += 128)
+    reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16Eighth, kBf16Eighth, kBf16Eighth, kBf16Eighth);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint64_t ones8 = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
+  const int total = coff[NT];
+  int cur_tile = -1;
+  bool failed = false;
+  for (;;) {
+    if (tid == 0) *chunk_slot = atomicAdd(work, 1);
+    __syncthreads();
+    const int c = *chunk_slot;
+    if (c >= total) break;
+    const ChunkPos cp = chunk_pos(c, coff, tstart, NT);
+    const bool new_w = cp.tile != cur_tile;
+    if (new_w && tid == 0) {
+      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.fwd_bytes);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.fwd_bytes, B.wbar);
+    }
+    cur_tile = cp.tile;
+    gather_x<F>(S, vfeat, recs, cp.row0, cp.cnt, enc, Ahi, Alo, warp, lane);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (new_w) {
+      bool ok = tid == 0 ? tc::mbar_wait(B.wbar, B.wphase) : true;
+      B.wphase ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+    }
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t ahi = tc::smem_addr(Ahi), alo = tc::smem_addr(Alo), w = tc::smem_addr(Wsm);
+    float out3[3] = {0.f, 0.f, 0.f};
+    for (int l = 0; l <= L; ++l) {
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t wofs = (uint32_t)(l < L ? l * H * 128 : L * H * 128);
+        const uint32_t bias = l < L ? w + lay.bias_off + 32 * l : w + lay.obias_off;
+        issue_split_layer(tmem, ahi, alo, w + wofs, w + lay.lo_off + wofs, bias, ones8, l < L ? H : 16,
+                          l == 0 ? 4 : H / 16);
+        tc::mma_commit(B.mbar);
+      }
+      if (!wait_mma(B, tid)) { failed = true; break; }
+      if (l < L) {
+        epi_relu_split<H>(taddr, Ahi, Alo, tid);  // the output layer also takes split inputs
+        tc::fence_proxy_async();
+      } else {
+        float v[4];
+        tc::tmem_ld4(taddr, v);
+        tc::tmem_wait_ld();
+        out3[0] = v[0]; out3[1] = v[1]; out3[2] = v[2];
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (failed) break;
+    if (tid < cp.cnt)
+      cout[cp.row0 + tid] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
+  }
+  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------------------
+// Backward on tcgen05.  Tensor memory (512 columns): [0,64) data-GEMM
+// accumulator, then per layer l = 0..L a weight-gradient accumulator
+// (128 lanes = output units, 64 columns = inputs) and a 16-column bias
+// accumulator (column 0 used), both living across the chunks of a tile.
+//
+// Shared memory tiles (16 KB, one sample per 128-byte row), in this order:
+//   D (hidden delta), X (input hi), H1..HL (activation hi), DO (output-logit
+//   gradient), LoA, LoB (lo halves during the recomputation, ping-pong).
+// An MN-major M = 128 operand spans two 64-wide atoms 16 KB apart: for D and
+// DO the second atom is the next tile, whose products land in accumulator
+// lanes 64..127 (output units that do not exist) and are never read.
+// ---------------------------------------------------------------------------
+template <int F, int H, int L>
+__global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float* __restrict__ vfeat,
+                                                        const TrainRecT* __restrict__ recs,
+                                                        const int32_t* __restrict__ tstart,
+                                                        const int32_t* __restrict__ coff, int* work,
+                                                        const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
+                                                        int img_stride, const float4* __restrict__ dout, float* gvfeat,
+                                                        float* gmlp) {
+  constexpr int IN = F + 27;
+  constexpr int kTiles = 5 + L;
+  const ImageLayout lay(H, L);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* Dt = base;
+  uint8_t* Xt = base + 16384;
+  uint8_t* Ht = base + 2 * 16384;  // H_l at Ht + (l-1)*16384, l = 1..L
+  uint8_t* DOt = base + (2 + L) * 16384;
+  uint8_t* LoA = DOt + 16384;
+  uint8_t* LoB = LoA + 16384;
+  uint8_t* Wsm = base + kTiles * 16384;
+  uint8_t* ones = Wsm + ((lay.total + 1023) & ~1023);  // 1 KB of 1/8, 1 KB of 1.0
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 2048);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int NT = S.num_tiles;
+  Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
+  if (tid == 0) {
+    tc::mbar_init(B.wbar, 1);
+    tc::mbar_init(B.mbar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
+    tc::tmem_relinquish();
+  }
+  for (int k = tid; k < 64; k += 128) {
+    reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16Eighth, kBf16Eighth, kBf16Eighth, kBf16Eighth);
+    reinterpret_cast<uint4*>(ones + 1024)[k] = make_uint4(kBf16One, kBf16One, kBf16One, kBf16One);
+  }
+  // all tiles start zeroed: DO columns beyond 3 and the columns beyond H of
+  // the activation / delta tiles are never written afterwards
+  for (int k = tid; k < kTiles * 16384 / 16; k += 128) reinterpret_cast<uint4*>(base)[k] = make_uint4(0, 0, 0, 0);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tw = tmem;  // data accumulator
+  auto tdw = [&](int l) { return tmem + 64u + 64u * (uint32_t)l; };
+  auto tdb = [&](int l) { return tmem + 64u + 64u * (uint32_t)(L + 1) + 16u * (uint32_t)l; };
+  const uint64_t ones8 = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
+  const uint64_t ones1 = tc::sdesc_sw128_sbo(tc::smem_addr(ones + 1024), 0);
+  const int total = coff[NT];
+  int cur_tile = -1;
+  bool failed = false, have_acc = false;
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+
+  // flush the weight/bias gradient accumulators of `tile` to global memory
+  auto flush = [&](int tile) {
+    float* G = gmlp + (size_t)tile * S.params_per_tile;
+    int64_t off = 0;
+    for (int l = 0; l <= L; ++l) {
+      const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
+      float v[64];
+      for (int cc = 0; cc < 64; cc += 16) tc::tmem_ld16(taddr + 64u + 64u * l + cc, v + cc);
+      float bv[4];
+      tc::tmem_ld4(taddr + 64u + 64u * (L + 1) + 16u * l, bv);
+      tc::tmem_wait_ld();
+      if (tid < fo) {
+        for (int i = 0; i < fi; ++i) atomicAdd(G + off + (int64_t)tid * fi + i, v[i]);
+        atomicAdd(G + off + (int64_t)fo * fi + tid, bv[0]);
+      }
+      off += (int64_t)fi * fo + fo;
+    }
+  };
+
+  for (;;) {
+    if (tid == 0) *chunk_slot = atomicAdd(work, 1);
+    __syncthreads();
+    const int c = *chunk_slot;
+    if (c >= total) break;
+    const ChunkPos cp = chunk_pos(c, coff, tstart, NT);
+    const bool new_w = cp.tile != cur_tile;
+    if (new_w && have_acc) {
+      tc::fence_after_sync();
+      flush(cur_tile);
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (new_w && tid == 0) {
+      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.total);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.total, B.wbar);
+    }
+    const bool first_of_tile = new_w;
+    cur_tile = cp.tile;
+    gather_x<F>(S, vfeat, recs, cp.row0, cp.cnt, enc, Xt, LoA, warp, lane);
+    // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
+    {
+      const float4 d = tid < cp.cnt ? dout[cp.row0 + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(tid, 0)) = make_uint2(pack_bf2(d.x, d.y), pack_bf2(d.z, 0.f));
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (new_w) {
+      bool ok = tid == 0 ? tc::mbar_wait(B.wbar, B.wphase) : true;
+      B.wphase ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+    }
+    const uint32_t w = tc::smem_addr(Wsm);
+    // forward recomputation of the hidden activations H1..HL (split operands;
+    // the lo halves alternate between LoA and LoB)
+    for (int l = 0; l < L; ++l) {
+      uint8_t* lo_in = (l & 1) ? LoB : LoA;
+      uint8_t* lo_out = (l & 1) ? LoA : LoB;
+      if (tid == 0) {
+        tc::fence_after_sync();
+        issue_split_layer(tw, tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(lo_in),
+                          w + l * H * 128, w + lay.lo_off + l * H * 128, w + lay.bias_off + 32 * l, ones8, H,
+                          l == 0 ? 4 : H / 16);
+        tc::mma_commit(B.mbar);
+      }
+      if (!wait_mma(B, tid)) { failed = true; break; }
+      epi_relu_split<H>(taddr, Ht + l * 16384, l + 1 < L ? lo_out : nullptr, tid);
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (failed) break;
+    // backward: layer L (output) down to 0.  delta of layer l's output is in
+    // DO (l = L) or D; its input activation is HL..H1 or X.
+    for (int l = L; l >= 0; --l) {
+      const uint32_t dlt = tc::smem_addr(l == L ? DOt : Dt);
+      const uint32_t act = tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384);
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const bool acc0 = !first_of_tile;
+        // weight gradient: dW_l[o][i] += sum_s delta[s][o] act[s][i]  (K = 128 samples)
+        const uint32_t idw = idesc_bf16(64, true, true);
+        for (int kk = 0; kk < 8; ++kk)
+          tc::mma_f16(tdw(l), sdesc_mn(dlt + 2048 * kk, 16384), sdesc_mn(act + 2048 * kk, 16384), idw,
+                      (acc0 || kk > 0) ? 1u : 0u);
+        // bias gradient: db_l[o] += sum_s delta[s][o]  (B = ones, K-major)
+        const uint32_t idb = idesc_bf16(16, true, false);
+        for (int kk = 0; kk < 8; ++kk)
+          tc::mma_f16(tdb(l), sdesc_mn(dlt + 2048 * kk, 16384), ones1, idb, (acc0 || kk > 0) ? 1u : 0u);
+        // data gradient w.r.t. the layer input: delta x W_l^T (N = 64 inputs)
+        const uint32_t wt = w + (uint32_t)lay.t_off + 8192u * (uint32_t)l;
+        const uint32_t idd = idesc_bf16(64, false, false);
+        const int ksteps = l == L ? 1 : H / 16;
+        for (int kk = 0; kk < ksteps; ++kk)
+          tc::mma_f16(tw, tc::sdesc_sw128(dlt + 32 * kk), tc::sdesc_sw128(wt + 32 * kk), idd, kk > 0);
+        tc::mma_commit(B.mbar);
+      }
+      if (!wait_mma(B, tid)) { failed = true; break; }
+      if (l > 0) {
+        // delta of layer l-1's output = (delta W_l) * [act > 0], BF16 into D
+#pragma unroll
+        for (int half = 0; half < H / 32; ++half) {
+          float v[32];
+          tc::tmem_ld16(taddr + 32 * half, v);
+          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const uint4 hv = *reinterpret_cast<const uint4*>(Ht + (l - 1) * 16384 + tc::sw128_offset(tid, 4 * half + q));
+            const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+            uint32_t o[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const float a0 = pos_lo(hw[j]) ? v[8 * q + 2 * j] : 0.f;
+              const float a1 = pos_hi(hw[j]) ? v[8 * q + 2 * j + 1] : 0.f;
+              o[j] = pack_bf2(a0, a1);
+            }
+            *reinterpret_cast<uint4*>(Dt + tc::sw128_offset(tid, 4 * half + q)) = make_uint4(o[0], o[1], o[2], o[3]);
+          }
+        }
+        tc::fence_proxy_async();
+      } else {
+        // feature gradient: first F inputs (the TMEM load is warp-collective,
+        // so every thread loads), scattered to the 8 corner vertices
+        float dx[F];
+#pragma unroll
+        for (int cc = 0; cc < F; cc += 16) tc::tmem_ld16(taddr + cc, dx + cc);
+        tc::tmem_wait_ld();
+        if (tid < cp.cnt) {
+          const TrainRecT t = recs[cp.row0 + tid];
+          float wk[8];
+          trilinear_weights(t.f, wk);
+          const int32_t* cn = S.corners + (size_t)t.rec * 8;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            float* g = gvfeat + (size_t)cn[k] * F;
+#pragma unroll
+            for (int q = 0; q < F; ++q) atomicAdd(g + q, wk[k] * dx[q]);
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (failed) break;
+    have_acc = true;
+  }
+  if (!failed && have_acc) {
+    tc::fence_after_sync();
+    flush(cur_tile);
+  }
+  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+}  // namespace
+
+int train_tc_image_bytes(int H, int L) { return ImageLayout(H, L).total; }
+
+// dynamic shared memory of the backward kernel (checked against the 227 KB limit)
+int train_tc_bwd_smem_bytes(int H, int L) {
+  return 1024 + 16384 * (5 + L) + ((ImageLayout(H, L).total + 1023) & ~1023) + 2048 + 64;
+}
+
+template <int F, int H, int L>
+cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool backward, cudaStream_t st) {
+  const ImageLayout lay(H, L);
+  cudaError_t e;
+  if (!backward) {
+    e = cudaMemsetAsync(a.wimg, 0, (size_t)a.img_stride * S.num_tiles, st);
+    if (e != cudaSuccess) return e;
+    pack_train_weights<<<dim3(32, S.num_tiles), 256, 0, st>>>(a.mlp, S.params_per_tile, F + 27, H, L, a.img_stride,
+                                                              a.wimg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ray_enc_kernel<<<(int)((a.n + 127) / 128 < 65536 ? (a.n + 127) / 128 : 65536), 128, 0, st>>>(a.dirs, a.n, a.enc);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    train_chunks_kernel<<<1, 32, 0, st>>>(a.tstart, S.num_tiles, a.coff);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  e = cudaMemsetAsync(a.work, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  if (!backward) {
+    const int smem = 1024 + 32768 + ((lay.fwd_bytes + 1023) & ~1023) + 1024 + 64;
+    static bool cfg = false;
+    if (!cfg) {
+      if ((e = cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess)
+        return e;
+      cfg = true;
+    }
+    // two CTAs per SM (shared memory and 2 x 64 tensor-memory columns allow it)
+    tr_mlp_fwd_tc<F, H, L><<<2 * a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
+                                                             a.work, a.enc, a.wimg, a.img_stride, a.cout);
+  } else {
+    const int smem = train_tc_bwd_smem_bytes(H, L);
+    static bool cfg = false;
+    if (!cfg) {
+      if ((e = cudaFuncSetAttribute(tr_mlp_bwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess)
+        return e;
+      cfg = true;
+    }
+    tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
+                                                         a.work, a.enc, a.wimg, a.img_stride, a.dout, a.gvfeat,
+                                                         a.gmlp);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_train_tc(const SceneDev& S, const TrainTcArgs& a, bool backward, cudaStream_t st) {
+  const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
+  if (F == 32 && H == 64 && L == 3) return launch_train_tc_t<32, 64, 3>(S, a, backward, st);
+  if (F == 16 && H == 32 && L == 2) return launch_train_tc_t<16, 32, 2>(S, a, backward, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace snisr
