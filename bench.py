@@ -35,6 +35,12 @@ WORKLOAD = ("cfg2 full-frame render 1280x720: 4x4x1 tiles of 128^3 over 3 m, ~3.
             "corner features, per-tile FP16 MLP 59-64x3-3, 207k-triangle proxy BVH, 8 seeded poses")
 MLP_FLOP_PER_SAMPLE = 2 * (59 * 64 + 64 * 64 + 64 * 64 + 64 * 3)  # 24,320
 GATHER_BYTES_PER_SAMPLE = 8 * (32 + 1) * 2                         # 528 (FP16 features + density)
+# bytes of one tile's FP16 weight image for the tensor-core MLP (H = 64, L = 3):
+# W_l [64][64] x 3, W_out [16][64], hidden-bias tile [64][64], output-bias tile [16][64]
+TC_IMAGE_BYTES = 3 * 64 * 128 + 2048 + 64 * 128 + 2048               # 36,864
+TRAIN_WORKLOAD = ("cfg3 training step (forward + backward): 1 tile of 256^3 over 4 m, ~4% occupied, FP32 32-dim "
+                  "vertex features, MLP 59-64x3-3, 65,536 rays from 8 seeded 640x480 views, MSE against a "
+                  "second scene's render (features + N(0, 0.02))")
 
 
 def _peaks():
@@ -61,7 +67,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
         return self
@@ -161,6 +167,67 @@ def cpu_baseline_run(synth, steps: int, target_s: float, threads: int):
                       f"{threads} threads, rays start at the scene entry (no proxy mesh, as the reference renderer)"}
 
 
+def train_bench(dev, steps: int, warmup: int, flush):
+    """Training forward + backward (autograd through the hand-written adjoint)
+    of the cfg3 workload, tensor-core form and plain FP32 form."""
+    import numpy as np
+    import torch
+
+    import snisr
+    from snisr.train import tile_field
+    cfg = snisr.CFG3
+    nrays, views = 65536, 8
+    synth = snisr.SynthScene(cfg, max_pixels=1024, max_samples_per_ray=48)
+    scene = snisr.Scene(synth.desc, dev.index)
+    a = synth.arrays()
+    vf = torch.from_numpy(a["vertex_feat"].astype(np.float32)).to(dev).requires_grad_(True)
+    vd = torch.from_numpy(a["vertex_density"].astype(np.float32)).to(dev).requires_grad_(True)
+    W = torch.from_numpy(a["mlp_params"].copy()).to(dev).requires_grad_(True)
+    rng = np.random.default_rng(2003)
+    os_, ds_ = [], []
+    for v in range(views):
+        cam = synth.camera(v)
+        d = snisr.camera_rays(cam, dev.index).cpu().numpy()
+        idx = np.sort(rng.choice(d.shape[0], nrays // views, replace=False))
+        ds_.append(d[idx])
+        os_.append(np.broadcast_to(np.array([cam.c2w[3], cam.c2w[7], cam.c2w[11]], np.float32), (idx.size, 3)))
+    o = torch.from_numpy(np.ascontiguousarray(np.concatenate(os_))).to(dev)
+    d = torch.from_numpy(np.ascontiguousarray(np.concatenate(ds_))).to(dev)
+    rt = torch.zeros(nrays, dtype=torch.int32, device=dev)
+    with torch.no_grad():
+        vf_t = vf + 0.02 * torch.randn(vf.shape, generator=torch.Generator(device=dev).manual_seed(7), device=dev)
+        target = tile_field(vf_t.contiguous(), vd.detach(), W.detach(), scene, o, d, rt, snisr.FORM_PLAIN_FP32)
+    stream = torch.cuda.current_stream()
+    res = {"workload": TRAIN_WORKLOAD, "unit": UNIT}
+    for name, form in (("tc", snisr.FORM_TC), ("plain_fp32", snisr.FORM_PLAIN_FP32)):
+        def step():
+            vf.grad = vd.grad = W.grad = None
+            rgb = tile_field(vf, vd, W, scene, o, d, rt, form)
+            loss = ((rgb - target) ** 2).mean()
+            loss.backward()
+            return loss
+        for _ in range(warmup):
+            step()
+        scene.check()
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            loss = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        scene.check()
+        res[name] = {"value": round(nrays * steps / (total * 1e-3) / 1e6, 3),
+                     "ms_per_step": round(total / steps, 4), "loss": float(loss)}
+    res["speedup_tc_vs_plain"] = round(res["tc"]["value"] / res["plain_fp32"]["value"], 3)
+    res["l2"] = "flushed before each step"
+    scene.close()
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -184,14 +251,16 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=24)
-    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--max-samples-per-ray", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-run", action="store_true",
-                    help="only render a few frames of both forms (small workspace; for ncu captures)")
+    ap.add_argument("--no-train", action="store_true")
+    ap.add_argument("--profile-run", choices=["render", "train"], default=None,
+                    help="render: a few frames of both forms (small workspace); train: a few training steps of "
+                         "both forms (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -206,6 +275,11 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.profile_run == "train":
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+        res = train_bench(dev, args.steps, args.warmup, flush)
+        print(json.dumps({"profile_run": "train", "train": res}))
+        return
     cfg = snisr.CFG2
     synth = snisr.SynthScene(cfg, max_samples_per_ray=args.max_samples_per_ray)
     scene = snisr.Scene(synth.desc, local)
@@ -216,7 +290,7 @@ def main():
     out = (torch.empty(n, 3, device=dev), torch.empty(n, device=dev), torch.empty(n, device=dev))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
-    if args.profile_run:
+    if args.profile_run == "render":
         for i in range(args.warmup + args.steps):
             scene.render(cams[i % len(cams)], snisr.FORM_TC, out)
         scene.render(cams[0], snisr.FORM_PLAIN_FP32, out)
@@ -251,33 +325,43 @@ def main():
     ms_tc = _max_over_ranks(ws, ms_tc)
     value = ws * n * args.steps / (ms_tc * 1e-3) / 1e6
     # plain FP32 form (the >= 2x target's denominator)
-    ms_plain = _max_over_ranks(ws, timed(snisr.FORM_PLAIN_FP32, max(4, args.steps // 3), 3))
-    plain_value = ws * n * max(4, args.steps // 3) / (ms_plain * 1e-3) / 1e6
+    plain_steps = min(24, max(4, args.steps // 3))
+    ms_plain = _max_over_ranks(ws, timed(snisr.FORM_PLAIN_FP32, plain_steps, 3))
+    plain_value = ws * n * plain_steps / (ms_plain * 1e-3) / 1e6
 
     # stages and counters of the TC form, averaged over the poses
     scene.set_profiling(True)
     stage_sum = None
-    stats_sum = {"samples": 0, "voxel_steps": 0, "chunks": 0}
-    for i in range(len(cams)):
+    stats_sum = {"samples": 0, "voxel_steps": 0, "chunks": 0, "voxels": 0, "vertices": 0}
+    prof_steps = min(args.steps, 16)
+    for i in range(prof_steps):
         flush.zero_()
-        scene.render(cams[i], snisr.FORM_TC, out)
+        scene.render(cams[i % len(cams)], snisr.FORM_TC, out)
         st = scene.stage_times()
         stage_sum = st if stage_sum is None else [a + b for a, b in zip(stage_sum, st)]
-        fs = scene.frame_stats()
+        fs = {**scene.frame_stats(), **scene.frame_footprint()}
         for k in stats_sum:
             stats_sum[k] += fs[k]
     scene.set_profiling(False)
-    npose = len(cams)
+    npose = prof_steps
     stages = dict(zip(["raygen_proxy", "traverse", "scan", "scatter", "mlp_tc", "total"],
                       [round(v / npose, 4) for v in stage_sum]))
     samples = stats_sum["samples"] / npose
     vsteps = stats_sum["voxel_steps"] / npose
     chunks = stats_sum["chunks"] / npose
+    dvox = stats_sum["voxels"] / npose
+    dvert = stats_sum["vertices"] / npose
 
     hbm, tc_peak, peak_kind = _peaks()
-    # algorithmic work per launch (per frame)
-    img = 26128  # bytes of one tile's weight image
+    # algorithmic work per launch (per frame).  MLP stage, gather model: per
+    # sample 528 B of corner features + density, the 32 B sample record, the
+    # 64 B FP16 view encoding and 12 B of colour atomics; one weight image per
+    # 128-sample chunk.
+    img = TC_IMAGE_BYTES
     mlp_bytes = samples * (GATHER_BYTES_PER_SAMPLE + 32 + 64 + 12) + chunks * img
+    # compulsory-bytes variant: every distinct trilinear corner once per frame
+    # (FP16 features + density), plus records, encodings, colours and images
+    mlp_bytes_compulsory = dvert * (32 + 1) * 2 + samples * (32 + 64 + 12) + chunks * img
     mlp_flop = samples * MLP_FLOP_PER_SAMPLE
     trav_bytes = vsteps * 8 + samples * (32 + 32) + n * (32 + 8)
     t_mlp = stages["mlp_tc"] * 1e-3
@@ -294,6 +378,14 @@ def main():
         roof = {"bound": "hbm", "achieved": trav_bytes / t_trav / 1e9, "peak": hbm, "unit": "GB/s"}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["kernel"] = dom
+    roof["launch_ms"] = round(t_mlp * 1e3 if dom == "mlp_tc" else t_trav * 1e3, 4)
+    roof["algorithmic_bytes"] = int(mlp_bytes if dom == "mlp_tc" else trav_bytes)
+    roof["algorithmic_flop"] = int(mlp_flop) if dom == "mlp_tc" else 0
+    if dom == "mlp_tc":
+        roof["compulsory"] = {"bytes": int(mlp_bytes_compulsory), "gbs": round(mlp_bytes_compulsory / t_mlp / 1e9, 1),
+                              "frac_hbm": round(mlp_bytes_compulsory / t_mlp / 1e9 / hbm, 4),
+                              "distinct_vertices": int(dvert), "distinct_voxels": int(dvox)}
+        roof["tensor_frac"] = round(mlp_flop / t_mlp / 1e12 / tc_peak, 4)
     roof["peak_source"] = f"{peak_kind} (MEASURED_PEAKS.json burst)" if peak_kind == "measured" else "fallback"
     roof["traffic"] = None
     prof = os.path.join(ROOT, "profiles", "traffic.json")
@@ -301,7 +393,12 @@ def main():
         try:
             with open(prof) as f:
                 tj = json.load(f)
-            roof["traffic"] = tj.get(dom)
+            ent = tj.get(dom)
+            if isinstance(ent, dict):
+                roof["traffic"] = ent.get("dram_bytes_per_launch")
+                roof["traffic_source"] = ent.get("source")
+            else:
+                roof["traffic"] = ent
         except Exception:
             pass
     for k in ("achieved", "frac"):
@@ -317,13 +414,18 @@ def main():
             scene.render_host(cams[i], snisr.FORM_TC, rgb_h, dep_h, op_h)
         _barrier(ws)
         t0 = time.perf_counter()
-        for i in range(args.steps):
+        e2e_steps = min(args.steps, 200)
+        for i in range(e2e_steps):
             scene.render_host(cams[i % len(cams)], snisr.FORM_TC, rgb_h, dep_h, op_h)
         t_e2e = _max_over_ranks(ws, time.perf_counter() - t0)
         _barrier(ws)
-        e2e = {"value": round(ws * n * args.steps / t_e2e / 1e6, 3), "unit": UNIT,
+        e2e = {"value": round(ws * n * e2e_steps / t_e2e / 1e6, 3), "unit": UNIT, "steps": e2e_steps,
                "h2d_bytes_per_step": 68, "d2h_bytes_per_step": n * 20,
                "path": "snisr_render_host (camera by value -> device; rgb/depth/opacity -> pinned host)"}
+
+    train = None
+    if not args.no_train:
+        train = train_bench(dev, min(40, max(4, args.steps // 2)), args.warmup, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -339,14 +441,16 @@ def main():
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "fps": round(value / (n / 1e6) / ws, 2),
             "plain_fp32": {"value": round(plain_value, 3), "unit": UNIT,
-                           "ms_per_step": round(ms_plain / max(4, args.steps // 3), 4)},
+                           "ms_per_step": round(ms_plain / plain_steps, 4), "steps": plain_steps},
             "speedup_vs_plain": round(value / plain_value, 3),
             "stages_ms": stages,
-            "frame_counters": {"samples": int(samples), "voxel_steps": int(vsteps), "mlp_chunks": int(chunks)},
+            "frame_counters": {"samples": int(samples), "voxel_steps": int(vsteps), "mlp_chunks": int(chunks),
+                               "distinct_voxels": int(dvox), "distinct_vertices": int(dvert)},
             "roofline": roof,
             "clocks": clocks,
             "gpu_launches": 5 * args.steps,
             "e2e": e2e,
+            "train": train,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

@@ -306,6 +306,10 @@ snisr_status snisr_scene_stage_times(snisr_scene* scene, float* ms, int32_t cap,
 /* Counters of the last TC-form frame (synchronises `stream`): out[0] samples,
  * out[1] voxel DDA steps, out[2] sample slots reserved, out[3] MLP chunks. */
 snisr_status snisr_scene_frame_stats(snisr_scene* scene, int64_t* out, void* stream);
+/* Footprint of the last TC-form frame (profiling aid; synchronises `stream`):
+ * out[0] distinct voxels whose samples the MLP stage read, out[1] distinct
+ * vertices behind them (their trilinear corners). */
+snisr_status snisr_scene_frame_footprint(snisr_scene* scene, int64_t* out, void* stream);
 
 /* Diagnostics of the tcgen05 operand layouts.  mode 0: one 128 x N x 64 MMA
  * (N = 32 or 64) through the descriptors of the tensor-core MLP: A [128][64],

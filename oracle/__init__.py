@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
             "oracle_volume_rendering": (None, [P, P, P, C.c_int64, C.c_int, C.c_float, P, P, P]),
             "oracle_positional_encoding": (None, [P, C.c_int64, C.c_int, P]),
             "oracle_grid_sample": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]),
+            "oracle_touched_voxels": (None, [P, P, P, P, C.c_int64, P]),
+            "oracle_train_samples": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
             "oracle_train_forward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, C.c_int, C.c_int]),
             "oracle_train_backward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int]),
         }
@@ -99,6 +101,7 @@ class OracleScene:
 
     def __init__(self, desc):
         self.desc = desc
+        self.num_voxels = int(desc.num_voxels)
         self._h = lib().oracle_scene_create(C.byref(desc))
 
     def __del__(self):
@@ -136,6 +139,22 @@ class OracleScene:
                                    nthreads or threads(), _EMUL[emulate])
         return rgb, cnt
 
+    def train_samples(self, vfeat, vdens, mlp, o, d, ray_tile):
+        """Samples of the training forward: offsets [n+1], global voxel id [S],
+        tile-local position in voxel units [S,3] (float64), delta / voxel [S]."""
+        _, cnt = self.train_forward(vfeat, vdens, mlp, o, d, ray_tile)
+        off = np.zeros(cnt.size + 1, np.int64)
+        np.cumsum(cnt, out=off[1:])
+        S = int(off[-1])
+        vox = np.zeros(S, np.int32)
+        pos = np.zeros((S, 3))
+        dv = np.zeros(S)
+        args = [np.ascontiguousarray(a, np.float32) for a in (vfeat, vdens, mlp)]
+        rt = np.ascontiguousarray(ray_tile, np.int32)
+        lib().oracle_train_samples(self._h, *map(_p, args), _p(o), _p(d), _p(rt), o.shape[0], _p(off), _p(vox),
+                                   _p(pos), _p(dv))
+        return off, vox, pos, dv
+
     def train_backward(self, vfeat, vdens, mlp, o, d, ray_tile, grad_rgb, emulate: str | None = None):
         """FP64 gradients of sum(grad_rgb * rgb): (d vfeat, d vdens, d mlp).  emulate as in train_forward."""
         n = o.shape[0]
@@ -148,6 +167,12 @@ class OracleScene:
         lib().oracle_train_backward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(g), _p(gF), _p(gG),
                                     _p(gW), _EMUL[emulate])
         return gF, gG, gW
+
+    def touched_voxels(self, o, d, t_start=None):
+        """Boolean mask [num_voxels] of the voxels holding samples of the rays (single-threaded)."""
+        t = np.zeros(self.num_voxels, np.uint8)
+        lib().oracle_touched_voxels(self._h, _p(o), _p(d), _p(t_start), o.shape[0], _p(t))
+        return t.astype(bool)
 
     def render(self, o, d, t_start, form: int, nthreads: int | None = None):
         """form: 0 plain FP32, 1 FP64, 2 tensor-core emulation (FP16 MLP inputs, FP64 math)."""

@@ -288,6 +288,7 @@ void trilinear_w(const float f[3], T w[8]) {
 struct RayStats {
   int64_t samples = 0;
   int64_t voxels = 0;
+  uint8_t* touched = nullptr;  // optional [num_voxels] marks of sampled voxels
 };
 
 // form: 0 plain FP32 semantics, 1 FP64, 2 tensor-core emulation (FP16-rounded
@@ -323,6 +324,7 @@ void render_ray(const Scene& s, const float o[3], const float d[3], float t_star
       Dp += wt * (T)g.t;
       Tr *= (T(1) - alpha);
       st.samples++;
+      if (st.touched) st.touched[rec] = 1;
       if (Tr < (T)s.early) { stop = true; return false; }
       return true;
     });
@@ -537,6 +539,19 @@ void oracle_render(const oracle_scene* os, const float* o, const float* d, const
   }
 }
 
+// Voxels holding at least one sample of the rays (plain FP32 render,
+// single-threaded): touched [num_voxels] is set to 1 for each.
+void oracle_touched_voxels(const oracle_scene* os, const float* o, const float* d, const float* t_start, int64_t n,
+                           uint8_t* touched) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  RayStats st;
+  st.touched = touched;
+  for (int64_t i = 0; i < n; ++i) {
+    float rgb[3], dep, op;
+    render_ray<float>(s, o + 3 * i, d + 3 * i, t_start ? t_start[i] : 0.0f, 0, rgb, dep, op, st);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Training: forward and adjoint of one ray segment inside one tile, FP64.
 // Replaces the autograd graph of Tile.train_batch (training/scripts/tile/
@@ -552,6 +567,8 @@ struct TrainSample {
   double s;            // density logit
   double sigma, alpha, T, dv;  // dv = delta / voxel
   double c[3];
+  int32_t rec;                       // global voxel id
+  double pos[3];                     // tile-local position in voxel units (voxel coordinate + fraction)
   std::vector<double> x;             // MLP input
   std::vector<std::vector<double>> h;  // hidden activations (post-ReLU)
 };
@@ -638,6 +655,8 @@ void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const flo
     return voxel_samples(s, vc, nr, fr, ti, q, d, [&](const SampleGeom& g) {
       TrainSample ts;
       trilinear_w<double>(g.f, ts.w);
+      ts.rec = (int32_t)rec;
+      for (int a = 0; a < 3; ++a) ts.pos[a] = (double)vc[a] + (double)g.f[a];
       const int32_t* cn = s.d->voxel_corners + (int64_t)rec * 8;
       ts.s = 0;
       for (int k = 0; k < 8; ++k) {
@@ -927,6 +946,29 @@ void oracle_train_forward(const oracle_scene* os, const float* vfeat, const floa
     train_forward_ray(s, p, ray_tile[i], o + 3 * i, d + 3 * i, S, rgb + 3 * i);
     if (counts) counts[i] = (int32_t)S.size();
   });
+}
+
+// Sample geometry of the training forward (the samples train_forward_ray
+// takes, early stop included): per sample the global voxel id, the
+// tile-local position in voxel units and delta / voxel.  offsets [n+1]:
+// prefix sums of the counts returned by oracle_train_forward.
+void oracle_train_samples(const oracle_scene* os, const float* vfeat, const float* vdens, const float* mlp,
+                          const float* o, const float* d, const int32_t* ray_tile, int64_t n, const int64_t* offsets,
+                          int32_t* vox, double* pos, double* dv) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  TrainParams p{vfeat, vdens, mlp};
+  std::vector<TrainSample> S;
+  for (int64_t i = 0; i < n; ++i) {
+    double C[3];
+    train_forward_ray(s, p, ray_tile[i], o + 3 * i, d + 3 * i, S, C);
+    const int64_t b = offsets[i];
+    if ((int64_t)S.size() != offsets[i + 1] - b) continue;  // counts from another call: leave untouched
+    for (size_t k = 0; k < S.size(); ++k) {
+      vox[b + (int64_t)k] = S[k].rec;
+      for (int a = 0; a < 3; ++a) pos[3 * (b + (int64_t)k) + a] = S[k].pos[a];
+      dv[b + (int64_t)k] = S[k].dv;
+    }
+  }
 }
 
 // Training adjoint (FP64): gradients of L = sum(grad_rgb * rgb) accumulated

@@ -54,6 +54,7 @@ struct snisr_scene {
   int last_form = -1;
   cudaEvent_t ev[8] = {};
   float* out_bufs = nullptr;          // staging for render_host
+  uint32_t* fp_bits = nullptr;        // footprint bitmaps (voxels, vertices) + 2 counters, lazily
 };
 
 namespace {
@@ -624,6 +625,28 @@ snisr_status snisr_scene_frame_stats(snisr_scene* sc, int64_t* out, void* stream
   out[1] = (int64_t)steps;
   out[2] = w[CTRL_RESERVED];
   out[3] = w[CTRL_CHUNKS];
+  return SNISR_OK;
+}
+
+snisr_status snisr_scene_frame_footprint(snisr_scene* sc, int64_t* out, void* stream) {
+  if (check_scene(sc) != SNISR_OK || !out) return set_error(SNISR_INVALID_ARG, "frame_footprint: null argument");
+  if (sc->last_form != SNISR_FORM_TC) return set_error(SNISR_INVALID_ARG, "frame_footprint: no tensor-core frame rendered");
+  DeviceGuard guard(sc->device);
+  const int64_t nvox = sc->info.num_voxels, nvert = sc->info.num_vertices;
+  const int64_t vw = (nvox + 31) / 32, tw = (nvert + 31) / 32;
+  if (!sc->fp_bits) {
+    snisr_status s = dev_alloc(sc, &sc->fp_bits, (size_t)(vw + tw + 6) * 4, "frame_footprint");
+    if (s != SNISR_OK) return s;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* counts = reinterpret_cast<unsigned long long*>(sc->fp_bits + ((vw + tw + 1) & ~int64_t(1)));
+  CUDA_TRY(launch_footprint(sc->S, sc->ws, nvox, nvert, sc->fp_bits, sc->fp_bits + vw, counts, sc->num_sms, st),
+           "frame_footprint");
+  unsigned long long h[2];
+  CUDA_TRY(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st), "frame_footprint");
+  CUDA_TRY(cudaStreamSynchronize(st), "frame_footprint");
+  out[0] = (int64_t)h[0];
+  out[1] = (int64_t)h[1];
   return SNISR_OK;
 }
 

@@ -72,6 +72,10 @@ int train_tc_bwd_smem_bytes(int H, int L);
 // enc: [n][8] uint4 (BF16 hi / lo view encoding)
 cudaError_t launch_train_tc(const SceneDev& S, const TrainTcArgs& a, bool backward, cudaStream_t st);
 
+// distinct voxels / vertices read by the last batched frame -> counts[0], counts[1]
+cudaError_t launch_footprint(const SceneDev& S, const Workspace& ws, int64_t nvox, int64_t nvert, uint32_t* vox_bits,
+                             uint32_t* vert_bits, unsigned long long* counts, int num_sms, cudaStream_t st);
+
 cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
                             cudaStream_t st);
 

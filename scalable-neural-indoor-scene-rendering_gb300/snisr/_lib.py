@@ -126,6 +126,7 @@ _SIGNATURES = {
     "snisr_scene_set_profiling": (C.c_int, [P, C.c_int32]),
     "snisr_scene_stage_times": (C.c_int, [P, P, C.c_int32, P]),
     "snisr_scene_frame_stats": (C.c_int, [P, P, P]),
+    "snisr_scene_frame_footprint": (C.c_int, [P, P, P]),
     "snisr_last_error_string": (C.c_char_p, []),
     "snisr_version": (C.c_char_p, []),
     "snisr_abi_version": (C.c_int32, []),

@@ -130,6 +130,12 @@ class Scene:
         _lib.check(_lib.lib().snisr_scene_frame_stats(self._h, out, _stream(stream)))
         return {"samples": out[0], "voxel_steps": out[1], "reserved": out[2], "chunks": out[3]}
 
+    def frame_footprint(self, stream=None):
+        """Distinct voxels / vertices read by the last tensor-core frame."""
+        out = (C.c_int64 * 2)()
+        _lib.check(_lib.lib().snisr_scene_frame_footprint(self._h, out, _stream(stream)))
+        return {"voxels": out[0], "vertices": out[1]}
+
     def render(self, cam: _lib.Camera, form: int = _lib.FORM_TC, out=None, stream=None):
         import torch
         n = cam.width * cam.height

@@ -114,6 +114,21 @@ def test_render_tc_cfg1(cfg1, pose):
     assert float(np.sqrt(((_np(rgb) - trgb) ** 2).mean())) <= 2e-4
 
 
+def test_frame_footprint_cfg1(cfg1):
+    """Distinct voxels / vertices read by a tensor-core frame (the compulsory-
+    bytes roofline counter) match the oracle's sampled voxels exactly."""
+    s, sc, osc = cfg1
+    cam = s.camera(2)
+    sc.render(cam, snisr.FORM_TC)
+    fp = sc.frame_footprint()
+    d = oracle.camera_dirs(cam)
+    o = oracle.camera_origins(cam, d.shape[0])
+    touched = osc.touched_voxels(o, d)
+    corners = s.arrays()["voxel_corners"]
+    assert fp["voxels"] == int(touched.sum()) > 0
+    assert fp["vertices"] == len(np.unique(corners[touched]))
+
+
 def _subset(cam, n, seed):
     d = oracle.camera_dirs(cam)
     idx = np.random.default_rng(seed).choice(d.shape[0], n, replace=False)
