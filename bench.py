@@ -131,6 +131,16 @@ def _max_over_ranks(ws, v: float) -> float:
     return float(t.item())
 
 
+def rank_poses(rank: int, poses: int):
+    """Pose order of one replica: every rank starts at a different pose."""
+    return [(rank * 3 + p) % poses for p in range(poses)]
+
+
+def job_value(ws: int, rays_per_step: int, steps: int, max_ms: float) -> float:
+    """Whole-job Mrays/s: every rank renders `steps` frames; time = the slowest rank."""
+    return ws * rays_per_step * steps / (max_ms * 1e-3) / 1e6
+
+
 def cpu_baseline_run(synth, steps: int, target_s: float, threads: int):
     """The reference's method as a scalar host path (the oracle port, FP32,
     no proxy start as in the reference renderer), all host threads, on a
@@ -285,7 +295,7 @@ def main():
     scene = snisr.Scene(synth.desc, local)
     W, H = cfg.width, cfg.height
     n = W * H
-    cams = [synth.camera((rank * 3 + p) % cfg.poses) for p in range(cfg.poses)]
+    cams = [synth.camera(p) for p in rank_poses(rank, cfg.poses)]
     stream = torch.cuda.current_stream()
     out = (torch.empty(n, 3, device=dev), torch.empty(n, device=dev), torch.empty(n, device=dev))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
@@ -323,11 +333,11 @@ def main():
         ms_tc = timed(snisr.FORM_TC, args.steps, args.warmup)
     clocks = clk.summary()
     ms_tc = _max_over_ranks(ws, ms_tc)
-    value = ws * n * args.steps / (ms_tc * 1e-3) / 1e6
+    value = job_value(ws, n, args.steps, ms_tc)
     # plain FP32 form (the >= 2x target's denominator)
     plain_steps = min(24, max(4, args.steps // 3))
     ms_plain = _max_over_ranks(ws, timed(snisr.FORM_PLAIN_FP32, plain_steps, 3))
-    plain_value = ws * n * plain_steps / (ms_plain * 1e-3) / 1e6
+    plain_value = job_value(ws, n, plain_steps, ms_plain)
 
     # stages and counters of the TC form, averaged over the poses
     scene.set_profiling(True)

@@ -205,7 +205,9 @@ snisr_status snisr_render_rays(snisr_scene* scene, const float* origins_dev,
  * grouped by tile (non-decreasing ids).  vfeat_dev [NV][F] FP32 features,
  * vdens_dev [NV] FP32 density logits, mlp_dev [NT][P] FP32 MLP parameters.
  * Rays normalised.  rgb_dev [n*3] out.  form PLAIN_FP32: FP32 CUDA-core MLP;
- * TC: tcgen05 BF16 MMAs with FP32 accumulation.  Sample records are kept in
+ * TC: tcgen05 MMAs with FP32 accumulation -- forward products with split
+ * BF16 operands (hi + lo, ~16 significant bits), backward products with
+ * BF16 operands.  Sample records are kept in
  * a per-scene training workspace (grown on the first call of a larger batch,
  * n * max_samples_per_ray records) for the backward call. */
 snisr_status snisr_train_forward(snisr_scene* scene, const float* vfeat_dev,

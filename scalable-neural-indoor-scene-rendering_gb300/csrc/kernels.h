@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <mutex>
 
 #include "scene_dev.h"
 
@@ -30,6 +31,24 @@ struct Workspace {
   int wimg_stride = 0;            // bytes per tile image
   int wimg_bytes = 0;             // bytes copied per tile
 };
+
+// Runs `setup` (returning cudaError_t) once per device ordinal (< 64) for
+// this flag word, e.g. kernel attribute setup; later calls on that device
+// return cudaSuccess without running it, a failed setup is retried.
+// Serialised by one process-wide mutex.
+std::mutex& setup_mutex();
+template <class Fn>
+cudaError_t once_per_device(unsigned long long* flags, Fn&& setup) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+  std::lock_guard<std::mutex> lock(setup_mutex());
+  if (bit && (*flags & bit)) return cudaSuccess;
+  e = setup();
+  if (e == cudaSuccess) *flags |= bit;
+  return e;
+}
 
 // Shape of a supported MLP instantiation.
 bool mlp_shape_supported(int F, int H, int L);

@@ -381,8 +381,10 @@ __global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap,
 // encoding, hidden activations) are written by the threads in the 128-byte
 // swizzled K-major layout; weights arrive by bulk copy (TMA) once per tile
 // change; accumulators live in tensor memory (H columns x 128 lanes).
-// Hidden layers: FP16 x FP16 -> FP32.  The last Linear (H -> 3) runs on
-// CUDA cores in FP32 from the accumulator registers.
+// Every Linear, the output one included (N = 16, 3 used), is FP16 x FP16 ->
+// FP32 on tcgen05; biases enter as one extra K = 16 step (A = 1/16
+// everywhere, B slice = 16 copies of the bias).  The epilogue applies ReLU
+// (hidden) or sigmoid + compositing weight (output).
 template <int F, int H, int L>
 __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const SampleRec* __restrict__ sorted, int* ctrl,
                                                      int NT, const uint4* __restrict__ enc,
@@ -614,32 +616,40 @@ cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, fl
 template <int F, int H, int L>
 cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num_sms, cudaStream_t st) {
   const int smem = 1024 + 16384 + ((ws.wimg_bytes + 1023) & ~1023) + 1024 + 64;
-  static int per_sm = 0;  // resident CTAs per SM, computed once per process
-  if (per_sm == 0) {
-    cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributePreferredSharedMemoryCarveout,
+  static int per_sm = 1;  // resident CTAs per SM (same GB300 on every device)
+  static unsigned long long done = 0;
+  cudaError_t e = once_per_device(&done, [&]() -> cudaError_t {
+    cudaError_t r = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (r != cudaSuccess) return r;
+    r = cudaFuncSetAttribute(mlp_tc_kernel<F, H, L>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
+    if (r != cudaSuccess) return r;
     int dev = 0, smem_sm = 0, reserved = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     cudaFuncAttributes fa{};
-    e = cudaFuncGetAttributes(&fa, mlp_tc_kernel<F, H, L>);
-    if (e != cudaSuccess) return e;
+    r = cudaFuncGetAttributes(&fa, mlp_tc_kernel<F, H, L>);
+    if (r != cudaSuccess) return r;
     const int regs_cta = ((fa.numRegs + 7) & ~7) * 128;
     int n = smem_sm / (smem + reserved);
     n = min(n, 65536 / max(regs_cta, 1));
     n = min(n, 512 / H);  // tensor-memory columns per SM
     per_sm = max(1, min(n, 8));
-  }
+    return cudaSuccess;
+  });
+  if (e != cudaSuccess) return e;
   mlp_tc_kernel<F, H, L><<<num_sms * per_sm, 128, smem, st>>>(S, ws.sorted, ws.ctrl, S.num_tiles, ws.enc, ws.wimg,
                                                              ws.wimg_stride, ws.wimg_bytes, rgb);
   return cudaGetLastError();
 }
 
 }  // namespace
+
+std::mutex& setup_mutex() {
+  static std::mutex m;
+  return m;
+}
 
 bool mlp_shape_supported(int F, int H, int L) {
   return (F == 16 && H == 32 && L == 2) || (F == 32 && H == 64 && L == 3) || (F == 16 && H == 64 && L == 3) ||

@@ -631,25 +631,21 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
   if (e != cudaSuccess) return e;
   if (!backward) {
     const int smem = 1024 + 32768 + ((lay.fwd_bytes + 1023) & ~1023) + 1024 + 64;
-    static bool cfg = false;
-    if (!cfg) {
-      if ((e = cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess)
-        return e;
-      cfg = true;
-    }
+    static unsigned long long cfg = 0;
+    e = once_per_device(&cfg, [&]() {
+      return cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    });
+    if (e != cudaSuccess) return e;
     // two CTAs per SM (shared memory and 2 x 64 tensor-memory columns allow it)
     tr_mlp_fwd_tc<F, H, L><<<2 * a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                              a.work, a.enc, a.wimg, a.img_stride, a.cout);
   } else {
     const int smem = train_tc_bwd_smem_bytes(H, L);
-    static bool cfg = false;
-    if (!cfg) {
-      if ((e = cudaFuncSetAttribute(tr_mlp_bwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess)
-        return e;
-      cfg = true;
-    }
+    static unsigned long long cfg = 0;
+    e = once_per_device(&cfg, [&]() {
+      return cudaFuncSetAttribute(tr_mlp_bwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    });
+    if (e != cudaSuccess) return e;
     tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                          a.work, a.enc, a.wimg, a.img_stride, a.dout, a.gvfeat,
                                                          a.gmlp);

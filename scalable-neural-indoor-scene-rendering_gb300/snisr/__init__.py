@@ -5,13 +5,13 @@ include/snisr.h).  This package only marshals arguments: it has no compute
 fallback of its own.
 """
 from . import _lib
-from ._lib import FORM_PLAIN_FP32, FORM_TC, F16, F32, SnisrError, lib
+from ._lib import FORM_PLAIN_FP32, FORM_TC, F16, F32, Camera, SceneDesc, SnisrError, lib
 from .configs import ALL as CONFIGS, CFG1, CFG2, CFG3, CFG4, CFG5, Config
 from .scene import Scene, SynthScene, camera_rays
 from . import ops
 
 __all__ = [
-    "FORM_PLAIN_FP32", "FORM_TC", "F16", "F32", "SnisrError", "lib", "CONFIGS", "CFG1", "CFG2", "CFG3",
+    "FORM_PLAIN_FP32", "FORM_TC", "F16", "F32", "Camera", "SceneDesc", "SnisrError", "lib", "CONFIGS", "CFG1", "CFG2", "CFG3",
     "CFG4", "CFG5", "Config", "Scene", "SynthScene", "camera_rays", "build",
 ]
 

@@ -130,6 +130,12 @@ class Scene:
         _lib.check(_lib.lib().snisr_scene_frame_stats(self._h, out, _stream(stream)))
         return {"samples": out[0], "voxel_steps": out[1], "reserved": out[2], "chunks": out[3]}
 
+    def set_mlp(self, params, stream=None):
+        """Replaces the per-tile MLP parameters ([NT, P] FP32 CUDA tensor)."""
+        if not params.is_cuda or not params.is_contiguous():
+            raise RuntimeError("params must be a contiguous CUDA tensor")
+        _lib.check(_lib.lib().snisr_scene_set_mlp(self._h, _ptr(params), _stream(stream)))
+
     def frame_footprint(self, stream=None):
         """Distinct voxels / vertices read by the last tensor-core frame."""
         out = (C.c_int64 * 2)()
