@@ -231,7 +231,7 @@ def train_bench(dev, steps: int, warmup: int, flush):
             total += e0.elapsed_time(e1)
         scene.check()
         res[name] = {"value": round(nrays * steps / (total * 1e-3) / 1e6, 3),
-                     "ms_per_step": round(total / steps, 4), "loss": float(loss)}
+                     "ms_per_step": round(total / steps, 4), "loss": float(loss.detach())}
     res["speedup_tc_vs_plain"] = round(res["tc"]["value"] / res["plain_fp32"]["value"], 3)
     res["l2"] = "flushed before each step"
     scene.close()

@@ -234,12 +234,13 @@ snisr_status cam_to_dev(const snisr_camera* c, CamDev& out) {
 }  // namespace
 
 namespace snisr {
-snisr_status scene_train_ws(snisr_scene* sc, TrainWS** out, int* num_sms, int* msr) {
+snisr_status scene_train_ws(snisr_scene* sc, TrainWS** out, int* num_sms, int* msr, int64_t* nvox) {
   if (!sc) return set_error(SNISR_INVALID_ARG, "scene is null");
   if (!sc->train) sc->train = train_ws_new();
   *out = sc->train;
   *num_sms = sc->num_sms;
   *msr = sc->max_samples_per_ray;
+  *nvox = sc->info.num_voxels;
   return SNISR_OK;
 }
 snisr_status scene_views(snisr_scene* sc, SceneDev* S, Workspace* ws, int* device) {

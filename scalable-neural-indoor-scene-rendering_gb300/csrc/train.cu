@@ -42,24 +42,41 @@ static_assert(sizeof(TrainRec) == 48, "TrainRec layout");
 constexpr int kActStride = 256;  // x (64, input padded) | h1 | h2 | h3
 constexpr int kDltStride = 196;  // delta1 | delta2 | delta3 | delta_out (3 + pad)
 
-__device__ __forceinline__ float seg_logit(const SceneDev& S, const float* __restrict__ vdens, uint32_t rec,
-                                           const float f[3], float w[8]) {
+// Per-voxel corner density logits gathered from the caller's vertex logits
+// (32 bytes per voxel), rebuilt at every forward call: the march then reads
+// one contiguous block per sample instead of 8 scattered vertex values.
+__global__ void tr_dens_cache_kernel(const int32_t* __restrict__ corners, const float* __restrict__ vdens, int64_t nvox,
+                                     float4* dc) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+    const int4* cn = reinterpret_cast<const int4*>(corners + v * 8);
+    const int4 a = __ldg(cn), b = __ldg(cn + 1);
+    dc[2 * v] = make_float4(__ldg(vdens + a.x), __ldg(vdens + a.y), __ldg(vdens + a.z), __ldg(vdens + a.w));
+    dc[2 * v + 1] = make_float4(__ldg(vdens + b.x), __ldg(vdens + b.y), __ldg(vdens + b.z), __ldg(vdens + b.w));
+  }
+}
+
+// trilinear density logit (corner order k = 0..7, the oracle's summation order)
+__device__ __forceinline__ float seg_logit(const float4* __restrict__ dc, uint32_t rec, const float f[3], float w[8]) {
   trilinear_weights(f, w);
-  const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)rec * 8);
-  int4 a = __ldg(cn), b = __ldg(cn + 1);
-  const int c[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  const float4 a = __ldg(dc + 2 * (size_t)rec), b = __ldg(dc + 2 * (size_t)rec + 1);
   float g = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) g = fmaf(w[k], __ldg(vdens + c[k]), g);
+  g = fmaf(w[0], a.x, g); g = fmaf(w[1], a.y, g); g = fmaf(w[2], a.z, g); g = fmaf(w[3], a.w, g);
+  g = fmaf(w[4], b.x, g); g = fmaf(w[5], b.y, g); g = fmaf(w[6], b.z, g); g = fmaf(w[7], b.w, g);
   return g;
 }
 
-// count (write == false) or write records of each ray segment
-__global__ void tr_march_kernel(SceneDev S, const float* __restrict__ vdens, const float* __restrict__ orig,
+constexpr int kStage = 32;  // records per ray in the single-pass staging area
+
+// March of each ray segment.  mode 0 (single pass): count every sample and
+// write the first kStage records of ray i to stage[i * kStage + c].
+// mode 1 (rays with more than kStage samples only, after the scan): march
+// again and write records c >= kStage straight to recs[off[i] + c].
+__global__ void tr_march_kernel(SceneDev S, const float4* __restrict__ dc, const float* __restrict__ orig,
                                 const float* __restrict__ dirs, const int32_t* __restrict__ ray_tile, int64_t n,
-                                int32_t* cnt, const int32_t* __restrict__ off, TrainRec* recs, int64_t cap,
-                                int write) {
+                                int32_t* cnt, const int32_t* __restrict__ off, TrainRec* stage, TrainRec* recs,
+                                int64_t cap, int mode) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (mode == 1 && cnt[i] <= kStage) continue;
     const int tile = ray_tile[i];
     int c = 0;
     if (tile >= 0 && tile < S.num_tiles) {
@@ -69,23 +86,26 @@ __global__ void tr_march_kernel(SceneDev S, const float* __restrict__ vdens, con
       if (R.init_segment(S, o, d, tile)) {
         float T = 1.0f;
         Sample s;
-        int64_t base = write ? off[i] : 0;
+        const int64_t base = mode == 1 ? off[i] : 0;
         while (next_sample(S, R, s)) {
           float w[8];
-          const float g = seg_logit(S, vdens, s.rec, s.f, w);
+          const float g = seg_logit(dc, s.rec, s.f, w);
           const float sig = softplusf(g);
           const float dv = fmul(s.interval, S.inv_voxel);
           const float alpha = 1.0f - expf(-sig * dv);
-          if (write) {
-            if (base + c < cap) {
-              TrainRec r;
-              r.rec = s.rec; r.ray = (uint32_t)i; r.tile = (uint32_t)tile; r.pad0 = 0;
-              r.f[0] = s.f[0]; r.f[1] = s.f[1]; r.f[2] = s.f[2]; r.dv = dv;
-              r.T = T; r.alpha = alpha; r.s = g; r.pad1 = 0.f;
-              recs[base + c] = r;
-            } else {
-              atomicOr(S.err, ERR_OVERFLOW);
-            }
+          TrainRec* dst = nullptr;
+          if (mode == 0) {
+            if (c < kStage) dst = stage + i * kStage + c;
+          } else if (c >= kStage) {
+            if (base + c < cap) dst = recs + base + c;
+            else atomicOr(S.err, ERR_OVERFLOW);
+          }
+          if (dst) {
+            TrainRec r;
+            r.rec = s.rec; r.ray = (uint32_t)i; r.tile = (uint32_t)tile; r.pad0 = 0;
+            r.f[0] = s.f[0]; r.f[1] = s.f[1]; r.f[2] = s.f[2]; r.dv = dv;
+            r.T = T; r.alpha = alpha; r.s = g; r.pad1 = 0.f;
+            *dst = r;
           }
           ++c;
           T *= (1.0f - alpha);
@@ -93,7 +113,27 @@ __global__ void tr_march_kernel(SceneDev S, const float* __restrict__ vdens, con
         }
       }
     }
-    if (!write) cnt[i] = c;
+    if (mode == 0) cnt[i] = c;
+  }
+}
+
+// staged records -> ray-contiguous positions off[i] + c (c < kStage)
+__global__ void tr_compact_kernel(const TrainRec* __restrict__ stage, const int32_t* __restrict__ cnt,
+                                  const int32_t* __restrict__ off, int64_t n, TrainRec* recs, int64_t cap,
+                                  uint32_t* err) {
+  const int64_t total = n * kStage;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / kStage;
+    const int c = (int)(t % kStage);
+    if (c >= __ldg(cnt + i)) continue;
+    const int64_t dst = (int64_t)__ldg(off + i) + c;
+    if (dst < cap) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(stage + t);
+      uint4* d4 = reinterpret_cast<uint4*>(recs + dst);
+      d4[0] = s4[0]; d4[1] = s4[1]; d4[2] = s4[2];
+    } else {
+      atomicOr(err, ERR_OVERFLOW);
+    }
   }
 }
 
@@ -462,6 +502,9 @@ struct TrainWS {
   int img_stride = 0;
   int32_t *cnt = nullptr, *off = nullptr, *bsum = nullptr, *total = nullptr, *tstart = nullptr;
   TrainRec* recs = nullptr;
+  TrainRec* stage = nullptr;   // [rays][kStage] single-pass march output
+  float4* dcache = nullptr;    // [nvox][2] corner density logits of the current call
+  int64_t nvox = 0;
   float4 *c = nullptr, *dout = nullptr;
   float *act = nullptr, *dlt = nullptr;
   void* block = nullptr;
@@ -471,10 +514,10 @@ struct TrainWS {
 };
 
 snisr_status scene_views(snisr_scene* scene, SceneDev* S, Workspace* ws, int* device);
-snisr_status scene_train_ws(snisr_scene* scene, TrainWS** out, int* num_sms, int* max_samples_per_ray);
+snisr_status scene_train_ws(snisr_scene* scene, TrainWS** out, int* num_sms, int* max_samples_per_ray, int64_t* nvox);
 
-snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT) {
-  if (T->block && n <= T->rays) return SNISR_OK;
+snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nvox) {
+  if (T->block && n <= T->rays && nvox == T->nvox) return SNISR_OK;
   if (T->block) cudaFree(T->block);
   T->block = nullptr;
   const int64_t rays = n, cap = n * (int64_t)msr, nb = (rays + 1023) / 1024 + 2;
@@ -482,7 +525,8 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT) {
   const int img_stride = (train_tc_image_bytes(64, 3) + 127) & ~127;
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
               al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al((NT + 2) * 4) + al(16) +
-              al(rays * 128) + al((size_t)img_stride * NT);
+              al(rays * 128) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
+              al((size_t)nvox * 32);
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, sz);
   if (e != cudaSuccess) return set_error(SNISR_OOM, std::string("train workspace: ") + cudaGetErrorString(e));
@@ -502,6 +546,9 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT) {
   T->work = (int*)take(16);
   T->enc = (uint4*)take(rays * 128);
   T->wimg = (uint8_t*)take((size_t)img_stride * NT);
+  T->stage = (TrainRec*)take((size_t)rays * kStage * sizeof(TrainRec));
+  T->dcache = (float4*)take((size_t)nvox * 32);
+  T->nvox = nvox;
   T->img_stride = img_stride;
   T->block = p;
   T->bytes = sz;
@@ -533,20 +580,26 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
                           bool march) {
   Workspace ws;
   int device = 0, msr = 0;
+  int64_t nvox = 0;
   snisr_status s = scene_views(sc, &S, &ws, &device);
   if (s != SNISR_OK) return s;
-  if ((s = scene_train_ws(sc, &T, &num_sms, &msr)) != SNISR_OK) return s;
-  if ((s = train_ws_reserve(T, n, msr, S.num_tiles)) != SNISR_OK) return s;
+  if ((s = scene_train_ws(sc, &T, &num_sms, &msr, &nvox)) != SNISR_OK) return s;
+  if ((s = train_ws_reserve(T, n, msr, S.num_tiles, nvox)) != SNISR_OK) return s;
   if (!march) return SNISR_OK;
-  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, vdens, orig, dirs, ray_tile, n, T->cnt, nullptr, nullptr, 0, 0);
-  TR_TRY(cudaGetLastError(), "train: count");
+  tr_dens_cache_kernel<<<gridn(nvox, 256), 256, 0, st>>>(S.corners, vdens, nvox, T->dcache);
+  TR_TRY(cudaGetLastError(), "train: density cache");
+  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, nullptr, T->stage,
+                                                 nullptr, 0, 0);
+  TR_TRY(cudaGetLastError(), "train: march");
   const int nb = (int)((n + 1023) / 1024);
   scan_pass1<<<nb, 1024, 0, st>>>(T->cnt, n, T->bsum);
   scan_pass2<<<1, 1024, 0, st>>>(T->bsum, nb, T->total);
   scan_pass3<<<nb, 1024, 0, st>>>(T->cnt, n, T->bsum, T->off);
   TR_TRY(cudaGetLastError(), "train: scan");
-  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, vdens, orig, dirs, ray_tile, n, T->cnt, T->off, T->recs, T->cap, 1);
-  TR_TRY(cudaGetLastError(), "train: write");
+  tr_compact_kernel<<<gridn(n * kStage, 256), 256, 0, st>>>(T->stage, T->cnt, T->off, n, T->recs, T->cap, S.err);
+  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, T->off, nullptr,
+                                                 T->recs, T->cap, 1);
+  TR_TRY(cudaGetLastError(), "train: compact");
   tile_ranges_kernel<<<1, 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->cap, T->tstart, S.err);
   TR_TRY(cudaGetLastError(), "train: tile ranges");
   return SNISR_OK;

@@ -127,3 +127,29 @@ def test_train_gradients_vs_fp64_finite_differences(setup):
     # this step size; the bulk must agree to 1e-2
     assert np.median(errs) <= 1e-3
     assert (errs <= 1e-2).mean() >= 0.9
+
+
+@pytest.mark.parametrize("form", [snisr.FORM_PLAIN_FP32, snisr.FORM_TC])
+def test_train_long_segments_match_oracle(setup, form):
+    """Low density (logit -3): segments of up to 56 samples, longer than the
+    march's single-pass staging of 32 records per ray, so the second march
+    over the long rays runs; results must not change."""
+    import torch
+    S = setup
+    T = S["T"]
+    vd_np = np.full_like(S["vd"], -3.0)
+    ref, cnt = S["osc"].train_forward(S["vf"], vd_np, S["W"], S["o"], S["d"], S["rt"], emulate=None
+                                      if form == snisr.FORM_PLAIN_FP32 else "tc")
+    assert (cnt > 32).sum() > 50
+    vf, vd, W = (T(x).requires_grad_(True) for x in (S["vf"], vd_np, S["W"]))
+    rgb = tile_field(vf, vd, W, S["sc"], T(S["o"]), T(S["d"]), T(S["rt"]), form)
+    g = np.random.default_rng(8).standard_normal((S["d"].shape[0], 3))
+    (rgb * torch.from_numpy(g).float().cuda()).sum().backward()
+    S["sc"].check()
+    assert np.abs(rgb.detach().cpu().numpy() - ref).max() <= (1e-5 if form == snisr.FORM_PLAIN_FP32 else 1e-4)
+    gF, gG, gW = S["osc"].train_backward(S["vf"], vd_np, S["W"], S["o"], S["d"], S["rt"], g,
+                                         emulate=None if form == snisr.FORM_PLAIN_FP32 else "tc")
+    tol = 1e-3 if form == snisr.FORM_PLAIN_FP32 else 2e-3
+    assert _rel(vf.grad.cpu().numpy(), gF) <= tol
+    assert _rel(vd.grad.cpu().numpy(), gG) <= tol
+    assert _rel(W.grad.cpu().numpy(), gW) <= tol
