@@ -172,8 +172,10 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
 }
 
 // Gather of the split input rows [0,128) of the chunk into Xhi / Xlo: lane
-// (g, row) interpolates 8 FP32 channels over the 8 corners; view encoding
-// copied from the per-ray split table.
+// (g, row) interpolates 8 FP32 channels over the 8 corners of each of its G
+// rows; view encoding copied from the per-ray split table.  Loads are issued
+// in stages across the lane's rows (records, then corner ids and encodings,
+// then features) so that each stage waits for memory once, not once per row.
 template <int F>
 __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restrict__ vfeat,
                                          const TrainRecT* __restrict__ recs, int row0, int cnt,
@@ -181,34 +183,68 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
   constexpr int G = F / 8, RPI = 32 / G;
   const int my_g = lane / RPI, my_row = lane % RPI;
   const uint4 z = make_uint4(0, 0, 0, 0);
+  uint4 head[G], fr[G];  // {rec, ray, tile, pad}, {f0, f1, f2, dv}
+#pragma unroll
   for (int it = 0; it < G; ++it) {
     const int r = warp * 32 + it * RPI + my_row;
     if (r < cnt) {
-      const TrainRecT t = recs[row0 + r];
+      const uint4* src = reinterpret_cast<const uint4*>(recs + row0 + r);
+      head[it] = __ldg(src);
+      fr[it] = __ldg(src + 1);
+    }
+  }
+  int4 ca[G], cb[G];
+  uint4 eh[G], el[G];
+#pragma unroll
+  for (int it = 0; it < G; ++it) {
+    const int r = warp * 32 + it * RPI + my_row;
+    if (r < cnt) {
+      const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)head[it].x * 8);
+      ca[it] = __ldg(cn);
+      cb[it] = __ldg(cn + 1);
+      if (my_g < 4) {  // G >= 4 lanes share a row: lane group g copies encoding chunk g (and g + G)
+        eh[it] = __ldg(enc + (size_t)head[it].y * 8 + my_g);
+        el[it] = __ldg(enc + (size_t)head[it].y * 8 + 4 + my_g);
+      }
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < G; ++it) {
+    const int r = warp * 32 + it * RPI + my_row;
+    if (r < cnt) {
+      const float f[3] = {__uint_as_float(fr[it].x), __uint_as_float(fr[it].y), __uint_as_float(fr[it].z)};
       float w[8];
-      trilinear_weights(t.f, w);
-      const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)t.rec * 8);
-      const int4 a = __ldg(cn), b = __ldg(cn + 1);
-      const int c[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      trilinear_weights(f, w);
+      const int c[8] = {ca[it].x, ca[it].y, ca[it].z, ca[it].w, cb[it].x, cb[it].y, cb[it].z, cb[it].w};
+      float4 v0[8], v1[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         const float4* src = reinterpret_cast<const float4*>(vfeat + (size_t)c[k] * F + 8 * my_g);
-        const float4 v0 = __ldg(src), v1 = __ldg(src + 1);
-        acc[0] = fmaf(w[k], v0.x, acc[0]); acc[1] = fmaf(w[k], v0.y, acc[1]);
-        acc[2] = fmaf(w[k], v0.z, acc[2]); acc[3] = fmaf(w[k], v0.w, acc[3]);
-        acc[4] = fmaf(w[k], v1.x, acc[4]); acc[5] = fmaf(w[k], v1.y, acc[5]);
-        acc[6] = fmaf(w[k], v1.z, acc[6]); acc[7] = fmaf(w[k], v1.w, acc[7]);
+        v0[k] = __ldg(src);
+        v1[k] = __ldg(src + 1);
+      }
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        acc[0] = fmaf(w[k], v0[k].x, acc[0]); acc[1] = fmaf(w[k], v0[k].y, acc[1]);
+        acc[2] = fmaf(w[k], v0[k].z, acc[2]); acc[3] = fmaf(w[k], v0[k].w, acc[3]);
+        acc[4] = fmaf(w[k], v1[k].x, acc[4]); acc[5] = fmaf(w[k], v1[k].y, acc[5]);
+        acc[6] = fmaf(w[k], v1[k].z, acc[6]); acc[7] = fmaf(w[k], v1[k].w, acc[7]);
       }
       uint32_t h[4], l[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) split_bf2(acc[2 * j], acc[2 * j + 1], h[j], l[j]);
       *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, my_g)) = make_uint4(h[0], h[1], h[2], h[3]);
       *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, my_g)) = make_uint4(l[0], l[1], l[2], l[3]);
-#pragma unroll
-      for (int e = my_g; e < 4; e += G) {
-        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)t.ray * 8 + e);
-        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)t.ray * 8 + 4 + e);
+      if (my_g < 4) {
+        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, G + my_g)) = eh[it];
+        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, G + my_g)) = el[it];
+      }
+      if (G < 4 && my_g + G < 4) {  // G = 2: the second half of the encoding
+        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, 2 * G + my_g)) =
+            __ldg(enc + (size_t)head[it].y * 8 + G + my_g);
+        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, 2 * G + my_g)) =
+            __ldg(enc + (size_t)head[it].y * 8 + 4 + G + my_g);
       }
 #pragma unroll
       for (int ch = G + 4 + my_g; ch < 8; ch += G) {
@@ -485,12 +521,26 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     }
     const bool first_of_tile = new_w;
     cur_tile = cp.tile;
+    // this thread's own row: output gradient, and the record and corner ids
+    // the feature-gradient scatter needs at the end of the chunk (loaded now,
+    // consumed after the MMA chain)
+    const bool mine = tid < cp.cnt;
+    float4 dmine = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint4 my_fr = make_uint4(0, 0, 0, 0);
+    int4 my_ca = make_int4(0, 0, 0, 0), my_cb = make_int4(0, 0, 0, 0);
+    if (mine) {
+      dmine = __ldg(dout + cp.row0 + tid);
+      const uint4* src = reinterpret_cast<const uint4*>(recs + cp.row0 + tid);
+      const uint32_t my_rec = __ldg(src).x;
+      my_fr = __ldg(src + 1);
+      const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8);
+      my_ca = __ldg(cn);
+      my_cb = __ldg(cn + 1);
+    }
     gather_x<F>(S, vfeat, recs, cp.row0, cp.cnt, enc, Xt, LoA, warp, lane);
     // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
-    {
-      const float4 d = tid < cp.cnt ? dout[cp.row0 + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
-      *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(tid, 0)) = make_uint2(pack_bf2(d.x, d.y), pack_bf2(d.z, 0.f));
-    }
+    *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(tid, 0)) =
+        make_uint2(pack_bf2(dmine.x, dmine.y), pack_bf2(dmine.z, 0.f));
     tc::fence_proxy_async();
     __syncthreads();
     if (new_w) {
@@ -574,11 +624,11 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
 #pragma unroll
         for (int cc = 0; cc < F; cc += 16) tc::tmem_ld16(taddr + cc, dx + cc);
         tc::tmem_wait_ld();
-        if (tid < cp.cnt) {
-          const TrainRecT t = recs[cp.row0 + tid];
+        if (mine) {
+          const float f[3] = {__uint_as_float(my_fr.x), __uint_as_float(my_fr.y), __uint_as_float(my_fr.z)};
           float wk[8];
-          trilinear_weights(t.f, wk);
-          const int32_t* cn = S.corners + (size_t)t.rec * 8;
+          trilinear_weights(f, wk);
+          const int cn[8] = {my_ca.x, my_ca.y, my_ca.z, my_ca.w, my_cb.x, my_cb.y, my_cb.z, my_cb.w};
 #pragma unroll
           for (int k = 0; k < 8; ++k) {
             float* g = gvfeat + (size_t)cn[k] * F;
