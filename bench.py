@@ -238,6 +238,113 @@ def train_bench(dev, steps: int, warmup: int, flush):
     return res
 
 
+BATCH_WORKLOAD = ("cfg4 batched multi-tile training step (forward + backward): 32 tiles of 128^3 over 3 m, FP32 "
+                  "32-dim vertex features, per-tile MLP 59-64x3-3; ray segments from 8 seeded 640x480 views split at "
+                  "tile faces (tile DDA), log-uniform [1,024, 65,536] segments per tile, grouped by tile")
+
+
+def batched_bench(dev, steps: int, warmup: int, flush):
+    """cfg4: one batched forward+backward over all tiles (tensor-core form),
+    the same as 32 per-tile calls, the plain FP32 form, and the batched step
+    replayed from a CUDA graph."""
+    import numpy as np
+    import torch
+
+    import snisr
+    from snisr import batch
+    from snisr.train import tile_field
+    cfg = snisr.CFG4
+    synth = snisr.SynthScene(cfg, max_pixels=1024, max_samples_per_ray=24)
+    scene = snisr.Scene(synth.desc, dev.index)
+    o, d, t, counts = batch.tile_batch(synth, views=8, seed=4004, device=dev.index)
+    n = int(o.shape[0])
+    a = synth.arrays()
+    vf = torch.from_numpy(a["vertex_feat"].astype(np.float32)).to(dev).requires_grad_(True)
+    vd = torch.from_numpy(a["vertex_density"].astype(np.float32)).to(dev).requires_grad_(True)
+    W = torch.from_numpy(a["mlp_params"].copy()).to(dev).requires_grad_(True)
+    with torch.no_grad():
+        vf_t = vf + 0.02 * torch.randn(vf.shape, generator=torch.Generator(device=dev).manual_seed(7), device=dev)
+        target = tile_field(vf_t.contiguous(), vd.detach(), W.detach(), scene, o, d, t, snisr.FORM_PLAIN_FP32)
+    bounds = np.concatenate([[0], np.cumsum(counts)])
+    stream = torch.cuda.current_stream()
+
+    def step_batched(form):
+        rgb = tile_field(vf, vd, W, scene, o, d, t, form)
+        loss = ((rgb - target) ** 2).sum() / n
+        loss.backward()
+
+    def step_per_tile():
+        for i in range(len(counts)):
+            if counts[i] == 0:
+                continue
+            sl = slice(int(bounds[i]), int(bounds[i + 1]))
+            rgb = tile_field(vf, vd, W, scene, o[sl], d[sl], t[sl], snisr.FORM_TC)
+            (((rgb - target[sl]) ** 2).sum() / n).backward()
+
+    def timed(fn, k):
+        for _ in range(warmup):
+            vf.grad = vd.grad = W.grad = None
+            fn()
+        scene.check()
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(k):
+            vf.grad = vd.grad = W.grad = None
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        scene.check()
+        return total / k
+
+    res = {"workload": BATCH_WORKLOAD, "unit": UNIT, "segments": n, "tiles": int((counts > 0).sum()),
+           "segments_per_tile": [int(c) for c in counts]}
+    ms = timed(lambda: step_batched(snisr.FORM_TC), steps)
+    res["tc_batched"] = {"value": round(n / ms / 1e3, 3), "ms_per_step": round(ms, 4), "launches": "one per stage"}
+    ms_pt = timed(step_per_tile, max(3, steps // 2))
+    res["tc_per_tile_calls"] = {"value": round(n / ms_pt / 1e3, 3), "ms_per_step": round(ms_pt, 4),
+                                "calls": int((counts > 0).sum())}
+    ms_pl = timed(lambda: step_batched(snisr.FORM_PLAIN_FP32), max(3, steps // 2))
+    res["plain_fp32_batched"] = {"value": round(n / ms_pl / 1e3, 3), "ms_per_step": round(ms_pl, 4)}
+    # CUDA graph of the batched tensor-core step
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            vf.grad = vd.grad = W.grad = None
+            step_batched(snisr.FORM_TC)
+    stream.wait_stream(side)
+    torch.cuda.synchronize()
+    vf.grad = vd.grad = W.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step_batched(snisr.FORM_TC)
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    scene.check()
+    ms_g = total / steps
+    res["tc_batched_graph"] = {"value": round(n / ms_g / 1e3, 3), "ms_per_step": round(ms_g, 4)}
+    res["speedup_batched_vs_per_tile"] = round(ms_pt / ms, 3)
+    res["speedup_tc_vs_plain"] = round(ms_pl / ms, 3)
+    res["l2"] = "flushed before each step"
+    del graph
+    scene.close()
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -268,7 +375,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-train", action="store_true")
-    ap.add_argument("--profile-run", choices=["render", "train"], default=None,
+    ap.add_argument("--profile-run", choices=["render", "train", "batched"], default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
     args = ap.parse_args()
@@ -285,10 +392,11 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run == "train":
+    if args.profile_run in ("train", "batched"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-        res = train_bench(dev, args.steps, args.warmup, flush)
-        print(json.dumps({"profile_run": "train", "train": res}))
+        fn = train_bench if args.profile_run == "train" else batched_bench
+        res = fn(dev, args.steps, args.warmup, flush)
+        print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
     cfg = snisr.CFG2
     synth = snisr.SynthScene(cfg, max_samples_per_ray=args.max_samples_per_ray)
@@ -433,9 +541,10 @@ def main():
                "h2d_bytes_per_step": 68, "d2h_bytes_per_step": n * 20,
                "path": "snisr_render_host (camera by value -> device; rgb/depth/opacity -> pinned host)"}
 
-    train = None
+    train = batched = None
     if not args.no_train:
         train = train_bench(dev, min(40, max(4, args.steps // 2)), args.warmup, flush)
+        batched = batched_bench(dev, min(10, max(3, args.steps // 4)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -461,6 +570,7 @@ def main():
             "gpu_launches": 5 * args.steps,
             "e2e": e2e,
             "train": train,
+            "train_batched": batched,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
