@@ -209,6 +209,7 @@ def train_bench(dev, steps: int, warmup: int, flush):
         target = tile_field(vf_t.contiguous(), vd.detach(), W.detach(), scene, o, d, rt, snisr.FORM_PLAIN_FP32)
     stream = torch.cuda.current_stream()
     res = {"workload": TRAIN_WORKLOAD, "unit": UNIT}
+    res["tuning"], _ = scene.autotune_train(vf.detach(), vd.detach(), W.detach(), o, d, rt, reps=3)
     for name, form in (("tc", snisr.FORM_TC), ("plain_fp32", snisr.FORM_PLAIN_FP32)):
         def step():
             vf.grad = vd.grad = W.grad = None
@@ -302,6 +303,7 @@ def batched_bench(dev, steps: int, warmup: int, flush):
 
     res = {"workload": BATCH_WORKLOAD, "unit": UNIT, "segments": n, "tiles": int((counts > 0).sum()),
            "segments_per_tile": [int(c) for c in counts]}
+    res["tuning"], _ = scene.autotune_train(vf.detach(), vd.detach(), W.detach(), o, d, t, reps=2)
     ms = timed(lambda: step_batched(snisr.FORM_TC), steps)
     res["tc_batched"] = {"value": round(n / ms / 1e3, 3), "ms_per_step": round(ms, 4), "launches": "one per stage"}
     ms_pt = timed(step_per_tile, max(3, steps // 2))
@@ -436,6 +438,8 @@ def main():
         scene.check()
         return sum(a.elapsed_time(b) for a, b in evs)
 
+    # launch shapes chosen by the library's autotuner on the first pose
+    tuning, tune_ms = scene.autotune_render(cams[0], reps=3)
     # headline: tensor-core batched form
     with ClockSampler(local) as clk:
         ms_tc = timed(snisr.FORM_TC, args.steps, args.warmup)
@@ -556,6 +560,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms_tc / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": "tensor-core batched (tcgen05 FP16, FP32 accumulate)",
+                       "tuning": tuning, "autotune_ms_per_frame": round(tune_ms, 4),
                        "l2": "flushed between steps (256 MB write)", "poses": cfg.poses,
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "fps": round(value / (n / 1e6) / ws, 2),

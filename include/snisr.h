@@ -299,6 +299,33 @@ snisr_status snisr_synth_camera(const snisr_synth_scene* s, uint64_t pose_seed,
                                 int32_t width, int32_t height, float fov_x_deg,
                                 snisr_camera* cam);
 
+/* ------------------------------------------------------------------------ */
+/* Launch shapes and their autotuner (no counterpart in the reference).      */
+/* ------------------------------------------------------------------------ */
+typedef struct snisr_tuning {
+  int32_t traverse_threads;      /* TC render traversal block size: 32..256, multiple of 32 */
+  int32_t scatter_blocks_per_sm; /* per-tile bucketing grid: 1..64 blocks per SM           */
+  int32_t mlp_ctas_per_sm;       /* persistent MLP CTAs per SM: 0 = resident maximum, 1..8 */
+  int32_t train_march_threads;   /* training march block size: 32..256, multiple of 32     */
+  int32_t train_fwd_ctas_per_sm; /* training TC forward CTAs per SM: 1 or 2                */
+} snisr_tuning;
+snisr_status snisr_scene_get_tuning(const snisr_scene* scene, snisr_tuning* out);
+snisr_status snisr_scene_set_tuning(snisr_scene* scene, const snisr_tuning* tuning);
+/* Times launch shapes of the TC render of `cam` (coordinate descent over the
+ * knobs; each candidate: one warm-up frame, then `reps` frames timed with
+ * CUDA events on `stream`), keeps the fastest in the scene and returns it
+ * with its ms per frame.  Allocates temporary output buffers; synchronises. */
+snisr_status snisr_scene_autotune_render(snisr_scene* scene, const snisr_camera* cam, int32_t reps,
+                                         void* stream, snisr_tuning* out, float* best_ms);
+/* Same for the TC training step (forward + backward with dL/drgb = 1) on the
+ * given batch; gradient buffers are temporary.  Results do not depend on the
+ * launch shapes beyond the summation order of atomics. */
+snisr_status snisr_scene_autotune_train(snisr_scene* scene, const float* vfeat_dev,
+                                        const float* vdens_dev, const float* mlp_dev,
+                                        const float* origins_dev, const float* dirs_dev,
+                                        const int32_t* ray_tile_dev, int64_t n, int32_t reps,
+                                        void* stream, snisr_tuning* out, float* best_ms);
+
 /* Stage timing: when enabled, render calls record CUDA events between
  * stages.  stage_times synchronises on the last frame and returns, in ms:
  * TC form [ray setup + proxy, traverse, scan, scatter, MLP, total];

@@ -651,6 +651,164 @@ snisr_status snisr_scene_frame_footprint(snisr_scene* sc, int64_t* out, void* st
   return SNISR_OK;
 }
 
+snisr_status snisr_scene_get_tuning(const snisr_scene* sc, snisr_tuning* out) {
+  if (check_scene(const_cast<snisr_scene*>(sc)) != SNISR_OK || !out)
+    return set_error(SNISR_INVALID_ARG, "get_tuning: null argument");
+  const Tuning& t = sc->ws.tune;
+  *out = snisr_tuning{t.traverse_threads, t.scatter_blocks_per_sm, t.mlp_ctas_per_sm, t.train_march_threads,
+                      t.train_fwd_ctas_per_sm};
+  return SNISR_OK;
+}
+
+snisr_status snisr_scene_set_tuning(snisr_scene* sc, const snisr_tuning* t) {
+  if (check_scene(sc) != SNISR_OK || !t) return set_error(SNISR_INVALID_ARG, "set_tuning: null argument");
+  auto warps_ok = [](int v) { return v >= 32 && v <= 256 && v % 32 == 0; };
+  if (!warps_ok(t->traverse_threads) || !warps_ok(t->train_march_threads) || t->scatter_blocks_per_sm < 1 ||
+      t->scatter_blocks_per_sm > 64 || t->mlp_ctas_per_sm < 0 || t->mlp_ctas_per_sm > 8 ||
+      (t->train_fwd_ctas_per_sm != 1 && t->train_fwd_ctas_per_sm != 2))
+    return set_error(SNISR_INVALID_ARG, "set_tuning: value out of range");
+  sc->ws.tune = Tuning{t->traverse_threads, t->scatter_blocks_per_sm, t->mlp_ctas_per_sm, t->train_march_threads,
+                       t->train_fwd_ctas_per_sm};
+  return SNISR_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// coordinate descent over the knobs: `eval` times the current sc->ws.tune
+template <class Eval>
+snisr_status tune_descent(snisr_scene* sc, const std::vector<std::pair<int Tuning::*, std::vector<int>>>& knobs,
+                          Eval&& eval, float* best_ms) {
+  float best = 0.f;
+  snisr_status s = eval(&best);
+  if (s != SNISR_OK) return s;
+  for (const auto& kv : knobs) {
+    Tuning keep = sc->ws.tune;
+    for (int v : kv.second) {
+      if (v == keep.*(kv.first)) continue;
+      sc->ws.tune = keep;
+      sc->ws.tune.*(kv.first) = v;
+      float ms = 0.f;
+      if ((s = eval(&ms)) != SNISR_OK) {
+        sc->ws.tune = keep;
+        return s;
+      }
+      if (ms < best) {
+        best = ms;
+        keep = sc->ws.tune;
+      }
+    }
+    sc->ws.tune = keep;
+  }
+  *best_ms = best;
+  return SNISR_OK;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+
+extern "C" {
+
+snisr_status snisr_scene_autotune_render(snisr_scene* sc, const snisr_camera* cam, int32_t reps, void* stream,
+                                         snisr_tuning* out, float* best_ms) {
+  if (check_scene(sc) != SNISR_OK || !cam || !out || !best_ms || reps < 1)
+    return set_error(SNISR_INVALID_ARG, "autotune_render: bad argument");
+  const int64_t n = (int64_t)cam->width * cam->height;
+  if (n <= 0 || n > sc->ws.max_rays) return set_error(SNISR_INVALID_ARG, "autotune_render: camera exceeds max_pixels");
+  DeviceGuard guard(sc->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf buf;
+  CUDA_TRY(cudaMalloc(&buf.p, (size_t)n * 5 * sizeof(float)), "autotune_render: buffers");
+  float* rgb = static_cast<float*>(buf.p);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0), "autotune_render: event");
+  CUDA_TRY(cudaEventCreate(&e1), "autotune_render: event");
+  const bool prof = sc->profiling;
+  sc->profiling = false;
+  auto eval = [&](float* ms) -> snisr_status {
+    snisr_status s = snisr_render(sc, cam, SNISR_FORM_TC, rgb, rgb + 3 * n, rgb + 4 * n, stream);
+    if (s != SNISR_OK) return s;
+    CUDA_TRY(cudaEventRecord(e0, st), "autotune_render");
+    for (int r = 0; r < reps; ++r)
+      if ((s = snisr_render(sc, cam, SNISR_FORM_TC, rgb, rgb + 3 * n, rgb + 4 * n, stream)) != SNISR_OK) return s;
+    CUDA_TRY(cudaEventRecord(e1, st), "autotune_render");
+    CUDA_TRY(cudaEventSynchronize(e1), "autotune_render");
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, e0, e1), "autotune_render");
+    *ms = t / (float)reps;
+    return snisr_scene_check(sc, stream);
+  };
+  const std::vector<std::pair<int Tuning::*, std::vector<int>>> knobs = {
+      {&Tuning::traverse_threads, {64, 128, 256}},
+      {&Tuning::scatter_blocks_per_sm, {8, 16, 32}},
+      {&Tuning::mlp_ctas_per_sm, {2, 3, 0}},
+  };
+  snisr_status s = tune_descent(sc, knobs, eval, best_ms);
+  sc->profiling = prof;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != SNISR_OK) return s;
+  return snisr_scene_get_tuning(sc, out);
+}
+
+snisr_status snisr_scene_autotune_train(snisr_scene* sc, const float* vfeat, const float* vdens, const float* mlp,
+                                        const float* origins, const float* dirs, const int32_t* ray_tile, int64_t n,
+                                        int32_t reps, void* stream, snisr_tuning* out, float* best_ms) {
+  if (check_scene(sc) != SNISR_OK || !vfeat || !vdens || !mlp || !origins || !dirs || !ray_tile || n <= 0 ||
+      reps < 1 || !out || !best_ms)
+    return set_error(SNISR_INVALID_ARG, "autotune_train: bad argument");
+  DeviceGuard guard(sc->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nv = sc->info.num_vertices, F = sc->F, NT = sc->NT, P = sc->P;
+  const size_t grads = (size_t)(nv * F + nv + NT * P), bytes = (grads + (size_t)n * 6) * sizeof(float);
+  DevBuf buf;
+  CUDA_TRY(cudaMalloc(&buf.p, bytes), "autotune_train: buffers");
+  float* gF = static_cast<float*>(buf.p);
+  float* gG = gF + nv * F;
+  float* gW = gG + nv;
+  float* rgb = gW + NT * P;
+  float* grad = rgb + 3 * n;
+  std::vector<float> ones((size_t)n * 3, 1.0f);
+  CUDA_TRY(cudaMemcpyAsync(grad, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, st),
+           "autotune_train: gradient");
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0), "autotune_train: event");
+  CUDA_TRY(cudaEventCreate(&e1), "autotune_train: event");
+  auto step = [&]() -> snisr_status {
+    snisr_status s = snisr_train_forward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, rgb, stream);
+    if (s != SNISR_OK) return s;
+    return snisr_train_backward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, rgb, grad, gF, gG,
+                                gW, stream);
+  };
+  auto eval = [&](float* ms) -> snisr_status {
+    snisr_status s = step();
+    if (s != SNISR_OK) return s;
+    CUDA_TRY(cudaEventRecord(e0, st), "autotune_train");
+    for (int r = 0; r < reps; ++r)
+      if ((s = step()) != SNISR_OK) return s;
+    CUDA_TRY(cudaEventRecord(e1, st), "autotune_train");
+    CUDA_TRY(cudaEventSynchronize(e1), "autotune_train");
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, e0, e1), "autotune_train");
+    *ms = t / (float)reps;
+    return snisr_scene_check(sc, stream);
+  };
+  const std::vector<std::pair<int Tuning::*, std::vector<int>>> knobs = {
+      {&Tuning::train_march_threads, {64, 128, 256}},
+      {&Tuning::train_fwd_ctas_per_sm, {1, 2}},
+  };
+  snisr_status s = tune_descent(sc, knobs, eval, best_ms);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != SNISR_OK) return s;
+  return snisr_scene_get_tuning(sc, out);
+}
+
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev, int32_t N, int32_t bf16,
                             int32_t mode, void* stream) {
   if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1) || mode < 0 || mode > 2 ||

@@ -15,6 +15,15 @@ struct CamDev {
   float c2w[12];
 };
 
+// Launch shapes chosen per scene (snisr_scene_set_tuning / autotune).
+struct Tuning {
+  int traverse_threads = 128;     // traverse_kernel block size (multiple of 32, <= 256)
+  int scatter_blocks_per_sm = 16; // scatter_kernel grid = SMs x this
+  int mlp_ctas_per_sm = 0;        // persistent mlp_tc_kernel CTAs per SM (0 = resident maximum)
+  int train_march_threads = 128;  // tr_march_kernel block size (multiple of 32, <= 256)
+  int train_fwd_ctas_per_sm = 2;  // tr_mlp_fwd_tc CTAs per SM (1 or 2)
+};
+
 // Per-scene workspace, sized at creation; nothing is allocated per frame.
 struct Workspace {
   float4* ray_o = nullptr;     // [max_rays] origin
@@ -30,6 +39,7 @@ struct Workspace {
   const uint8_t* wimg = nullptr;  // per-tile tensor-core weight images
   int wimg_stride = 0;            // bytes per tile image
   int wimg_bytes = 0;             // bytes copied per tile
+  Tuning tune;
 };
 
 // Runs `setup` (returning cudaError_t) once per device ordinal (< 64) for
@@ -85,6 +95,7 @@ struct TrainTcArgs {
   float* gvfeat;
   float* gmlp;
   int num_sms;
+  int fwd_ctas_per_sm;
 };
 int train_tc_image_bytes(int H, int L);
 int train_tc_bwd_smem_bytes(int H, int L);

@@ -225,10 +225,10 @@ __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const flo
 // Depth and opacity are final here: density comes from the voxel data, so
 // transmittance and early stop do not wait for the MLP.
 // ---------------------------------------------------------------------------
-constexpr int kTravThreads = 128;
+constexpr int kTravMaxThreads = 256;  // block size is a tuning knob (multiple of 32)
 constexpr uint32_t kBlk = 256;
 
-__global__ void __launch_bounds__(kTravThreads) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
+__global__ void __launch_bounds__(kTravMaxThreads) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
                                                                 const float4* __restrict__ ray_d, int64_t n,
                                                                 SampleRec* recs, uint32_t cap, uint32_t* blk_count,
                                                                 int* ctrl, float* depth, float* opac) {
@@ -615,6 +615,7 @@ cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, fl
 
 template <int F, int H, int L>
 cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num_sms, cudaStream_t st) {
+  // persistent CTAs per SM: the resident maximum, or fewer when tuned so
   const int smem = 1024 + 16384 + ((ws.wimg_bytes + 1023) & ~1023) + 1024 + 64;
   static int per_sm = 1;  // resident CTAs per SM (same GB300 on every device)
   static unsigned long long done = 0;
@@ -639,7 +640,8 @@ cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num
     return cudaSuccess;
   });
   if (e != cudaSuccess) return e;
-  mlp_tc_kernel<F, H, L><<<num_sms * per_sm, 128, smem, st>>>(S, ws.sorted, ws.ctrl, S.num_tiles, ws.enc, ws.wimg,
+  const int ctas = ws.tune.mlp_ctas_per_sm > 0 ? min(ws.tune.mlp_ctas_per_sm, per_sm) : per_sm;
+  mlp_tc_kernel<F, H, L><<<num_sms * ctas, 128, smem, st>>>(S, ws.sorted, ws.ctrl, S.num_tiles, ws.enc, ws.wimg,
                                                              ws.wimg_stride, ws.wimg_bytes, rgb);
   return cudaGetLastError();
 }
@@ -701,16 +703,17 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   e = cudaMemsetAsync(rgb, 0, sizeof(float) * 3 * n, st);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
-  const int hist_bytes = (int)sizeof(uint32_t) * S.num_tiles * (kTravThreads / 32);
-  traverse_kernel<<<grid_for(n, kTravThreads, 1 << 24), kTravThreads, hist_bytes, st>>>(S, ws.ray_o, ws.ray_d, n, ws.recs,
-                                                                                ws.cap, ws.blk_count, ws.ctrl,
-                                                                                depth, opac);
+  const int tt = ws.tune.traverse_threads;
+  const int hist_bytes = (int)sizeof(uint32_t) * S.num_tiles * (tt / 32);
+  traverse_kernel<<<grid_for(n, tt, 1 << 24), tt, hist_bytes, st>>>(S, ws.ray_o, ws.ray_d, n, ws.recs, ws.cap,
+                                                                     ws.blk_count, ws.ctrl, depth, opac);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
-  scatter_kernel<<<num_sms * 16, 256, 0, st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl, S.num_tiles, ws.sorted);
+  scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, 256, 0, st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl,
+                                                                          S.num_tiles, ws.sorted);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[3], st)) != cudaSuccess) return e;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;

@@ -577,8 +577,7 @@ namespace {
 
 snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig, const float* dirs,
                           const int32_t* ray_tile, int64_t n, SceneDev& S, TrainWS*& T, int& num_sms, cudaStream_t st,
-                          bool march) {
-  Workspace ws;
+                          bool march, Workspace& ws) {
   int device = 0, msr = 0;
   int64_t nvox = 0;
   snisr_status s = scene_views(sc, &S, &ws, &device);
@@ -588,8 +587,9 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
   if (!march) return SNISR_OK;
   tr_dens_cache_kernel<<<gridn(nvox, 256), 256, 0, st>>>(S.corners, vdens, nvox, T->dcache);
   TR_TRY(cudaGetLastError(), "train: density cache");
-  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, nullptr, T->stage,
-                                                 nullptr, 0, 0);
+  const int mt = ws.tune.train_march_threads;
+  tr_march_kernel<<<gridn(n, mt), mt, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, nullptr, T->stage,
+                                               nullptr, 0, 0);
   TR_TRY(cudaGetLastError(), "train: march");
   const int nb = (int)((n + 1023) / 1024);
   scan_pass1<<<nb, 1024, 0, st>>>(T->cnt, n, T->bsum);
@@ -597,8 +597,8 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
   scan_pass3<<<nb, 1024, 0, st>>>(T->cnt, n, T->bsum, T->off);
   TR_TRY(cudaGetLastError(), "train: scan");
   tr_compact_kernel<<<gridn(n * kStage, 256), 256, 0, st>>>(T->stage, T->cnt, T->off, n, T->recs, T->cap, S.err);
-  tr_march_kernel<<<gridn(n, 128), 128, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, T->off, nullptr,
-                                                 T->recs, T->cap, 1);
+  tr_march_kernel<<<gridn(n, mt), mt, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, T->off, nullptr,
+                                               T->recs, T->cap, 1);
   TR_TRY(cudaGetLastError(), "train: compact");
   tile_ranges_kernel<<<1, 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->cap, T->tstart, S.err);
   TR_TRY(cudaGetLastError(), "train: tile ranges");
@@ -620,13 +620,14 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   SceneDev S;
   TrainWS* T = nullptr;
   int num_sms = 0;
-  snisr_status s = train_common(sc, vdens, orig, dirs, ray_tile, n, S, T, num_sms, st, true);
+  Workspace ws;
+  snisr_status s = train_common(sc, vdens, orig, dirs, ray_tile, n, S, T, num_sms, st, true, ws);
   if (s != SNISR_OK) return s;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
   cudaError_t e;
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, nullptr, nullptr, num_sms};
+                  T->c, T->dout, nullptr, nullptr, num_sms, ws.tune.train_fwd_ctas_per_sm};
     e = launch_train_tc(S, a, false, st);
     if (e == cudaErrorInvalidValue) return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
   } else if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
@@ -658,7 +659,8 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   SceneDev S;
   TrainWS* T = nullptr;
   int num_sms = 0;
-  snisr_status s = train_common(sc, vdens, orig, dirs, ray_tile, n, S, T, num_sms, st, false);
+  Workspace ws;
+  snisr_status s = train_common(sc, vdens, orig, dirs, ray_tile, n, S, T, num_sms, st, false, ws);
   if (s != SNISR_OK) return s;
   if (T->last_n != n) return set_error(SNISR_INVALID_ARG, "train_backward: must follow train_forward on the same rays");
   tr_composite_bwd<<<gridn(n, 128), 128, 0, st>>>(S, T->recs, T->c, T->cnt, T->off, n, T->cap, grad_rgb, T->dout,
@@ -670,7 +672,7 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   if (T->last_form != form) return set_error(SNISR_INVALID_ARG, "train_backward: the forward call used another form");
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, gvfeat, gmlp, num_sms};
+                  T->c, T->dout, gvfeat, gmlp, num_sms, ws.tune.train_fwd_ctas_per_sm};
     e = launch_train_tc(S, a, true, st);
   } else if (F == 32 && H == 64 && L == 3)
     e = train_plain_mlp_bwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->dout, T->act, T->dlt, gvfeat,

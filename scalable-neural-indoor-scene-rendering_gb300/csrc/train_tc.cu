@@ -686,8 +686,9 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
       return cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     });
     if (e != cudaSuccess) return e;
-    // two CTAs per SM (shared memory and 2 x 64 tensor-memory columns allow it)
-    tr_mlp_fwd_tc<F, H, L><<<2 * a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
+    // up to two CTAs per SM (shared memory and 2 x 64 tensor-memory columns allow it)
+    const int per_sm = a.fwd_ctas_per_sm == 1 ? 1 : 2;
+    tr_mlp_fwd_tc<F, H, L><<<per_sm * a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                              a.work, a.enc, a.wimg, a.img_stride, a.cout);
   } else {
     const int smem = train_tc_bwd_smem_bytes(H, L);

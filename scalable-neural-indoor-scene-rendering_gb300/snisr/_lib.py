@@ -73,6 +73,16 @@ class Camera(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("traverse_threads", C.c_int32), ("scatter_blocks_per_sm", C.c_int32), ("mlp_ctas_per_sm", C.c_int32),
+        ("train_march_threads", C.c_int32), ("train_fwd_ctas_per_sm", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 class SynthParams(C.Structure):
     _fields_ = [
         ("kind", C.c_int32),
@@ -127,6 +137,10 @@ _SIGNATURES = {
     "snisr_scene_stage_times": (C.c_int, [P, P, C.c_int32, P]),
     "snisr_scene_frame_stats": (C.c_int, [P, P, P]),
     "snisr_scene_frame_footprint": (C.c_int, [P, P, P]),
+    "snisr_scene_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "snisr_scene_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "snisr_scene_autotune_render": (C.c_int, [P, C.POINTER(Camera), C.c_int32, P, C.POINTER(Tuning), FP]),
+    "snisr_scene_autotune_train": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, C.POINTER(Tuning), FP]),
     "snisr_last_error_string": (C.c_char_p, []),
     "snisr_version": (C.c_char_p, []),
     "snisr_abi_version": (C.c_int32, []),

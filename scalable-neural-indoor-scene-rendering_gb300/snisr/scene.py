@@ -130,6 +130,41 @@ class Scene:
         _lib.check(_lib.lib().snisr_scene_frame_stats(self._h, out, _stream(stream)))
         return {"samples": out[0], "voxel_steps": out[1], "reserved": out[2], "chunks": out[3]}
 
+    def tuning(self) -> dict:
+        """Launch shapes in use (snisr_tuning fields)."""
+        t = _lib.Tuning()
+        _lib.check(_lib.lib().snisr_scene_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Sets launch-shape knobs by name; the others keep their values."""
+        t = _lib.Tuning()
+        _lib.check(_lib.lib().snisr_scene_get_tuning(self._h, C.byref(t)))
+        for k, v in kw.items():
+            if not hasattr(t, k):
+                raise KeyError(k)
+            setattr(t, k, int(v))
+        _lib.check(_lib.lib().snisr_scene_set_tuning(self._h, C.byref(t)))
+
+    def autotune_render(self, cam: _lib.Camera, reps: int = 3, stream=None):
+        """Times launch shapes of the TC render of `cam`, keeps the fastest.
+        Returns (tuning dict, ms per frame)."""
+        t = _lib.Tuning()
+        ms = C.c_float()
+        _lib.check(_lib.lib().snisr_scene_autotune_render(self._h, C.byref(cam), int(reps), _stream(stream),
+                                                          C.byref(t), C.byref(ms)))
+        return t.as_dict(), float(ms.value)
+
+    def autotune_train(self, vfeat, vdens, mlp, origins, dirs, ray_tile, reps: int = 3, stream=None):
+        """Times launch shapes of the TC training step on this batch, keeps the
+        fastest.  Returns (tuning dict, ms per step)."""
+        t = _lib.Tuning()
+        ms = C.c_float()
+        _lib.check(_lib.lib().snisr_scene_autotune_train(
+            self._h, _ptr(vfeat), _ptr(vdens), _ptr(mlp), _ptr(origins), _ptr(dirs), _ptr(ray_tile),
+            int(origins.shape[0]), int(reps), _stream(stream), C.byref(t), C.byref(ms)))
+        return t.as_dict(), float(ms.value)
+
     def set_mlp(self, params, stream=None):
         """Replaces the per-tile MLP parameters ([NT, P] FP32 CUDA tensor)."""
         if not params.is_cuda or not params.is_contiguous():
