@@ -347,6 +347,55 @@ def batched_bench(dev, steps: int, warmup: int, flush):
     return res
 
 
+LARGE_WORKLOAD = ("cfg5 large-scene full-frame render 1920x1080, 75 deg: 8x8x2 tiles of 128^3 over 24x24x6 m "
+                  "(multi-room), ~3.4% occupied, FP16 32-dim corner features, per-tile FP16 MLP 59-64x3-3, "
+                  "~1.0M-triangle proxy BVH, 16 seeded poses")
+
+
+def large_scene_bench(dev, steps: int, warmup: int, flush):
+    """cfg5: tensor-core and plain FP32 renders of 1920x1080 frames."""
+    import torch
+
+    import snisr
+    cfg = snisr.CFG5
+    synth = snisr.SynthScene(cfg)
+    scene = snisr.Scene(synth.desc, dev.index)
+    n = cfg.width * cfg.height
+    cams = [synth.camera(p) for p in range(cfg.poses)]
+    out = (torch.empty(n, 3, device=dev), torch.empty(n, device=dev), torch.empty(n, device=dev))
+    tuning, _ = scene.autotune_render(cams[0], reps=2)
+    stream = torch.cuda.current_stream()
+
+    def timed(form, k):
+        for i in range(warmup):
+            scene.render(cams[i % len(cams)], form, out)
+        scene.check()
+        torch.cuda.synchronize()
+        total = 0.0
+        for i in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            scene.render(cams[i % len(cams)], form, out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        scene.check()
+        return total / k
+
+    ms = timed(snisr.FORM_TC, steps)
+    ms_pl = timed(snisr.FORM_PLAIN_FP32, max(2, steps // 8))
+    info = scene.info
+    res = {"workload": LARGE_WORKLOAD, "unit": UNIT, "tuning": tuning,
+           "tc": {"value": round(n / ms / 1e3, 3), "ms_per_step": round(ms, 4), "fps": round(1e3 / ms, 2)},
+           "plain_fp32": {"value": round(n / ms_pl / 1e3, 3), "ms_per_step": round(ms_pl, 4)},
+           "speedup_tc_vs_plain": round(ms_pl / ms, 3), "l2": "flushed before each frame",
+           "scene": {"voxels": int(info.num_voxels), "triangles": int(info.num_triangles),
+                     "device_gb": round(info.device_bytes / 1e9, 2)}}
+    scene.close()
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -377,7 +426,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-train", action="store_true")
-    ap.add_argument("--profile-run", choices=["render", "train", "batched"], default=None,
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large"], default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
     args = ap.parse_args()
@@ -394,9 +444,9 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run in ("train", "batched"):
+    if args.profile_run in ("train", "batched", "large"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-        fn = train_bench if args.profile_run == "train" else batched_bench
+        fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench}[args.profile_run]
         res = fn(dev, args.steps, args.warmup, flush)
         print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
@@ -545,10 +595,12 @@ def main():
                "h2d_bytes_per_step": 68, "d2h_bytes_per_step": n * 20,
                "path": "snisr_render_host (camera by value -> device; rgb/depth/opacity -> pinned host)"}
 
-    train = batched = None
+    train = batched = large = None
     if not args.no_train:
         train = train_bench(dev, min(40, max(4, args.steps // 2)), args.warmup, flush)
         batched = batched_bench(dev, min(10, max(3, args.steps // 4)), 3, flush)
+    if not args.no_large:
+        large = large_scene_bench(dev, min(32, max(4, args.steps // 4)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -576,6 +628,7 @@ def main():
             "e2e": e2e,
             "train": train,
             "train_batched": batched,
+            "large_scene": large,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
             "oracle_positional_encoding": (None, [P, C.c_int64, C.c_int, P]),
             "oracle_grid_sample": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]),
             "oracle_touched_voxels": (None, [P, P, P, P, C.c_int64, P]),
+            "oracle_start_from_hit": (None, [P, P, C.c_int64, P]),
             "oracle_train_samples": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
             "oracle_train_forward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, C.c_int, C.c_int]),
             "oracle_train_backward": (None, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int]),
@@ -167,6 +168,13 @@ class OracleScene:
         lib().oracle_train_backward(self._h, *map(_p, args), _p(o), _p(d), _p(rt), n, _p(g), _p(gF), _p(gG),
                                     _p(gW), _EMUL[emulate])
         return gF, gG, gW
+
+    def start_from_hit(self, t_hit):
+        """Start distances for proxy-hit distances (hit - 2 voxels, 0 on a miss)."""
+        t_hit = np.ascontiguousarray(t_hit, np.float32)
+        out = np.zeros_like(t_hit)
+        lib().oracle_start_from_hit(self._h, _p(t_hit), t_hit.size, _p(out))
+        return out
 
     def touched_voxels(self, o, d, t_start=None):
         """Boolean mask [num_voxels] of the voxels holding samples of the rays (single-threaded)."""

@@ -505,6 +505,12 @@ void oracle_proxy(const oracle_scene* os, const float* o, const float* d, int64_
   });
 }
 
+// Start distance from a proxy-mesh hit distance (the rule of oracle_proxy).
+void oracle_start_from_hit(const oracle_scene* os, const float* t_hit, int64_t n, float* t_start) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  for (int64_t i = 0; i < n; ++i) t_start[i] = t_hit[i] >= 0.0f ? std::max(t_hit[i] - s.start_off, 0.0f) : 0.0f;
+}
+
 // Occupied-voxel sequence per ray (no transmittance).
 void oracle_trace(const oracle_scene* os, const float* o, const float* d, const float* t_start, int64_t n, int K,
                   int32_t* visited, int32_t* count, int threads) {
