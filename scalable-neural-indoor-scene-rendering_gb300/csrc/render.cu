@@ -249,51 +249,86 @@ __global__ void __launch_bounds__(kTravMaxThreads) traverse_kernel(SceneDev S, c
   }
   const uint32_t ray_id = (uint32_t)i;
   uint32_t cur = 0, end = 0;  // warp-uniform block cursor
+  // Each round a live lane emits the samples of one voxel (up to kVoxSamples:
+  // a voxel holds at most 4 samples at 0.5-voxel steps), so that a voxel's
+  // samples are consecutive records and later share their corner loads.
+  constexpr int kVoxSamples = 4;
   for (;;) {
-    Sample s;
-    bool have = false;
-    float wt = 0.0f;
+    uint32_t vrec = 0, vtile = 0;
+    float vf[kVoxSamples][3], vw[kVoxSamples];
+    int ns = 0;
     if (live) {
-      have = next_sample(S, R, s);
-      if (!have) {
-        live = false;
-      } else {
+      Sample s;
+#pragma unroll
+      for (int j = 0; j < kVoxSamples; ++j) {
+        if (j > 0 && !(live && R.in_voxel && R.z < R.far_)) break;
+        if (!next_sample(S, R, s)) {
+          live = false;
+          break;
+        }
         float w[8];
-        float sig = sample_sigma(S, s, w);
-        float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
-        wt = T * alpha;
+        const float sig = sample_sigma(S, s, w);
+        const float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
+        const float wt = T * alpha;
         D += wt * s.t;
         T *= (1.0f - alpha);
-        if (T < S.early_stop) live = false;
+        vrec = s.rec;
+        vtile = (uint32_t)s.tile;
+        vf[j][0] = s.f[0]; vf[j][1] = s.f[1]; vf[j][2] = s.f[2];
+        vw[j] = wt;
+        ns = j + 1;
+        if (T < S.early_stop) {
+          live = false;
+          break;
+        }
       }
     }
-    unsigned m = __ballot_sync(kFull, have);
-    if (m == 0) break;
-    uint32_t cnt = __popc(m), idx = __popc(m & lanemask_lt());
-    uint32_t slot;
+    // warp prefix sum of the per-lane sample counts
+    uint32_t pre = (uint32_t)ns;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, pre, o);
+      if (lane >= o) pre += y;
+    }
+    const uint32_t cnt = __shfl_sync(kFull, pre, 31);
+    if (cnt == 0) break;
+    pre -= (uint32_t)ns;  // exclusive
+    const uint32_t base_old = cur;
+    uint32_t rem, nb = 0;
     if (cur + cnt > end) {
-      uint32_t nb = 0;
       // the open block (if any) is filled to the end by this round
       if (lane == 0 && end != 0 && (end - kBlk) / kBlk < (cap + kBlk - 1) / kBlk) blk_count[(end - kBlk) / kBlk] = kBlk;
       if (lane == 0) nb = (uint32_t)atomicAdd(ctrl + CTRL_RESERVED, (int)kBlk);
       nb = __shfl_sync(kFull, nb, 0);
-      uint32_t rem = end - cur;
-      slot = idx < rem ? cur + idx : nb + (idx - rem);
+      rem = end - cur;
       cur = nb + (cnt - rem);
       end = nb + kBlk;
     } else {
-      slot = cur + idx;
+      rem = cnt;  // everything fits in the open block
       cur += cnt;
     }
-    bool wrote = have && slot < cap;
-    if (have && !wrote) atomicOr(S.err, ERR_OVERFLOW);
-    unsigned m2 = __ballot_sync(kFull, wrote);
-    if (wrote) {
-      uint4* dst = reinterpret_cast<uint4*>(recs + slot);
-      dst[0] = make_uint4(s.rec, ray_id, __float_as_uint(wt), (uint32_t)s.tile);
-      dst[1] = make_uint4(__float_as_uint(s.f[0]), __float_as_uint(s.f[1]), __float_as_uint(s.f[2]), 0u);
-      unsigned g = __match_any_sync(m2, s.tile);
-      if (lane == __ffs(g) - 1) atomicAdd(hist + s.tile, (uint32_t)__popc(g));
+    bool dropped = false;
+#pragma unroll
+    for (int j = 0; j < kVoxSamples; ++j) {
+      if (j < ns) {
+        const uint32_t k = pre + (uint32_t)j;
+        const uint32_t slot = k < rem ? base_old + k : nb + (k - rem);
+        if (slot < cap) {
+          uint4* dst = reinterpret_cast<uint4*>(recs + slot);
+          dst[0] = make_uint4(vrec, ray_id, __float_as_uint(vw[j]), vtile);
+          dst[1] = make_uint4(__float_as_uint(vf[j][0]), __float_as_uint(vf[j][1]), __float_as_uint(vf[j][2]), 0u);
+        } else {
+          dropped = true;
+        }
+      }
+    }
+    if (dropped) atomicOr(S.err, ERR_OVERFLOW);
+    // tile histogram: one add per group of lanes that emitted samples of the same tile
+    const unsigned mh = __ballot_sync(kFull, ns > 0);
+    if (ns > 0) {
+      const unsigned g = __match_any_sync(mh, vtile);
+      const unsigned tot = __reduce_add_sync(g, (unsigned)ns);
+      if (lane == __ffs(g) - 1) atomicAdd(hist + vtile, tot);
     }
   }
   if (lane == 0 && end != 0 && (end - kBlk) / kBlk < (cap + kBlk - 1) / kBlk)
