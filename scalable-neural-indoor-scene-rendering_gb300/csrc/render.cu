@@ -466,25 +466,55 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   uint32_t wphase = 0, mphase = 0;
   bool failed = false;
 
-  for (;;) {
-    if (tid == 0) *chunk_slot = atomicAdd(ctrl + CTRL_WORK, 1);
-    __syncthreads();
-    const int c = *chunk_slot;
-    if (c >= total_chunks) break;
+  // Chunks are claimed one ahead: while chunk c runs its MMA chain, thread 0
+  // has already claimed the next chunk (slots alternate by iteration parity)
+  // and every thread loads its own row's record of that chunk (32 rows per
+  // warp: thread tid holds row tid), so the next gather starts from registers.
+  struct ChunkRows {
+    int c, tile, row0, cnt;
+  };
+  auto locate = [&](int c) {
+    ChunkRows r{c, 0, 0, 0};
+    if (c >= total_chunks) return r;
     int lo = 0, hi = NT;  // largest t with coff[t] <= c
     while (hi - lo > 1) {
       int mid = (lo + hi) >> 1;
       if (__ldg(coff + mid) <= c) lo = mid; else hi = mid;
     }
-    const int tile = lo;
-    const int row0 = __ldg(off + tile) + (c - __ldg(coff + tile)) * 128;
-    const int cnt = min(128, __ldg(off + tile + 1) - row0);
+    r.tile = lo;
+    r.row0 = __ldg(off + lo) + (c - __ldg(coff + lo)) * 128;
+    r.cnt = min(128, __ldg(off + lo + 1) - r.row0);
+    return r;
+  };
+  auto load_row = [&](const ChunkRows& r, uint4& ra, uint4& rb) {
+    ra = make_uint4(kInvalid, 0, 0, 0);
+    rb = make_uint4(0, 0, 0, 0);
+    if (r.c < total_chunks && tid < r.cnt) {
+      const uint4* src = reinterpret_cast<const uint4*>(sorted + r.row0 + tid);
+      ra = __ldg(src);
+      rb = __ldg(src + 1);
+    }
+  };
+  if (tid == 0) chunk_slot[0] = atomicAdd(ctrl + CTRL_WORK, 1);
+  __syncthreads();
+  ChunkRows cr = locate(chunk_slot[0]);
+  uint4 my_ra, my_rb;
+  load_row(cr, my_ra, my_rb);
+  for (int iter = 0;; ++iter) {
+    if (cr.c >= total_chunks) break;
+    int* next_slot = chunk_slot + ((iter + 1) & 1);
+    if (tid == 0) *next_slot = atomicAdd(ctrl + CTRL_WORK, 1);  // read after the gather's barrier
+    const int tile = cr.tile, row0 = cr.row0, cnt = cr.cnt;
+    (void)row0;
     const bool new_w = tile != cur_tile;
     if (new_w && tid == 0) {
       tc::mbar_arrive_expect_tx(wbar, (uint32_t)img_bytes);
       tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)tile * img_stride, (uint32_t)img_bytes, wbar);
     }
     cur_tile = tile;
+    // this thread's output row (ray id, compositing weight)
+    const uint32_t my_ray = my_ra.y;
+    const float my_wt = __uint_as_float(my_ra.z);
 
     // gather: per warp iteration RPI = 32/G rows; lane (g = lane / RPI,
     // row = lane % RPI) owns channel group g of one row.  The FP16 cache is
@@ -494,6 +524,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     // over the 8 corners in FP32 and writes one 16-byte chunk of the
     // swizzled A row (8 consecutive rows per 8-lane phase: conflict-free).
     // A row holds chunks [0,G) features, [G,G+4) view encoding, the rest 0.
+    // Row records come from the lane holding the row (lane = row - warp*32).
     {
       constexpr int RPI = 32 / G;
       const int my_g = lane / RPI, my_row = lane % RPI;
@@ -504,18 +535,12 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         uint4 cv[2][8];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const int rbase = warp * 32 + (it + u) * RPI;
-          uint4 ra = make_uint4(kInvalid, 0, 0, 0), rb = make_uint4(0, 0, 0, 0);
-          if (lane < RPI && rbase + lane < cnt) {
-            const uint4* src = reinterpret_cast<const uint4*>(sorted + row0 + rbase + lane);
-            ra = src[0];
-            rb = src[1];
-          }
-          rec[u] = __shfl_sync(kFull, ra.x, my_row);
-          ray[u] = __shfl_sync(kFull, ra.y, my_row);
-          fx[u] = __uint_as_float(__shfl_sync(kFull, rb.x, my_row));
-          fy[u] = __uint_as_float(__shfl_sync(kFull, rb.y, my_row));
-          fz[u] = __uint_as_float(__shfl_sync(kFull, rb.z, my_row));
+          const int src_lane = (it + u) * RPI + my_row;
+          rec[u] = __shfl_sync(kFull, my_ra.x, src_lane);
+          ray[u] = __shfl_sync(kFull, my_ra.y, src_lane);
+          fx[u] = __uint_as_float(__shfl_sync(kFull, my_rb.x, src_lane));
+          fy[u] = __uint_as_float(__shfl_sync(kFull, my_rb.y, src_lane));
+          fz[u] = __uint_as_float(__shfl_sync(kFull, my_rb.z, src_lane));
           if (rec[u] != kInvalid) {
             const uint4* fp = S.feat16 + (size_t)rec[u] * 8 * G + my_g;
 #pragma unroll
@@ -561,6 +586,9 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     }
     tc::fence_proxy_async();
     __syncthreads();
+    const ChunkRows nx = locate(*next_slot);
+    uint4 nra, nrb;
+    load_row(nx, nra, nrb);
     if (new_w) {
       // one thread polls the barrier; the others wait at bar.sync, which
       // keeps the shared-memory pipe free for the gathers of other CTAs
@@ -622,11 +650,12 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     }
     if (failed) break;
     if (tid < cnt) {
-      const uint4 ra = *reinterpret_cast<const uint4*>(sorted + row0 + tid);
-      const float wt = __uint_as_float(ra.z);
 #pragma unroll
-      for (int c3 = 0; c3 < 3; ++c3) atomicAdd(rgb + 3 * (size_t)ra.y + c3, wt * sigmoidf_(out3[c3]));
+      for (int c3 = 0; c3 < 3; ++c3) atomicAdd(rgb + 3 * (size_t)my_ray + c3, my_wt * sigmoidf_(out3[c3]));
     }
+    cr = nx;
+    my_ra = nra;
+    my_rb = nrb;
   }
   if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
   tc::fence_before_sync();
