@@ -369,45 +369,67 @@ __global__ void scan_kernel(int* ctrl, int NT) {
   ctrl[CTRL_SAMPLES] = o;
 }
 
-// Stage 3: move samples into per-tile order (warp-aggregated cursors).
-// Slot s is valid iff s % 256 < blk_count[s / 256] (per-warp blocks are
-// filled in order; only each warp's last block is partial).
-__global__ void scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap, const uint32_t* __restrict__ blk_count,
-                               int* ctrl, int NT, SampleRec* sorted) {
-  const int lane = threadIdx.x & 31;
+// Stage 3: move samples into per-tile order.  A CTA takes a slab of
+// kScatU * 256 consecutive record slots, ranks its records per tile with
+// warp-aggregated shared-memory counters, reserves one range per tile with a
+// single global atomic, and writes.  Slot s is valid iff s % 256 <
+// blk_count[s / 256] (per-warp blocks are filled in order; only each warp's
+// last block is partial).  Consecutive records of one tile keep their order
+// within a warp (samples of one voxel stay adjacent).
+constexpr int kScatThreads = 256, kScatU = 4;
+__global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap,
+                                                               const uint32_t* __restrict__ blk_count, int* ctrl,
+                                                               int NT, SampleRec* sorted) {
+  extern __shared__ uint32_t sh_scat[];  // count[NT], base[NT]
+  uint32_t* scount = sh_scat;
+  uint32_t* sbase = sh_scat + NT;
+  const int tid = threadIdx.x, lane = tid & 31;
   const uint32_t total = min((uint32_t)ctrl[CTRL_RESERVED], cap);
   const int* off = ctrl + CTRL_HEADER + NT;
   int* cursor = ctrl + CTRL_HEADER + NT + (NT + 1) + (NT + 1);
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  constexpr int U = 2;  // records per lane in flight
-  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * U; base < total; base += warps * 32 * U) {
-    uint4 a[U], b[U];
-    bool valid[U];
+  constexpr uint32_t kSlab = kScatU * kScatThreads;
+  for (uint32_t slab = blockIdx.x * kSlab; slab < total; slab += gridDim.x * kSlab) {
+    for (int t = tid; t < NT; t += kScatThreads) scount[t] = 0;
+    __syncthreads();
+    uint4 a[kScatU], b[kScatU];
+    uint32_t rank[kScatU];
+    bool valid[kScatU];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const uint32_t s = base + u * 32 + lane;
-      valid[u] = s < total && (s % kBlk) < __ldg(blk_count + s / kBlk);
+    for (int u = 0; u < kScatU; ++u) {
+      const uint32_t sidx = slab + u * kScatThreads + tid;
+      valid[u] = sidx < total && (sidx % kBlk) < __ldg(blk_count + sidx / kBlk);
       if (valid[u]) {
-        const uint4* src = reinterpret_cast<const uint4*>(recs + s);
-        a[u] = src[0];
-        b[u] = src[1];
+        const uint4* src = reinterpret_cast<const uint4*>(recs + sidx);
+        a[u] = __ldg(src);
+        b[u] = __ldg(src + 1);
       }
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      unsigned m = __ballot_sync(kFull, valid[u]);
+    for (int u = 0; u < kScatU; ++u) {
+      const unsigned m = __ballot_sync(kFull, valid[u]);
       if (valid[u]) {
-        unsigned g = __match_any_sync(m, a[u].w);
-        int leader = __ffs(g) - 1;
-        int pos = 0;
-        if (lane == leader) pos = atomicAdd(cursor + a[u].w, __popc(g));
-        pos = __shfl_sync(g, pos, leader);
-        pos += __popc(g & lanemask_lt());
-        uint4* dst = reinterpret_cast<uint4*>(sorted + off[a[u].w] + pos);
+        const unsigned g = __match_any_sync(m, a[u].w);
+        const int leader = __ffs(g) - 1;
+        uint32_t r0 = 0;
+        if (lane == leader) r0 = atomicAdd(scount + a[u].w, (uint32_t)__popc(g));
+        r0 = __shfl_sync(g, r0, leader);
+        rank[u] = r0 + __popc(g & lanemask_lt());
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < NT; t += kScatThreads)
+      if (scount[t]) sbase[t] = (uint32_t)atomicAdd(cursor + t, (int)scount[t]);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kScatU; ++u) {
+      if (valid[u]) {
+        const uint32_t t = a[u].w;
+        uint4* dst = reinterpret_cast<uint4*>(sorted + off[t] + sbase[t] + rank[u]);
         dst[0] = a[u];
         dst[1] = b[u];
       }
     }
+    __syncthreads();  // counts are reset for the next slab
   }
 }
 
@@ -776,8 +798,8 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
-  scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, 256, 0, st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl,
-                                                                          S.num_tiles, ws.sorted);
+  scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, kScatThreads, 2 * S.num_tiles * (int)sizeof(uint32_t),
+                   st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl, S.num_tiles, ws.sorted);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[3], st)) != cudaSuccess) return e;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
