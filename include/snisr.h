@@ -269,6 +269,44 @@ snisr_status snisr_op_integrate_points(const float* rgba_dev, const float* z_dis
                                        int64_t npix, float early_stop, float* frame_dev,
                                        float* transparency_dev, void* stream);
 
+/* Specular pass (the reference's reflection MLP and its batching).        */
+/* FASTRENDERING.sort_by_key (rendering/src/reorder.cu:10-22): stable sort of
+ * (keys int16, values int32) by key in place, then unique_by_key over
+ * (keys, starts): keys[k] = k-th distinct key, starts[k] = starts[first
+ * position of its run] (positions past the run count keep the sorted keys and
+ * the old starts).  *num_unique = number of distinct keys (host).  Uses
+ * stream-ordered temporaries and synchronises `stream`. */
+snisr_status snisr_op_sort_by_key(int16_t* keys_dev, int32_t* values_dev, int32_t* starts_dev,
+                                  int64_t n, int64_t* num_unique, void* stream);
+/* FASTRENDERING.assign_pixels (rendering/src/reorder.cu:24-94): network k's
+ * pixels [pixel_starts[k], pixel_starts[k+1]) over blocks [block_starts[k],
+ * block_starts[k+1]); the first (count mod blocks) blocks take one pixel more. */
+snisr_status snisr_op_assign_pixels(const int16_t* net_dev, const int32_t* pixel_starts_dev,
+                                    const int32_t* block_starts_dev, int64_t num_net,
+                                    int16_t* new_net_dev, int32_t* new_pixel_starts_dev, void* stream);
+/* Parameters per network of the reflection MLP (22556 FP16 values). */
+int32_t snisr_op_inference_mlp_param_count(void);
+/* FASTRENDERING.inference_mlp (rendering/src/rayreflection_render.cu:111-301):
+ * block b evaluates network net[b] (int16, -1 = none; ids >= num_groups are
+ * skipped) on the samples of pixels [pixel_starts[b], pixel_starts[b+1]) of
+ * the sorted pixel list (query_pixel_indices maps them to frame pixels);
+ * pixels with transparency < trans_stop are skipped and their results left
+ * untouched.  MLP 63 -> 64 x 5 (LeakyReLU 0.01) -> 28 on the position
+ * encoding of (sample - group centre) * inverse_far; colour = sigmoid(SH
+ * degree 2 of the normalised ray direction), density = max(out[27], 0).
+ * params: [num_groups][22556] FP16 bit patterns in the reference layout
+ * (per layer bias[out] then W[in][out]); samples [npix][spr][3],
+ * rays_d [npix][3], sample_results [npix][spr][4].  Runs on tcgen05 with
+ * FP16 operands and FP32 accumulation (the reference accumulates in FP16).
+ * err_dev (optional): the value 2 is OR-ed in if a bounded device wait ran out. */
+snisr_status snisr_op_inference_mlp(int32_t samples_per_ray, int32_t num_block, float inverse_far,
+                                    float trans_stop, const int16_t* net_dev, int32_t num_groups,
+                                    const float* transparency_dev, const int32_t* query_pixel_indices_dev,
+                                    const int32_t* pixel_starts_dev, const float* group_centers_dev,
+                                    const float* samples_dev, const float* rays_d_dev,
+                                    const uint16_t* params_dev, float* sample_results_dev,
+                                    uint32_t* err_dev, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Seeded synthetic scenes (input generation for tests and benchmarks).      */
 /* ------------------------------------------------------------------------ */

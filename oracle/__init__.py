@@ -62,6 +62,11 @@ def lib() -> C.CDLL:
                                                C.c_int, C.c_int, P, P]),
             "oracle_op_inverse_z": (None, [P, P, P, P, C.c_int64, C.c_int, C.c_int, P, P]),
             "oracle_op_integrate": (None, [P, P, C.c_int64, C.c_float, P, P]),
+            "oracle_op_sort_by_key": (C.c_int64, [P, P, P, C.c_int64]),
+            "oracle_eval_sh2": (None, [P, P, C.c_int64, P]),
+            "oracle_op_assign_pixels": (None, [P, P, P, C.c_int64, P, P]),
+            "oracle_op_inference_mlp": (None, [C.c_int, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P, P, P, P,
+                                               C.c_int, C.c_int]),
             "oracle_ray_aabb": (None, [P, P, P, C.c_float, P]),
             "oracle_voxel_traversal": (C.c_int, [P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float]),
             "oracle_ray_triangle_onesided": (C.c_float, [P, P, P, P, P]),
@@ -269,4 +274,33 @@ def grid_sample(vol, idx):
     C_, D, H, W = vol.shape
     out = np.zeros((idx.shape[0], C_))
     lib().oracle_grid_sample(_p(vol), C_, D, H, W, _p(idx), idx.shape[0], _p(out))
+    return out
+
+
+def op_sort_by_key(keys, values, starts):
+    """In place, as FASTRENDERING.sort_by_key; returns the number of distinct keys."""
+    assert keys.dtype == np.int16 and values.dtype == np.int32 and starts.dtype == np.int32
+    return int(lib().oracle_op_sort_by_key(_p(keys), _p(values), _p(starts), keys.size))
+
+
+def op_assign_pixels(net, pixel_starts, block_starts, new_net, new_pixel_starts):
+    lib().oracle_op_assign_pixels(_p(net), _p(pixel_starts), _p(block_starts), net.size, _p(new_net),
+                                  _p(new_pixel_starts))
+
+
+def op_inference_mlp(spr, num_block, inverse_far, trans_stop, net, transparency, qpix, pstarts, centers, samples,
+                     rays_d, params_f16, results, mode: int, nthreads: int | None = None):
+    """FASTRENDERING.inference_mlp; mode 0: the reference's FP16 arithmetic, 1: FP64 with FP16 operands.
+    params_f16: uint16 bit patterns [G][22556]; results [npix][spr][4] float32, written in place."""
+    args = [np.ascontiguousarray(a) for a in (net, transparency, qpix, pstarts, centers, samples, rays_d, params_f16)]
+    lib().oracle_op_inference_mlp(int(spr), int(num_block), float(inverse_far), float(trans_stop),
+                                  *map(_p, args), _p(results), int(mode), nthreads or threads())
+
+
+def eval_sh2(coeff_basis_major, dirs):
+    """SH degree 2 (FP64): coeff [n][27] (3 * basis + channel), unit dirs [n][3] -> [n][3]."""
+    c = np.ascontiguousarray(coeff_basis_major, np.float64)
+    d = np.ascontiguousarray(dirs, np.float64)
+    out = np.zeros((d.shape[0], 3))
+    lib().oracle_eval_sh2(_p(c), _p(d), d.shape[0], _p(out))
     return out

@@ -1134,4 +1134,185 @@ void oracle_trilinear_base(const float* voxels, int Mx, int My, int Mz, const fl
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Specular pass ops (rendering/src/reorder.cu, rendering/src/rayreflection_render.cu)
+// ---------------------------------------------------------------------------
+// FASTRENDERING.sort_by_key (reorder.cu:10-22): stable sort of (keys,
+// values) by key, then unique_by_key over (keys, starts): keys[k] = the k-th
+// distinct key, starts[k] = starts[first position of its run].  Returns the
+// number of runs.
+int64_t oracle_op_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, int64_t n) {
+  std::vector<int64_t> idx((size_t)n);
+  for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return keys[a] < keys[b]; });
+  std::vector<int16_t> k2((size_t)n);
+  std::vector<int32_t> v2((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    k2[(size_t)i] = keys[idx[(size_t)i]];
+    v2[(size_t)i] = values[idx[(size_t)i]];
+  }
+  int64_t k = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    keys[i] = k2[(size_t)i];
+    values[i] = v2[(size_t)i];
+  }
+  for (int64_t i = 0; i < n; ++i)
+    if (i == 0 || keys[i] != keys[i - 1]) {
+      keys[k] = keys[i];
+      starts[k] = starts[i];
+      ++k;
+    }
+  return k;
+}
+
+// FASTRENDERING.assign_pixels (reorder.cu:24-94): per network k, blocks
+// [block_starts[k], block_starts[k+1]) share its pixels, the first
+// (count mod blocks) blocks taking one pixel more.
+void oracle_op_assign_pixels(const int16_t* net, const int32_t* pixel_starts, const int32_t* block_starts,
+                             int64_t num_net, int16_t* new_net, int32_t* new_pixel_starts) {
+  for (int64_t k = 0; k < num_net; ++k) {
+    int32_t ps = pixel_starts[k];
+    const int32_t num = pixel_starts[k + 1] - pixel_starts[k];
+    const int32_t nb = block_starts[k + 1] - block_starts[k];
+    if (nb <= 0) continue;
+    const int32_t base = num / nb, add = num - base * nb;
+    for (int32_t i = 0; i < nb; ++i) {
+      new_net[block_starts[k] + i] = net[k];
+      new_pixel_starts[block_starts[k] + i] = ps;
+      ps += i < add ? base + 1 : base;
+    }
+  }
+}
+
+}  // extern "C"
+namespace {
+constexpr int kSpecIn = 63, kSpecH = 64, kSpecHidden = 5, kSpecOut = 28, kSpecParams = 22556;
+inline float h16(float v) { return round_f16(v); }
+inline float hfma(float a, float b, float c) { return round_f16((float)((double)a * (double)b + (double)c)); }
+inline float hmul(float a, float b) { return round_f16((float)((double)a * (double)b)); }
+inline float hadd(float a, float b) { return round_f16((float)((double)a + (double)b)); }
+inline float hsub(float a, float b) { return round_f16((float)((double)a - (double)b)); }
+const double kSH[] = {0.28209479177387814, 0.4886025119029199, 1.0925484305920792, -1.0925484305920792,
+                      0.31539156525252005, -1.0925484305920792, 0.5462742152960396};
+
+// SH degree 2 in FP64, coefficients c[3 * basis + channel] (the device
+// layout of rayreflection_render.cu:61-108; formula of training/scripts/sh.py
+// eval_sh), unit direction (X, Y, Z).
+void sh2_eval(const double* c, double X, double Y, double Z, double out[3]) {
+  for (int i = 0; i < 3; ++i) {
+    double v = kSH[0] * c[i] - kSH[1] * Y * c[3 + i] + kSH[1] * Z * c[6 + i] - kSH[1] * X * c[9 + i];
+    v += kSH[2] * X * Y * c[12 + i] + kSH[3] * Y * Z * c[15 + i] + kSH[4] * (2 * Z * Z - X * X - Y * Y) * c[18 + i] +
+         kSH[5] * X * Z * c[21 + i] + kSH[6] * (X * X - Y * Y) * c[24 + i];
+    out[i] = v;
+  }
+}
+
+// One specular sample (rayreflection_render.cu:176-287).  mode 0: the
+// reference's FP16 arithmetic (each HFMA and SH operation rounded to FP16;
+// the reference's fast __sinf/__cosf are replaced by the exact sine/cosine
+// rounded to float, a difference FP16 rounding absorbs almost always).
+// mode 1: FP64 accumulation with FP16-rounded inputs, weights and hidden
+// activations (the tensor-core form's semantics); SH and sigmoid in FP64.
+void spec_sample(const float pt[3], const float c[3], float inv_far, const float dir[3], const uint16_t* W, int mode,
+                 float out[4]) {
+  float p[3];
+  for (int a = 0; a < 3; ++a) p[a] = (pt[a] - c[a]) * inv_far;
+  double x[kSpecH] = {0};
+  for (int a = 0; a < 3; ++a) x[a] = h16(p[a]);
+  for (int i = 0; i < 10; ++i) {
+    const float f = (float)(1 << i);
+    for (int a = 0; a < 3; ++a) {
+      const float arg = f * p[a];
+      x[3 + 6 * i + a] = h16((float)std::sin((double)arg));
+      x[6 + 6 * i + a] = h16((float)std::cos((double)arg));
+    }
+  }
+  auto w = [&](size_t k) { return (double)f16_to_f32(W[k]); };
+  size_t off = 0;
+  double cur[kSpecH], nx[kSpecH];
+  for (int i = 0; i < kSpecH; ++i) cur[i] = x[i];
+  int fin = kSpecIn;
+  for (int l = 0; l <= kSpecHidden; ++l) {
+    const int fo = l == kSpecHidden ? kSpecOut : kSpecH;
+    for (int j = 0; j < fo; ++j) {
+      double acc = w(off + (size_t)j);
+      if (mode == 0) {
+        float a = (float)acc;
+        for (int i = 0; i < fin; ++i) a = hfma((float)cur[i], (float)w(off + fo + (size_t)i * fo + j), a);
+        acc = a;
+      } else {
+        for (int i = 0; i < fin; ++i) acc += cur[i] * w(off + fo + (size_t)i * fo + j);
+      }
+      if (l < kSpecHidden) {
+        if (mode == 0) acc = acc < 0.0 ? hmul((float)acc, h16(0.01f)) : acc;
+        else acc = h16((float)(acc < 0.0 ? acc * 0.01 : acc));
+      }
+      nx[j] = acc;
+    }
+    off += (size_t)fo + (size_t)fin * fo;
+    for (int j = 0; j < fo; ++j) cur[j] = nx[j];
+    fin = kSpecH;
+  }
+  out[3] = (float)std::max(cur[kSpecOut - 1], 0.0);
+  // SH degree 2 (PlenOctree convention, coefficient layout [basis][rgb])
+  if (mode == 0) {
+    const float inv = 1.0f / std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    const float X = h16(dir[0] * inv), Y = h16(dir[1] * inv), Z = h16(dir[2] * inv);
+    float col[3];
+    for (int i = 0; i < 3; ++i) col[i] = hmul(h16((float)kSH[0]), (float)cur[i]);
+    const float C1 = h16((float)kSH[1]);
+    for (int i = 0; i < 3; ++i) {
+      const float t1 = hmul(hmul(C1, Y), (float)cur[3 + i]);
+      const float t2 = hmul(hmul(C1, Z), (float)cur[6 + i]);
+      const float t3 = hmul(hmul(C1, X), (float)cur[9 + i]);
+      col[i] = hsub(hadd(hsub(col[i], t1), t2), t3);
+    }
+    const float xx = hmul(X, X), yy = hmul(Y, Y), zz = hmul(Z, Z), xy = hmul(X, Y), yz = hmul(Y, Z), xz = hmul(X, Z);
+    const float t = hsub(hsub(hmul(h16(2.0f), zz), xx), yy), t2 = hsub(xx, yy);
+    for (int i = 0; i < 3; ++i) {
+      col[i] = hadd(col[i], hmul(hmul(h16((float)kSH[2]), xy), (float)cur[12 + i]));
+      col[i] = hadd(col[i], hmul(hmul(h16((float)kSH[3]), yz), (float)cur[15 + i]));
+      col[i] = hadd(col[i], hmul(hmul(h16((float)kSH[4]), t), (float)cur[18 + i]));
+      col[i] = hadd(col[i], hmul(hmul(h16((float)kSH[5]), xz), (float)cur[21 + i]));
+      col[i] = hadd(col[i], hmul(hmul(h16((float)kSH[6]), t2), (float)cur[24 + i]));
+    }
+    for (int i = 0; i < 3; ++i) out[i] = 1.0f / (1.0f + std::exp(-col[i]));
+  } else {
+    const double nrm = std::sqrt((double)dir[0] * dir[0] + (double)dir[1] * dir[1] + (double)dir[2] * dir[2]);
+    double v[3];
+    sh2_eval(cur, dir[0] / nrm, dir[1] / nrm, dir[2] / nrm, v);
+    for (int i = 0; i < 3; ++i) out[i] = (float)(1.0 / (1.0 + std::exp(-v[i])));
+  }
+}
+}  // namespace
+extern "C" {
+
+// SH degree 2 (FP64) of n unit directions; coeff [n][27] basis-major.
+void oracle_eval_sh2(const double* coeff, const double* dirs, int64_t n, double* out) {
+  for (int64_t i = 0; i < n; ++i) sh2_eval(coeff + 27 * i, dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], out + 3 * i);
+}
+
+// FASTRENDERING.inference_mlp (rayreflection_render.cu:111-301): block b
+// evaluates network net[b] on the samples of pixels [pstarts[b],
+// pstarts[b+1]) of the sorted pixel list (query_pixel_indices maps them to
+// frame pixels); pixels whose transparency is below trans_stop are skipped
+// (their results are not written).  params: [G][22556] FP16 bit patterns.
+// mode as in spec_sample.
+void oracle_op_inference_mlp(int spr, int64_t num_block, float inverse_far, float trans_stop, const int16_t* net,
+                             const float* transparency, const int32_t* qpix, const int32_t* pstarts,
+                             const float* centers, const float* samples, const float* rays_d, const uint16_t* params,
+                             float* results, int mode, int threads) {
+  parallel_for(num_block, threads, [&](int64_t b) {
+    const int g = net[b];
+    if (g == -1) return;
+    for (int64_t task = (int64_t)pstarts[b] * spr; task < (int64_t)pstarts[b + 1] * spr; ++task) {
+      const int64_t pix = qpix[task / spr];
+      if (transparency[pix] < trans_stop) continue;
+      const int64_t ori = pix * spr + task % spr;
+      spec_sample(samples + 3 * ori, centers + 3 * (int64_t)g, inverse_far, rays_d + 3 * pix,
+                  params + (size_t)g * kSpecParams, mode, results + 4 * ori);
+    }
+  });
+}
 }  // extern "C"

@@ -106,6 +106,18 @@ cudaError_t launch_train_tc(const SceneDev& S, const TrainTcArgs& a, bool backwa
 cudaError_t launch_footprint(const SceneDev& S, const Workspace& ws, int64_t nvox, int64_t nvert, uint32_t* vox_bits,
                              uint32_t* vert_bits, unsigned long long* counts, int num_sms, cudaStream_t st);
 
+// specular pass ops (specular.cu)
+cudaError_t launch_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, int64_t n, int64_t* count_host,
+                               cudaStream_t st);
+cudaError_t launch_assign_pixels(const int16_t* net, const int32_t* pixel_starts, const int32_t* block_starts,
+                                 int64_t num_net, int16_t* new_net, int32_t* new_pixel_starts, cudaStream_t st);
+int inference_mlp_param_count();
+cudaError_t launch_inference_mlp(int spr, int num_block, float inv_far, float trans_stop, const int16_t* net,
+                                 int num_groups, const float* transparency, const int32_t* qpix,
+                                 const int32_t* pstarts, const float* centers, const float* samples,
+                                 const float* rays_d, const uint16_t* params, float* results, int* work,
+                                 uint32_t* err, int num_sms, cudaStream_t st);
+
 cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
                             cudaStream_t st);
 

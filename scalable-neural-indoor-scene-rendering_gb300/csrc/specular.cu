@@ -1,0 +1,544 @@
+// The reference's specular pass ops, rebuilt for sm_103a:
+//   sort_by_key / assign_pixels (rendering/src/reorder.cu:10-94): batching of
+//     the reflection pixels by network;
+//   inference_mlp (rendering/src/rayreflection_render.cu:111-301): the
+//     per-group MLP 63 -> 64 x 5 (LeakyReLU 0.01) -> 28 on position encodings,
+//     SH degree 2 of the view direction, sigmoid, density = max(out[27], 0).
+// The reference evaluates the MLP with scalar FP16 FMA chains (FP16
+// accumulation); here it runs on tcgen05 (FP16 operands, FP32 accumulation
+// in tensor memory), which is closer to exact arithmetic.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "kernels.h"
+#include "snisr.h"
+#include "snisr_internal.h"
+#include "tc_ptx.cuh"
+
+namespace snisr {
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ unsigned lanemask_lt_() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of (int16 key, int32 value), 2 passes of 8 bits on
+// the key with its sign bit flipped (signed order).  Block = 256 threads x 4
+// rounds = 1024 consecutive elements.
+// ---------------------------------------------------------------------------
+constexpr int kSortThreads = 256, kSortPer = 4, kSortBlock = kSortThreads * kSortPer;
+
+__device__ __forceinline__ uint32_t digit_of(int16_t k, int pass) {
+  return ((uint32_t)(uint16_t)(k ^ (int16_t)0x8000) >> (8 * pass)) & 0xFFu;
+}
+
+__global__ void sort_hist_kernel(const int16_t* __restrict__ keys, int64_t n, int pass, uint32_t* hist, int nblocks) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortBlock;
+  for (int r = 0; r < kSortPer; ++r) {
+    const int64_t i = base + r * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(h + digit_of(keys[i], pass), 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];  // digit-major
+}
+
+// exclusive scan of m values in place (one block of 1024 threads)
+__global__ void scan_u32_kernel(uint32_t* v, int64_t m) {
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (m + 1023) / 1024;
+  const int64_t b = t * per, e = min(m, b + per);
+  uint32_t s = 0;
+  for (int64_t i = b; i < e; ++i) s += v[i];
+  part[t] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele over the 1024 partial sums
+    const uint32_t y = t >= o ? part[t - o] : 0u;
+    __syncthreads();
+    part[t] += y;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - s;
+  for (int64_t i = b; i < e; ++i) {
+    const uint32_t x = v[i];
+    v[i] = run;
+    run += x;
+  }
+}
+
+__global__ void sort_scatter_kernel(const int16_t* __restrict__ kin, const int32_t* __restrict__ vin, int64_t n,
+                                    int pass, const uint32_t* __restrict__ offs, int nblocks, int16_t* kout,
+                                    int32_t* vout) {
+  __shared__ uint32_t wcnt[kSortThreads / 32][256];
+  __shared__ uint32_t run[256];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  run[tid] = 0;
+  const int64_t base = (int64_t)blockIdx.x * kSortBlock;
+  for (int r = 0; r < kSortPer; ++r) {
+    for (int w = 0; w < kSortThreads / 32; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+    const int64_t i = base + r * kSortThreads + tid;
+    const bool valid = i < n;
+    int16_t k = 0;
+    int32_t v = 0;
+    uint32_t d = 0, rank = 0;
+    if (valid) {
+      k = kin[i];
+      v = vin[i];
+      d = digit_of(k, pass);
+    }
+    const unsigned m = __ballot_sync(kFull, valid);
+    if (valid) {
+      const unsigned g = __match_any_sync(m, d);
+      rank = __popc(g & lanemask_lt_());
+      if (rank == 0) wcnt[warp][d] = __popc(g);
+    }
+    __syncthreads();
+    // per digit: prefix over the warps of this round (thread tid owns digit tid)
+    {
+      uint32_t acc = run[tid];
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        const uint32_t c = wcnt[w][tid];
+        wcnt[w][tid] = acc;
+        acc += c;
+      }
+      run[tid] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = offs[(size_t)d * nblocks + blockIdx.x] + wcnt[warp][d] + rank;
+      kout[pos] = k;
+      vout[pos] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// unique_by_key: flag[i] = first element of a run of equal keys
+__global__ void run_flags_kernel(const int16_t* __restrict__ k, int64_t n, uint32_t* flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    flag[i] = (i == 0 || k[i] != k[i - 1]) ? 1u : 0u;
+}
+
+__global__ void run_compact_kernel(const int16_t* __restrict__ ksorted, const int32_t* __restrict__ starts_in,
+                                   const uint32_t* __restrict__ pos, int64_t n, int16_t* keys, int32_t* starts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    keys[i] = ksorted[i];  // positions past the run count keep the sorted keys
+    if (i == 0 || ksorted[i] != ksorted[i - 1]) starts[pos[i]] = starts_in[i];
+  }
+}
+
+__global__ void run_keys_kernel(const int16_t* __restrict__ ksorted, const uint32_t* __restrict__ pos, int64_t n,
+                                int16_t* keys, int64_t* count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i == 0 || ksorted[i] != ksorted[i - 1]) keys[pos[i]] = ksorted[i];
+    if (i == n - 1) *count = (int64_t)pos[i] + ((i == 0 || ksorted[i] != ksorted[i - 1]) ? 1 : 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// assign_pixels: network k's pixels over blocks [bs[k], bs[k+1]), the first
+// (count mod blocks) blocks taking one pixel more.
+// ---------------------------------------------------------------------------
+__global__ void assign_pixels_kernel(const int16_t* __restrict__ net, const int32_t* __restrict__ ps,
+                                     const int32_t* __restrict__ bs, int64_t num_net, int16_t* new_net,
+                                     int32_t* new_ps) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < num_net; k += (int64_t)gridDim.x * blockDim.x) {
+    int32_t p = ps[k];
+    const int32_t num = ps[k + 1] - ps[k], nb = bs[k + 1] - bs[k];
+    if (nb <= 0) continue;
+    const int32_t base = num / nb, add = num - base * nb;
+    for (int32_t i = 0; i < nb; ++i) {
+      new_net[bs[k] + i] = net[k];
+      new_ps[bs[k] + i] = p;
+      p += i < add ? base + 1 : base;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// inference_mlp on tcgen05
+// ---------------------------------------------------------------------------
+constexpr int kSpIn = 63, kSpH = 64, kSpHidden = 5, kSpOut = 28, kSpParams = 22556;
+constexpr uint32_t kErrTimeout = 2u;
+
+// reference parameter offsets: per layer bias[fo] then W[fi][fo]
+__host__ __device__ constexpr int sp_layer_off(int l) {
+  return l == 0 ? 0 : (kSpH + kSpIn * kSpH) + (l - 1) * (kSpH + kSpH * kSpH);
+}
+
+__device__ __forceinline__ uint32_t swz(int row, int k) {  // byte offset of element (row, k) in a K-major SW128 tile
+  return (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u + ((uint32_t)((k >> 3) ^ (row & 7)) << 4) +
+         (uint32_t)((k & 7) << 1);
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+// shared memory: A (16 KB) | W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) |
+// bias tiles B0, B1 (2 x 8 KB) | 1/16 atom (1 KB) | barriers, slots
+constexpr int kSpA = 0, kSpW = 16384, kSpWout = kSpW + 5 * 8192, kSpB0 = kSpWout + 4096, kSpB1 = kSpB0 + 8192,
+              kSpOnes = kSpB1 + 8192, kSpBars = kSpOnes + 1024, kSpSmem = kSpBars + 64;
+
+// pack network g's parameters (reference layout, FP16) into the swizzled tiles
+__device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
+  // hidden layers: row = output j, K = input i
+  for (int e = tid; e < kSpHidden * kSpH * (kSpH / 8); e += 128) {
+    const int l = e / (kSpH * 8), j = (e / 8) % kSpH, c = e % 8;
+    const int fi = l == 0 ? kSpIn : kSpH, off = sp_layer_off(l) + kSpH;
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i0 = 8 * c + 2 * q, i1 = i0 + 1;
+      const float a = i0 < fi ? __half2float(P[off + i0 * kSpH + j]) : 0.f;
+      const float b = i1 < fi ? __half2float(P[off + i1 * kSpH + j]) : 0.f;
+      w[q] = pack_h2(a, b);
+    }
+    *reinterpret_cast<uint4*>(sm + kSpW + l * 8192 + swz(j, 8 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  // output layer: 32 rows (28 used)
+  for (int e = tid; e < 32 * 8; e += 128) {
+    const int j = e / 8, c = e % 8, off = sp_layer_off(kSpHidden) + kSpOut;
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i0 = 8 * c + 2 * q;
+      const float a = j < kSpOut ? __half2float(P[off + i0 * kSpOut + j]) : 0.f;
+      const float b = j < kSpOut ? __half2float(P[off + (i0 + 1) * kSpOut + j]) : 0.f;
+      w[q] = pack_h2(a, b);
+    }
+    *reinterpret_cast<uint4*>(sm + kSpWout + swz(j, 8 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  // bias tiles: B0 K-slices 0..3 = layers 0..3; B1 slice 0 = layer 4, slice 1 = output (rows < 28)
+  for (int e = tid; e < 2 * kSpH * 8; e += 128) {
+    const int t = e / (kSpH * 8), j = (e / 8) % kSpH, c = e % 8;
+    const int slice = c / 2;  // 16 K columns = 2 chunks of 8
+    int layer = -1;
+    if (t == 0) layer = slice;
+    else if (slice == 0) layer = kSpHidden - 1;
+    else if (slice == 1) layer = kSpHidden;
+    float b = 0.f;
+    if (layer >= 0 && layer < kSpHidden) b = __half2float(P[sp_layer_off(layer) + j]);
+    else if (layer == kSpHidden && j < kSpOut) b = __half2float(P[sp_layer_off(kSpHidden) + j]);
+    const uint32_t h = pack_h2(b, b);
+    *reinterpret_cast<uint4*>(sm + (t == 0 ? kSpB0 : kSpB1) + swz(j, 8 * c)) = make_uint4(h, h, h, h);
+  }
+}
+
+__global__ void __launch_bounds__(128, 2)
+    inference_mlp_kernel(int spr, int num_block, float inv_far, float trans_stop, const int16_t* __restrict__ net,
+                         int num_groups, const float* __restrict__ transparency, const int32_t* __restrict__ qpix,
+                         const int32_t* __restrict__ pstarts, const float* __restrict__ centers,
+                         const float* __restrict__ samples, const float* __restrict__ rays_d,
+                         const __half* __restrict__ params, float4* results, int* work, uint32_t* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSpBars);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 1);
+  int* blk_slot = reinterpret_cast<int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t mbar = tc::smem_addr(bars);
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 64);
+    tc::tmem_relinquish();
+  }
+  for (int k = tid; k < 64; k += 128)  // 1/16 in FP16: bias step D += (1/16) * 16 copies of b = b
+    reinterpret_cast<uint4*>(sm + kSpOnes)[k] = make_uint4(0x2C002C00u, 0x2C002C00u, 0x2C002C00u, 0x2C002C00u);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint64_t ones = tc::sdesc_sw128_sbo(tc::smem_addr(sm + kSpOnes), 0);
+  const uint32_t a_base = tc::smem_addr(sm + kSpA);
+  const uint32_t id_h = tc::idesc_f16(kSpH, 0), id_o = tc::idesc_f16(32, 0);
+  uint32_t mphase = 0;
+  int cur_net = -1;
+  bool failed = false;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous slot value
+    if (tid == 0) *blk_slot = atomicAdd(work, 1);
+    __syncthreads();
+    const int b = *blk_slot;
+    if (b >= num_block) break;
+    const int g = net[b];
+    if (g < 0 || g >= num_groups) continue;  // -1: no network (the reference returns); bad ids are skipped
+    if (g != cur_net) {
+      pack_net(params + (size_t)g * kSpParams, sm, tid);
+      tc::fence_proxy_async();
+      __syncthreads();
+      cur_net = g;
+    }
+    const float cx = centers[3 * g], cy = centers[3 * g + 1], cz = centers[3 * g + 2];
+    const int64_t t0 = (int64_t)pstarts[b] * spr, t1 = (int64_t)pstarts[b + 1] * spr;
+    for (int64_t c0 = t0; c0 < t1; c0 += 128) {
+      // A row of this thread: position encoding of its task (zeros when skipped)
+      const int64_t t = c0 + tid;
+      bool live = t < t1;
+      int64_t pix = 0, ori = 0;
+      if (live) {
+        pix = qpix[t / spr];
+        live = transparency[pix] >= trans_stop;
+        ori = pix * spr + t % spr;
+      }
+      {
+        uint32_t h[32];
+        if (live) {
+          const float p[3] = {(samples[3 * ori] - cx) * inv_far, (samples[3 * ori + 1] - cy) * inv_far,
+                              (samples[3 * ori + 2] - cz) * inv_far};
+          float x[64];
+          x[0] = p[0]; x[1] = p[1]; x[2] = p[2];
+#pragma unroll
+          for (int i = 0; i < 10; ++i) {
+            const float f = (float)(1 << i);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              x[3 + 6 * i + a] = __sinf(f * p[a]);
+              x[6 + 6 * i + a] = __cosf(f * p[a]);
+            }
+          }
+          x[63] = 0.f;
+#pragma unroll
+          for (int q = 0; q < 32; ++q) h[q] = pack_h2(x[2 * q], x[2 * q + 1]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) h[q] = 0u;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, c)) =
+              make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+      }
+      tc::fence_proxy_async();
+      __syncthreads();
+      float out[32];
+      for (int l = 0; l <= kSpHidden; ++l) {
+        if (tid == 0) {
+          tc::fence_after_sync();
+          const bool last = l == kSpHidden;
+          const uint32_t wb = tc::smem_addr(sm + (last ? kSpWout : kSpW + l * 8192));
+          const uint32_t id = last ? id_o : id_h;
+          for (int kk = 0; kk < 4; ++kk)
+            tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+          const uint32_t bt = tc::smem_addr(sm + (l < 4 ? kSpB0 + 32 * l : kSpB1 + 32 * (l - 4)));
+          tc::mma_f16(tmem, ones, tc::sdesc_sw128(bt), id, 1);
+          tc::mma_commit(mbar);
+        }
+        const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
+        mphase ^= 1u;
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        tc::fence_after_sync();
+        if (l < kSpHidden) {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            float v[32];
+            tc::tmem_ld16(taddr + 32 * half, v);
+            tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              uint32_t o[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                float a0 = v[8 * q + 2 * j], a1 = v[8 * q + 2 * j + 1];
+                a0 = a0 < 0.f ? 0.01f * a0 : a0;
+                a1 = a1 < 0.f ? 0.01f * a1 : a1;
+                o[j] = pack_h2(a0, a1);
+              }
+              *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, 4 * half + q)) =
+                  make_uint4(o[0], o[1], o[2], o[3]);
+            }
+          }
+          tc::fence_proxy_async();
+        } else {
+          tc::tmem_ld16(taddr, out);
+          tc::tmem_ld16(taddr + 16, out + 16);
+          tc::tmem_wait_ld();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+      }
+      if (failed) break;
+      if (live) {
+        const float dx = rays_d[3 * pix], dy = rays_d[3 * pix + 1], dz = rays_d[3 * pix + 2];
+        const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+        const float X = dx * inv, Y = dy * inv, Z = dz * inv;
+        const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f;
+        const float C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+                             0.5462742152960396f};
+        const float xx = X * X, yy = Y * Y, zz = Z * Z;
+        float rgb[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          float v = C0 * out[i] - C1 * Y * out[3 + i] + C1 * Z * out[6 + i] - C1 * X * out[9 + i];
+          v += C2[0] * X * Y * out[12 + i] + C2[1] * Y * Z * out[15 + i] + C2[2] * (2.f * zz - xx - yy) * out[18 + i] +
+               C2[3] * X * Z * out[21 + i] + C2[4] * (xx - yy) * out[24 + i];
+          rgb[i] = 1.0f / (1.0f + expf(-v));
+        }
+        results[ori] = make_float4(rgb[0], rgb[1], rgb[2], fmaxf(out[kSpOut - 1], 0.f));
+      }
+    }
+    if (failed) break;
+  }
+  if (failed && tid == 0 && err) atomicOr(err, kErrTimeout);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+}  // namespace
+
+cudaError_t launch_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, int64_t n, int64_t* count_host,
+                               cudaStream_t st) {
+  if (n <= 0) {
+    *count_host = 0;
+    return cudaSuccess;
+  }
+  const int nblocks = (int)((n + kSortBlock - 1) / kSortBlock);
+  const size_t hist_n = (size_t)256 * nblocks;
+  // temporaries: keys x2, values, starts copy, flags/positions, histogram, count
+  const size_t bytes = (size_t)n * 2 * 2 + (size_t)n * 4 * 3 + hist_n * 4 + 64;
+  void* tmp = nullptr;
+  cudaError_t e = cudaMallocAsync(&tmp, bytes, st);
+  if (e != cudaSuccess) return e;
+  uint8_t* q = static_cast<uint8_t*>(tmp);
+  int16_t* k1 = reinterpret_cast<int16_t*>(q);
+  int16_t* k2 = k1 + n;
+  int32_t* v1 = reinterpret_cast<int32_t*>(q + (((size_t)n * 4 + 15) & ~size_t(15)));
+  int32_t* s_copy = v1 + n;
+  uint32_t* pos = reinterpret_cast<uint32_t*>(s_copy + n);
+  uint32_t* hist = pos + n;
+  int64_t* cnt = reinterpret_cast<int64_t*>((reinterpret_cast<uintptr_t>(hist + hist_n) + 7) & ~uintptr_t(7));
+  const int64_t gb = (n + 255) / 256;
+  const int g = (int)(gb < 65535 ? gb : 65535);
+  do {
+    if ((e = cudaMemcpyAsync(s_copy, starts, (size_t)n * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) break;
+    // pass 0: keys/values -> k1/v1; pass 1: k1/v1 -> k2/values
+    sort_hist_kernel<<<nblocks, kSortThreads, 0, st>>>(keys, n, 0, hist, nblocks);
+    scan_u32_kernel<<<1, 1024, 0, st>>>(hist, (int64_t)hist_n);
+    sort_scatter_kernel<<<nblocks, kSortThreads, 0, st>>>(keys, values, n, 0, hist, nblocks, k1, v1);
+    sort_hist_kernel<<<nblocks, kSortThreads, 0, st>>>(k1, n, 1, hist, nblocks);
+    scan_u32_kernel<<<1, 1024, 0, st>>>(hist, (int64_t)hist_n);
+    sort_scatter_kernel<<<nblocks, kSortThreads, 0, st>>>(k1, v1, n, 1, hist, nblocks, k2, values);
+    run_flags_kernel<<<g, 256, 0, st>>>(k2, n, pos);
+    scan_u32_kernel<<<1, 1024, 0, st>>>(pos, n);
+    run_compact_kernel<<<g, 256, 0, st>>>(k2, s_copy, pos, n, keys, starts);
+    run_keys_kernel<<<g, 256, 0, st>>>(k2, pos, n, keys, cnt);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(count_host, cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+  } while (false);
+  cudaError_t e2 = cudaFreeAsync(tmp, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e != cudaSuccess ? e : e2;
+}
+
+cudaError_t launch_assign_pixels(const int16_t* net, const int32_t* pixel_starts, const int32_t* block_starts,
+                                 int64_t num_net, int16_t* new_net, int32_t* new_pixel_starts, cudaStream_t st) {
+  if (num_net <= 0) return cudaSuccess;
+  const int64_t gb = (num_net + 127) / 128;
+  assign_pixels_kernel<<<(int)(gb < 65535 ? gb : 65535), 128, 0, st>>>(
+      net, pixel_starts, block_starts, num_net, new_net, new_pixel_starts);
+  return cudaGetLastError();
+}
+
+int inference_mlp_param_count() { return kSpParams; }
+
+cudaError_t launch_inference_mlp(int spr, int num_block, float inv_far, float trans_stop, const int16_t* net,
+                                 int num_groups, const float* transparency, const int32_t* qpix,
+                                 const int32_t* pstarts, const float* centers, const float* samples,
+                                 const float* rays_d, const uint16_t* params, float* results, int* work,
+                                 uint32_t* err, int num_sms, cudaStream_t st) {
+  if (num_block <= 0) return cudaSuccess;
+  const int smem = kSpSmem + 1024;
+  static unsigned long long done = 0;
+  cudaError_t e = once_per_device(&done, [&]() {
+    return cudaFuncSetAttribute(inference_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  });
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(work, 0, sizeof(int), st)) != cudaSuccess) return e;
+  const int grid = min(2 * num_sms, num_block);
+  inference_mlp_kernel<<<grid, 128, smem, st>>>(spr, num_block, inv_far, trans_stop, net, num_groups, transparency,
+                                                qpix, pstarts, centers, samples, rays_d,
+                                                reinterpret_cast<const __half*>(params),
+                                                reinterpret_cast<float4*>(results), work, err);
+  return cudaGetLastError();
+}
+
+}  // namespace snisr
+
+using namespace snisr;
+
+extern "C" {
+
+snisr_status snisr_op_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, int64_t n, int64_t* num_unique,
+                                  void* stream) {
+  if (n < 0 || !num_unique) return set_error(SNISR_INVALID_ARG, "sort_by_key: bad argument");
+  if (n > ((int64_t)1 << 31) - 1) return set_error(SNISR_INVALID_ARG, "sort_by_key: more than 2^31-1 elements");
+  if (n > 0 && (!keys || !values || !starts)) return set_error(SNISR_INVALID_ARG, "sort_by_key: null argument");
+  cudaError_t e = launch_sort_by_key(keys, values, starts, n, num_unique, (cudaStream_t)stream);
+  if (e != cudaSuccess)
+    return set_error(e == cudaErrorMemoryAllocation ? SNISR_OOM : SNISR_CUDA_ERROR,
+                     std::string("sort_by_key: ") + cudaGetErrorString(e));
+  return SNISR_OK;
+}
+
+snisr_status snisr_op_assign_pixels(const int16_t* net, const int32_t* pixel_starts, const int32_t* block_starts,
+                                    int64_t num_net, int16_t* new_net, int32_t* new_pixel_starts, void* stream) {
+  if (num_net < 0) return set_error(SNISR_INVALID_ARG, "assign_pixels: bad size");
+  if (num_net == 0) return SNISR_OK;
+  if (!net || !pixel_starts || !block_starts || !new_net || !new_pixel_starts)
+    return set_error(SNISR_INVALID_ARG, "assign_pixels: null argument");
+  cudaError_t e = launch_assign_pixels(net, pixel_starts, block_starts, num_net, new_net, new_pixel_starts,
+                                       (cudaStream_t)stream);
+  if (e != cudaSuccess) return set_error(SNISR_CUDA_ERROR, std::string("assign_pixels: ") + cudaGetErrorString(e));
+  return SNISR_OK;
+}
+
+int32_t snisr_op_inference_mlp_param_count(void) { return inference_mlp_param_count(); }
+
+snisr_status snisr_op_inference_mlp(int32_t samples_per_ray, int32_t num_block, float inverse_far, float trans_stop,
+                                    const int16_t* net, int32_t num_groups, const float* transparency,
+                                    const int32_t* query_pixel_indices, const int32_t* pixel_starts,
+                                    const float* group_centers, const float* samples, const float* rays_d,
+                                    const uint16_t* params, float* sample_results, uint32_t* err_dev, void* stream) {
+  if (samples_per_ray <= 0 || num_block < 0 || num_groups < 0)
+    return set_error(SNISR_INVALID_ARG, "inference_mlp: bad size");
+  if (num_block == 0) return SNISR_OK;
+  if (!net || !transparency || !query_pixel_indices || !pixel_starts || !group_centers || !samples || !rays_d ||
+      !params || !sample_results)
+    return set_error(SNISR_INVALID_ARG, "inference_mlp: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int* work = nullptr;
+  cudaError_t e = cudaMallocAsync(&work, sizeof(int), st);
+  if (e != cudaSuccess) return set_error(SNISR_OOM, std::string("inference_mlp: ") + cudaGetErrorString(e));
+  e = launch_inference_mlp(samples_per_ray, num_block, inverse_far, trans_stop, net, num_groups, transparency,
+                           query_pixel_indices, pixel_starts, group_centers, samples, rays_d, params, sample_results,
+                           work, err_dev, sms > 0 ? sms : 1, st);
+  cudaError_t e2 = cudaFreeAsync(work, st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return set_error(SNISR_CUDA_ERROR, std::string("inference_mlp: ") + cudaGetErrorString(e));
+  return SNISR_OK;
+}
+
+}  // extern "C"

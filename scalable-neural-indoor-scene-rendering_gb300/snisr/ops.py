@@ -120,3 +120,95 @@ def sparse_sampling(rays_o, rays_d, node_flags, num_voxel, center, size, nsample
     d = torch.full((rays_o.shape[0], nsamples), -1, dtype=torch.float32, device=rays_o.device)
     Sample_sparse(rays_o, rays_d, node_flags.permute(2, 1, 0).contiguous(), *center, size, num_voxel, z, d)
     return z, d
+
+
+# ---------------------------------------------------------------------------
+# Specular pass (the reference's reflection MLP and its batching by network)
+# ---------------------------------------------------------------------------
+_err_words = {}
+
+
+def _err_word(device):
+    import torch
+    t = _err_words.get(device)
+    if t is None:
+        t = torch.zeros(1, dtype=torch.int32, device=device)
+        _err_words[device] = t
+    return t
+
+
+def check_errors():
+    """Synchronises and raises if an inference_mlp call's bounded device wait ran out."""
+    import torch
+    for dev, t in _err_words.items():
+        torch.cuda.synchronize(dev)
+        if int(t.item()) != 0:
+            t.zero_()
+            raise _lib.SnisrError(_lib.DEVICE_TIMEOUT, "inference_mlp: a bounded device wait ran out")
+
+
+def sort_by_key(keys_tensor, values_tensor, starts_tensor):
+    """Stable sort of (int16 keys, int32 values) in place, then unique_by_key
+    over (keys, starts); returns the number of distinct keys
+    (rendering/src/reorder.cu:10-22)."""
+    import torch
+    _check(keys_tensor, "keys", torch.int16)
+    _check(values_tensor, "values", torch.int32)
+    _check(starts_tensor, "starts", torch.int32)
+    n = keys_tensor.numel()
+    if values_tensor.numel() != n or starts_tensor.numel() != n:
+        raise RuntimeError("sort_by_key: keys, values and starts must have the same length")
+    import ctypes
+    out = ctypes.c_int64()
+    _lib.check(_lib.lib().snisr_op_sort_by_key(keys_tensor.data_ptr(), values_tensor.data_ptr(),
+                                               starts_tensor.data_ptr(), n, ctypes.byref(out), _stream()))
+    return int(out.value)
+
+
+def assign_pixels(netIdxs, pixel_starts, block_starts, num_thread, new_netIdxs, new_pixel_starts):
+    """Pixels of each network spread over its blocks (rendering/src/reorder.cu:24-94)."""
+    import torch
+    _check(netIdxs, "netIdxs", torch.int16)
+    _check(pixel_starts, "pixel_starts", torch.int32)
+    _check(block_starts, "block_starts", torch.int32)
+    _check(new_netIdxs, "new_netIdxs", torch.int16)
+    _check(new_pixel_starts, "new_pixel_starts", torch.int32)
+    num_net = netIdxs.numel()
+    if pixel_starts.numel() < num_net + 1 or block_starts.numel() < num_net + 1:
+        raise RuntimeError("assign_pixels: pixel_starts and block_starts need num_net + 1 entries")
+    _lib.check(_lib.lib().snisr_op_assign_pixels(netIdxs.data_ptr(), pixel_starts.data_ptr(), block_starts.data_ptr(),
+                                                 num_net, new_netIdxs.data_ptr(), new_pixel_starts.data_ptr(),
+                                                 _stream()))
+
+
+def inference_mlp(max_samples_per_ray, num_block, num_thread, inverse_far, trans_stop, netIdxs, transparency,
+                  query_pixel_indices, pixel_starts, group_centers, samples, rays_d, params, sample_results):
+    """Per-group reflection MLP with SH colour (rendering/src/rayreflection_render.cu:111-301) on tcgen05.
+    params: float16 [G, 22556] in the reference layout."""
+    import torch
+    _check(netIdxs, "netIdxs", torch.int16)
+    _check(transparency, "transparency", torch.float32)
+    _check(query_pixel_indices, "query_pixel_indices", torch.int32)
+    _check(pixel_starts, "pixel_starts", torch.int32)
+    _check(group_centers, "group_centers", torch.float32)
+    _check(samples, "samples", torch.float32)
+    _check(rays_d, "rays_d", torch.float32)
+    _check(sample_results, "sample_results", torch.float32)
+    if not params.is_cuda or not params.is_contiguous() or params.dtype != torch.float16:
+        raise RuntimeError("params must be a contiguous CUDA float16 tensor")
+    P = _lib.lib().snisr_op_inference_mlp_param_count()
+    if params.numel() % P != 0:
+        raise RuntimeError(f"params must hold a multiple of {P} values")
+    npix = query_pixel_indices.numel()
+    spr = int(max_samples_per_ray)
+    if samples.numel() != npix * spr * 3 or sample_results.numel() != npix * spr * 4 or rays_d.numel() != npix * 3:
+        raise RuntimeError("inference_mlp: samples / sample_results / rays_d sizes disagree with the pixel count")
+    if pixel_starts.numel() < int(num_block) + 1 or netIdxs.numel() < int(num_block):
+        raise RuntimeError("inference_mlp: netIdxs / pixel_starts shorter than num_block")
+    err = _err_word(samples.device)
+    _lib.check(_lib.lib().snisr_op_inference_mlp(spr, int(num_block), float(inverse_far), float(trans_stop),
+                                                 netIdxs.data_ptr(), params.numel() // P, transparency.data_ptr(),
+                                                 query_pixel_indices.data_ptr(), pixel_starts.data_ptr(),
+                                                 group_centers.data_ptr(), samples.data_ptr(), rays_d.data_ptr(),
+                                                 params.data_ptr(), sample_results.data_ptr(), err.data_ptr(),
+                                                 _stream()))

@@ -4,6 +4,7 @@ Python code on seeded inputs (CPU, float64):
   volume_rendering  training/scripts/utils.py:823-837   (cumprod compositing)
   query_voxel       training/scripts/tile/tile.py:225-236 (grid_sample lookup)
   Positional_Encoding  training/scripts/networks.py:4-15
+  eval_sh           training/scripts/sh.py:55-111 (degree 2)
 
 utils.py and tile.py import compiled extensions at module level, so only the
 needed function definitions are extracted (ast) and executed; networks.py
@@ -79,6 +80,16 @@ def main():
     pe = mod.Positional_Encoding(4)
     xp = rng.standard_normal((128, 3)).astype(np.float32)
     out.update(pe_x=xp, pe_out=pe(torch.from_numpy(xp).double()).numpy())
+
+    # SH degree 2 (training/scripts/sh.py eval_sh; sh [..., C, 9], unit dirs)
+    spec = importlib.util.spec_from_file_location("ref_sh", os.path.join(ref, "training/scripts/sh.py"))
+    shm = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(shm)
+    coeff = rng.standard_normal((256, 3, 9))
+    dirs = rng.standard_normal((256, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    out.update(sh_coeff=coeff, sh_dirs=dirs,
+               sh_out=shm.eval_sh(2, torch.from_numpy(coeff), torch.from_numpy(dirs)).numpy())
 
     path = os.path.join(HERE, "reference_python.npz")
     np.savez_compressed(path, **out)

@@ -262,3 +262,36 @@ def test_oracle_start_distance_skips_voxels():
     # the later sequence is a suffix of the full one
     for i in np.nonzero(c1)[0][:200]:
         assert list(v1[i, :c1[i]]) == list(v0[i, c0[i] - c1[i]:c0[i]])
+
+
+# ---------------------------------------------------------------- specular pass ops
+def test_sh2_matches_reference_python():
+    g = np.load(GOLD)
+    coeff = g["sh_coeff"].transpose(0, 2, 1).reshape(-1, 27)  # basis-major, as the device layout
+    np.testing.assert_allclose(oracle.eval_sh2(coeff, g["sh_dirs"]), g["sh_out"], rtol=0, atol=1e-12)
+
+
+def test_sort_by_key_is_stable_sort_plus_unique():
+    rng = np.random.default_rng(0)
+    keys = rng.integers(-1, 40, 5000).astype(np.int16)
+    k0 = keys.copy()
+    vals = rng.integers(0, 1 << 30, 5000).astype(np.int32)
+    v0 = vals.copy()
+    starts = np.arange(5000, dtype=np.int32)
+    n = oracle.op_sort_by_key(keys, vals, starts)
+    order = np.argsort(k0, kind="stable")
+    assert np.array_equal(vals, v0[order])
+    u, first = np.unique(k0[order], return_index=True)
+    assert n == u.size and np.array_equal(keys[:n], u) and np.array_equal(starts[:n], first)
+
+
+def test_assign_pixels_known_answer():
+    # net 7: 130 pixels over 3 blocks -> 44, 43, 43; net 2: 64 pixels over 1 block
+    net = np.array([7, 2], np.int16)
+    pixel_starts = np.array([0, 130, 194], np.int32)
+    block_starts = np.array([0, 3, 4], np.int32)
+    new_net = np.zeros(4, np.int16)
+    new_ps = np.zeros(4, np.int32)
+    oracle.op_assign_pixels(net, pixel_starts, block_starts, new_net, new_ps)
+    assert new_net.tolist() == [7, 7, 7, 2]
+    assert new_ps.tolist() == [0, 44, 87, 130]

@@ -1,0 +1,171 @@
+"""The reference's specular pass ops on the GPU against the oracle, called
+the way rendering/src/__init__.py:276-324 calls them (batching by network,
+then 4 steps of inverse-z sampling, reflection MLP and compositing).
+
+* sort_by_key, assign_pixels: bit-exact (keys, values, starts, run count,
+  per-block networks and pixel starts).
+* inference_mlp (tcgen05, FP16 operands, FP32 accumulation): writes exactly
+  the entries the oracle writes (skipped pixels untouched); against the
+  oracle's FP64 evaluation with FP16 operands: colour max-abs <= 1e-3,
+  density max-abs <= 2e-3 x max(1, |density|) (measured 1.3e-4, 3.7e-4);
+  against the oracle's restatement of the reference's FP16 arithmetic:
+  colour RMSE <= 1e-3 (measured 9.5e-5; the reference accumulates in FP16).
+* the 4-step specular frame: RMSE <= 2e-4 against the oracle pipeline
+  (measured 1.1e-5).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import snisr
+from snisr import ops
+
+import specular_problem as sp
+
+pytestmark = pytest.mark.gpu
+
+SENT = -7.0
+
+
+def _t(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _batch_gpu(net_t):
+    import torch
+    dev = net_t.device
+    npix = net_t.numel()
+    keys = net_t.clone()
+    q = torch.arange(npix, dtype=torch.int32, device=dev)
+    ps = torch.arange(npix, dtype=torch.int32, device=dev)
+    num_net = ops.sort_by_key(keys, q, ps)
+    end = torch.full((1,), npix, dtype=torch.int32, device=dev)
+    counts = torch.cat([ps[1:num_net], end]) - ps[:num_net]
+    ps2 = torch.cat([ps[:num_net], end])
+    bs = torch.cat([torch.zeros(1, dtype=torch.int32, device=dev), torch.cumsum(torch.ceil(counts / 64), 0).int()])
+    nb = int(bs[-1])
+    new_net = torch.empty(nb, dtype=torch.int16, device=dev)
+    new_ps = torch.empty(nb, dtype=torch.int32, device=dev)
+    ops.assign_pixels(keys[:num_net].contiguous(), ps2, bs, 0, new_net, new_ps)
+    return keys, q, num_net, nb, new_net, torch.cat([new_ps, end])
+
+
+def _batch_oracle(net):
+    npix = net.size
+    keys = net.copy()
+    q = np.arange(npix, dtype=np.int32)
+    ps = np.arange(npix, dtype=np.int32)
+    num_net = oracle.op_sort_by_key(keys, q, ps)
+    counts = np.concatenate([ps[1:num_net], [npix]]) - ps[:num_net]
+    ps2 = np.concatenate([ps[:num_net], [npix]]).astype(np.int32)
+    bs = np.concatenate([[0], np.cumsum(np.ceil(counts / 64))]).astype(np.int32)
+    nb = int(bs[-1])
+    new_net = np.zeros(nb, np.int16)
+    new_ps = np.zeros(nb, np.int32)
+    oracle.op_assign_pixels(np.ascontiguousarray(keys[:num_net]), ps2, bs, new_net, new_ps)
+    return keys, q, num_net, nb, new_net, np.concatenate([new_ps, [npix]]).astype(np.int32)
+
+
+def test_sort_by_key_bitexact(cuda):
+    rng = np.random.default_rng(1)
+    for n, lo, hi in ((100003, -1, 37), (5000, -32768, 32767), (1, 0, 1), (2048, 3, 4)):
+        keys = rng.integers(lo, hi, n).astype(np.int16)
+        vals = rng.integers(0, 1 << 30, n).astype(np.int32)
+        starts = rng.integers(0, 1 << 30, n).astype(np.int32)
+        k, v, s = _t(keys), _t(vals), _t(starts)
+        got = ops.sort_by_key(k, v, s)
+        want = oracle.op_sort_by_key(keys, vals, starts)
+        assert got == want
+        assert np.array_equal(k.cpu().numpy(), keys)  # run keys first, then the remaining sorted keys
+        assert np.array_equal(v.cpu().numpy(), vals)
+        assert np.array_equal(s.cpu().numpy()[:got], starts[:got])
+
+
+def test_batching_bitexact(cuda):
+    P = sp.problem(2)
+    g = _batch_gpu(_t(P["net"]))
+    o = _batch_oracle(P["net"])
+    assert g[2] == o[2] and g[3] == o[3]
+    assert np.array_equal(g[1].cpu().numpy(), o[1])
+    assert np.array_equal(g[4].cpu().numpy(), o[4]) and np.array_equal(g[5].cpu().numpy(), o[5])
+
+
+@pytest.fixture(scope="module")
+def spec(cuda):
+    P = sp.problem(3)
+    P["batch_gpu"] = _batch_gpu(_t(P["net"]))
+    P["batch_oracle"] = _batch_oracle(P["net"])
+    inv_near = P["inv_near"]
+    P["inv_bound"] = ((1.0 / (1.0 / inv_near + P["far"]) - inv_near) / 63).astype(np.float32)
+    return P
+
+
+def _samples(P, step):
+    pts, steps = oracle.op_inverse_z(P["rays_d"], P["origin"], P["inv_near"], P["inv_bound"], step, P["spr"])
+    return pts.reshape(P["npix"], P["spr"], 3).astype(np.float32), steps.reshape(P["npix"], P["spr"])
+
+
+def _mlp_gpu(P, samples, transparency):
+    _, q, _, nb, new_net, new_ps = P["batch_gpu"]
+    res = _t(np.full((P["npix"], P["spr"], 4), SENT, np.float32))
+    ops.inference_mlp(P["spr"], nb, 0, float(P["inverse_far"]), float(P["trans_stop"]), new_net, _t(transparency), q,
+                      new_ps, _t(P["centers"]), _t(samples), _t(P["rays_d"]), _t(P["params"]), res)
+    ops.check_errors()
+    return res.cpu().numpy()
+
+
+def _mlp_oracle(P, samples, transparency, mode):
+    _, q, _, nb, new_net, new_ps = P["batch_oracle"]
+    res = np.full((P["npix"], P["spr"], 4), SENT, np.float32)
+    oracle.op_inference_mlp(P["spr"], nb, P["inverse_far"], P["trans_stop"], new_net, transparency, q, new_ps,
+                            P["centers"], samples, P["rays_d"], P["params"].view(np.uint16), res, mode)
+    return res
+
+
+def test_inference_mlp_vs_oracle(spec):
+    P = spec
+    samples, _ = _samples(P, 0)
+    got = _mlp_gpu(P, samples, P["transparency"])
+    fp64 = _mlp_oracle(P, samples, P["transparency"], 1)
+    ref16 = _mlp_oracle(P, samples, P["transparency"], 0)
+    wrote = got[..., 0] != SENT
+    assert np.array_equal(wrote, fp64[..., 0] != SENT)
+    assert 0.5 < wrote.mean() < 0.95  # -1 networks and stopped pixels skipped
+    g, f, r = got[wrote], fp64[wrote], ref16[wrote]
+    e_rgb = float(np.abs(g[:, :3] - f[:, :3]).max())
+    e_sig = float((np.abs(g[:, 3] - f[:, 3]) / np.maximum(1.0, np.abs(f[:, 3]))).max())
+    rmse16 = float(np.sqrt(((g[:, :3] - r[:, :3]) ** 2).mean()))
+    print(f"inference_mlp: rgb max-abs vs FP64 {e_rgb:.3g}, density {e_sig:.3g}, rgb RMSE vs FP16 reference {rmse16:.3g}")
+    assert e_rgb <= 1e-3 and e_sig <= 2e-3
+    assert rmse16 <= 1e-3
+
+
+def test_specular_frame_vs_oracle(spec):
+    """Four steps of 16 samples, transmittance carried (rendering/src/__init__.py:307-320)."""
+    P = spec
+    npix = P["npix"]
+    t_g = P["transparency"].copy()
+    t_o = P["transparency"].copy()
+    f_g = np.zeros((npix, 3), np.float32)
+    f_o = np.zeros((npix, 3), np.float32)
+    import torch
+    tt, ff = _t(t_g), _t(f_g)
+    for step in range(0, 64, 16):
+        samples, steps = _samples(P, step)
+        res = _t(np.zeros((npix, P["spr"], 4), np.float32))
+        _, q, _, nb, new_net, new_ps = P["batch_gpu"]
+        ops.inference_mlp(P["spr"], nb, 0, float(P["inverse_far"]), float(P["trans_stop"]), new_net, tt, q, new_ps,
+                          _t(P["centers"]), _t(samples), _t(P["rays_d"]), _t(P["params"]), res)
+        ops.integrate_points(res, _t(steps.astype(np.float32)), 0, float(P["trans_stop"]), tt, ff)
+        ro = np.zeros((npix, P["spr"], 4), np.float32)
+        _, qo, _, nbo, nno, npso = P["batch_oracle"]
+        oracle.op_inference_mlp(P["spr"], nbo, P["inverse_far"], P["trans_stop"], nno, t_o, qo, npso, P["centers"],
+                                samples, P["rays_d"], P["params"].view(np.uint16), ro, 1)
+        oracle.op_integrate(ro, steps.astype(np.float32), float(P["trans_stop"]), f_o, t_o)
+    ops.check_errors()
+    torch.cuda.synchronize()
+    rmse = float(np.sqrt(((ff.cpu().numpy() - f_o) ** 2).mean()))
+    print(f"specular frame RMSE vs oracle {rmse:.3g}")
+    assert rmse <= 2e-4
+    assert float(np.abs(f_o).max()) > 0.05
