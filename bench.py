@@ -396,6 +396,90 @@ def large_scene_bench(dev, steps: int, warmup: int, flush):
     return res
 
 
+SPEC_WORKLOAD = ("specular pass of a 1280x720 frame at reflection scale 2 (640x360 pixels): batching by network "
+                 "(sort_by_key, assign_pixels), then 4 steps of 16 inverse-z samples -> per-group reflection MLP "
+                 "63-64x5-28 with SH degree 2 (16 groups) -> compositing; seeded synthetic networks and rays")
+SPEC_FLOP_PER_SAMPLE = 2 * (63 * 64 + 4 * 64 * 64 + 64 * 28)  # 44,416
+
+
+def specular_bench(dev, steps: int, warmup: int, flush):
+    """The reference's specular pass through the drop-in ops (FRender.render's
+    loop, rendering/src/__init__.py:276-320)."""
+    import numpy as np
+    import torch
+
+    from snisr import ops
+    from snisr import spec_synth as sp
+    P = sp.problem(seed=7, G=16, H=360, W=640)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    npix, spr = P["npix"], P["spr"]
+    net0, rays_d, origin = T(P["net"]), T(P["rays_d"]), T(P["origin"])
+    inv_near, centers, params = T(P["inv_near"]), T(P["centers"]), T(P["params"])
+    inv_bound = T(((1.0 / (1.0 / P["inv_near"] + P["far"]) - P["inv_near"]) / 63).astype(np.float32))
+    trans0 = T(P["transparency"])
+    samples = torch.empty(npix, spr, 3, device=dev)
+    isteps = torch.empty(npix, spr, device=dev)
+    results = torch.zeros(npix, spr, 4, device=dev)
+    frame = torch.zeros(npix, 3, device=dev)
+    trans = torch.empty_like(trans0)
+    stream = torch.cuda.current_stream()
+    ev_mlp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(4)]
+
+    def frame_pass(record_mlp=False):
+        keys = net0.clone()
+        q = torch.arange(npix, dtype=torch.int32, device=dev)
+        ps = torch.arange(npix, dtype=torch.int32, device=dev)
+        num_net = ops.sort_by_key(keys, q, ps)
+        end = torch.full((1,), npix, dtype=torch.int32, device=dev)
+        counts = torch.cat([ps[1:num_net], end]) - ps[:num_net]
+        bs = torch.cat([torch.zeros(1, dtype=torch.int32, device=dev), torch.cumsum(torch.ceil(counts / 64), 0).int()])
+        nb = int(bs[-1])
+        new_net = torch.empty(nb, dtype=torch.int16, device=dev)
+        new_ps = torch.empty(nb, dtype=torch.int32, device=dev)
+        ops.assign_pixels(keys[:num_net].contiguous(), torch.cat([ps[:num_net], end]), bs, 0, new_net, new_ps)
+        new_ps = torch.cat([new_ps, end])
+        trans.copy_(trans0)
+        frame.zero_()
+        for k, step in enumerate(range(0, 64, spr)):
+            results.zero_()
+            ops.inverse_z_sampling(origin, rays_d, inv_near, inv_bound, 0, step, spr, samples, isteps)
+            if record_mlp:
+                ev_mlp[k][0].record(stream)
+            ops.inference_mlp(spr, nb, 0, float(P["inverse_far"]), float(P["trans_stop"]), new_net, trans, q, new_ps,
+                              centers, samples, rays_d, params, results)
+            if record_mlp:
+                ev_mlp[k][1].record(stream)
+            ops.integrate_points(results, isteps, 0, float(P["trans_stop"]), trans, frame)
+
+    for _ in range(warmup):
+        frame_pass()
+    torch.cuda.synchronize()
+    ops.check_errors()
+    # samples the MLP evaluates: pixels with a network whose initial transmittance
+    # passes the stop, 64 each (an upper bound: early-stopped pixels drop out later)
+    live = int(((trans0 >= float(P["trans_stop"])) & (net0 >= 0)).sum()) * 64
+    total = mlp_ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        frame_pass(record_mlp=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+        mlp_ms += sum(a.elapsed_time(b) for a, b in ev_mlp)
+    ops.check_errors()
+    ms, mlp = total / steps, mlp_ms / steps
+    _, tc_peak, kind = _peaks()
+    tflops = live * SPEC_FLOP_PER_SAMPLE / (mlp * 1e-3) / 1e12
+    return {"workload": SPEC_WORKLOAD, "unit": "Mpixels/s", "value": round(npix / ms / 1e3, 3),
+            "ms_per_step": round(ms, 4), "mlp_ms_per_frame": round(mlp, 4),
+            "mlp_samples_per_frame_upper_bound": live,
+            "mlp_tflops": round(tflops, 2), "mlp_tensor_frac": round(tflops / tc_peak, 4),
+            "note": "samples counted with the initial transmittance (an upper bound on the live samples)",
+            "l2": "flushed before each frame"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -427,7 +511,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-train", action="store_true")
     ap.add_argument("--no-large", action="store_true")
-    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large"], default=None,
+    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular"], default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
     args = ap.parse_args()
@@ -444,9 +528,10 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run in ("train", "batched", "large"):
+    if args.profile_run in ("train", "batched", "large", "specular"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-        fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench}[args.profile_run]
+        fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench,
+              "specular": specular_bench}[args.profile_run]
         res = fn(dev, args.steps, args.warmup, flush)
         print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
@@ -601,6 +686,7 @@ def main():
         batched = batched_bench(dev, min(10, max(3, args.steps // 4)), 3, flush)
     if not args.no_large:
         large = large_scene_bench(dev, min(32, max(4, args.steps // 4)), 3, flush)
+    specular = specular_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -629,6 +715,7 @@ def main():
             "train": train,
             "train_batched": batched,
             "large_scene": large,
+            "specular_pass": specular,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

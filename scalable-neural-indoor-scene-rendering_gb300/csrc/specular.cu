@@ -189,9 +189,10 @@ __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
 }
 
 // shared memory: A (16 KB) | W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) |
-// bias tiles B0, B1 (2 x 8 KB) | 1/16 atom (1 KB) | barriers, slots
-constexpr int kSpA = 0, kSpW = 16384, kSpWout = kSpW + 5 * 8192, kSpB0 = kSpWout + 4096, kSpB1 = kSpB0 + 8192,
-              kSpOnes = kSpB1 + 8192, kSpBars = kSpOnes + 1024, kSpSmem = kSpBars + 64;
+// FP32 biases [6][64] (1.5 KB, added by the epilogues) | barriers, slots:
+// ~62 KB, three CTAs per SM
+constexpr int kSpA = 0, kSpW = 16384, kSpWout = kSpW + 5 * 8192, kSpBias = kSpWout + 4096,
+              kSpBars = kSpBias + 6 * 64 * 4, kSpSmem = kSpBars + 64;
 
 // pack network g's parameters (reference layout, FP16) into the swizzled tiles
 __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
@@ -222,23 +223,18 @@ __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
     }
     *reinterpret_cast<uint4*>(sm + kSpWout + swz(j, 8 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
-  // bias tiles: B0 K-slices 0..3 = layers 0..3; B1 slice 0 = layer 4, slice 1 = output (rows < 28)
-  for (int e = tid; e < 2 * kSpH * 8; e += 128) {
-    const int t = e / (kSpH * 8), j = (e / 8) % kSpH, c = e % 8;
-    const int slice = c / 2;  // 16 K columns = 2 chunks of 8
-    int layer = -1;
-    if (t == 0) layer = slice;
-    else if (slice == 0) layer = kSpHidden - 1;
-    else if (slice == 1) layer = kSpHidden;
+  // biases (FP32), layer l at [l][64]; output layer: 28 used
+  float* bias = reinterpret_cast<float*>(sm + kSpBias);
+  for (int e = tid; e < 6 * 64; e += 128) {
+    const int l = e / 64, j = e % 64;
     float b = 0.f;
-    if (layer >= 0 && layer < kSpHidden) b = __half2float(P[sp_layer_off(layer) + j]);
-    else if (layer == kSpHidden && j < kSpOut) b = __half2float(P[sp_layer_off(kSpHidden) + j]);
-    const uint32_t h = pack_h2(b, b);
-    *reinterpret_cast<uint4*>(sm + (t == 0 ? kSpB0 : kSpB1) + swz(j, 8 * c)) = make_uint4(h, h, h, h);
+    if (l < kSpHidden) b = __half2float(P[sp_layer_off(l) + j]);
+    else if (j < kSpOut) b = __half2float(P[sp_layer_off(kSpHidden) + j]);
+    bias[e] = b;
   }
 }
 
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 3)
     inference_mlp_kernel(int spr, int num_block, float inv_far, float trans_stop, const int16_t* __restrict__ net,
                          int num_groups, const float* __restrict__ transparency, const int32_t* __restrict__ qpix,
                          const int32_t* __restrict__ pstarts, const float* __restrict__ centers,
@@ -259,15 +255,13 @@ __global__ void __launch_bounds__(128, 2)
     tc::tmem_alloc(tc::smem_addr(tmem_slot), 64);
     tc::tmem_relinquish();
   }
-  for (int k = tid; k < 64; k += 128)  // 1/16 in FP16: bias step D += (1/16) * 16 copies of b = b
-    reinterpret_cast<uint4*>(sm + kSpOnes)[k] = make_uint4(0x2C002C00u, 0x2C002C00u, 0x2C002C00u, 0x2C002C00u);
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-  const uint64_t ones = tc::sdesc_sw128_sbo(tc::smem_addr(sm + kSpOnes), 0);
+  const float* bias = reinterpret_cast<const float*>(sm + kSpBias);
   const uint32_t a_base = tc::smem_addr(sm + kSpA);
   const uint32_t id_h = tc::idesc_f16(kSpH, 0), id_o = tc::idesc_f16(32, 0);
   uint32_t mphase = 0;
@@ -304,15 +298,23 @@ __global__ void __launch_bounds__(128, 2)
         if (live) {
           const float p[3] = {(samples[3 * ori] - cx) * inv_far, (samples[3 * ori + 1] - cy) * inv_far,
                               (samples[3 * ori + 2] - cz) * inv_far};
+          // sin/cos of 2^i p (i = 0..9): one accurate sincos per coordinate, then
+          // double-angle steps (error ~2^9 x FP32 rounding at i = 9, below half
+          // an FP16 ulp)
           float x[64];
           x[0] = p[0]; x[1] = p[1]; x[2] = p[2];
+          float sn[3], cs[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) sincosf(p[a], &sn[a], &cs[a]);
 #pragma unroll
           for (int i = 0; i < 10; ++i) {
-            const float f = (float)(1 << i);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-              x[3 + 6 * i + a] = __sinf(f * p[a]);
-              x[6 + 6 * i + a] = __cosf(f * p[a]);
+              x[3 + 6 * i + a] = sn[a];
+              x[6 + 6 * i + a] = cs[a];
+              const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
+              sn[a] = s2;
+              cs[a] = c2;
             }
           }
           x[63] = 0.f;
@@ -338,8 +340,6 @@ __global__ void __launch_bounds__(128, 2)
           const uint32_t id = last ? id_o : id_h;
           for (int kk = 0; kk < 4; ++kk)
             tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
-          const uint32_t bt = tc::smem_addr(sm + (l < 4 ? kSpB0 + 32 * l : kSpB1 + 32 * (l - 4)));
-          tc::mma_f16(tmem, ones, tc::sdesc_sw128(bt), id, 1);
           tc::mma_commit(mbar);
         }
         const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
@@ -358,7 +358,8 @@ __global__ void __launch_bounds__(128, 2)
               uint32_t o[4];
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
-                float a0 = v[8 * q + 2 * j], a1 = v[8 * q + 2 * j + 1];
+                const int col = 32 * half + 8 * q + 2 * j;
+                float a0 = v[8 * q + 2 * j] + bias[64 * l + col], a1 = v[8 * q + 2 * j + 1] + bias[64 * l + col + 1];
                 a0 = a0 < 0.f ? 0.01f * a0 : a0;
                 a1 = a1 < 0.f ? 0.01f * a1 : a1;
                 o[j] = pack_h2(a0, a1);
@@ -372,6 +373,8 @@ __global__ void __launch_bounds__(128, 2)
           tc::tmem_ld16(taddr, out);
           tc::tmem_ld16(taddr + 16, out + 16);
           tc::tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < kSpOut; ++j) out[j] += bias[64 * kSpHidden + j];
         }
         tc::fence_before_sync();
         __syncthreads();
@@ -474,7 +477,7 @@ cudaError_t launch_inference_mlp(int spr, int num_block, float inv_far, float tr
   });
   if (e != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(work, 0, sizeof(int), st)) != cudaSuccess) return e;
-  const int grid = min(2 * num_sms, num_block);
+  const int grid = min(3 * num_sms, num_block);  // three CTAs per SM (shared memory ~63 KB each)
   inference_mlp_kernel<<<grid, 128, smem, st>>>(spr, num_block, inv_far, trans_stop, net, num_groups, transparency,
                                                 qpix, pstarts, centers, samples, rays_d,
                                                 reinterpret_cast<const __half*>(params),

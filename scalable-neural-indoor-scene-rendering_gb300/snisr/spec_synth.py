@@ -1,7 +1,9 @@
-"""Seeded synthetic inputs for the reference's specular pass ops (test and
-benchmark infrastructure): per-group reflection MLPs in the reference's
-parameter layout, group centres, a downscaled pixel grid of rays with their
-first-hit inverse depth, per-pixel network ids (-1 = none) and transmittance."""
+"""Seeded synthetic inputs for the specular pass ops (inputs for tests and
+benchmarks; the reference's trained networks and captured scenes are not
+distributed): per-group reflection MLPs in the reference's parameter layout
+(rendering/src/rayreflection_render.cu:111-301), group centres, a downscaled
+pixel grid of rays with their first-hit inverse depth, per-pixel network ids
+(-1 = none) and transmittance."""
 from __future__ import annotations
 
 import numpy as np

@@ -20,7 +20,7 @@ import oracle
 import snisr
 from snisr import ops
 
-import specular_problem as sp
+from snisr import spec_synth as sp
 
 pytestmark = pytest.mark.gpu
 
