@@ -307,6 +307,25 @@ snisr_status snisr_op_inference_mlp(int32_t samples_per_ray, int32_t num_block, 
                                     const uint16_t* params_dev, float* sample_results_dev,
                                     uint32_t* err_dev, void* stream);
 
+/* FASTRENDERING.rendering_diffuse_octree_fp16
+ * (rendering/src/raydiffuse_render_octree_fp16.cu:141-287) on the reference's
+ * scene format: rays_d [npix][3], visited [npix][K] sparse tile ids (-1
+ * padded, from snisr_op_tracing_tiles), origin [3] (device), group_map
+ * [NT] (tile2group), data_voxels [Nv][4] FP16 bit patterns, block_map
+ * [NT][64], node_map [Nn][D^3] int16, sample_flags [Nn][D^3] bytes (bool),
+ * voxels_start [Nn] int64, centers [NT][3]; D = num_voxel / 4 + 2 (18).
+ * Writes frame [npix][3]; inverse_near [npix] and net_idx [npix] only at
+ * pixels with a first hit (transmittance below trans_th), as the reference.
+ * FP16 trilinear and compositing with the CUDA half intrinsics; tile ids
+ * outside [0, num_tiles) are skipped. */
+snisr_status snisr_op_rendering_diffuse_octree(
+    const float* rays_d_dev, const int32_t* visited_dev, int64_t npix, int32_t K,
+    const float* origin_dev, const int32_t* group_map_dev, const uint16_t* data_voxels_dev,
+    const int32_t* block_map_dev, const int16_t* node_map_dev, const uint8_t* sample_flags_dev,
+    const int64_t* voxels_start_dev, const float* centers_dev, int32_t num_tiles, float tile_size,
+    float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
+    float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Seeded synthetic scenes (input generation for tests and benchmarks).      */
 /* ------------------------------------------------------------------------ */

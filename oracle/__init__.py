@@ -63,6 +63,9 @@ def lib() -> C.CDLL:
             "oracle_op_inverse_z": (None, [P, P, P, P, C.c_int64, C.c_int, C.c_int, P, P]),
             "oracle_op_integrate": (None, [P, P, C.c_int64, C.c_float, P, P]),
             "oracle_op_sort_by_key": (C.c_int64, [P, P, P, C.c_int64]),
+            "oracle_op_rendering_diffuse_octree": (None, [P, P, C.c_int64, C.c_int, P, P, P, P, P, P, P, P, C.c_float,
+                                                          C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, P, P, P,
+                                                          C.c_int]),
             "oracle_eval_sh2": (None, [P, P, C.c_int64, P]),
             "oracle_op_assign_pixels": (None, [P, P, P, C.c_int64, P, P]),
             "oracle_op_inference_mlp": (None, [C.c_int, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P, P, P, P,
@@ -304,3 +307,25 @@ def eval_sh2(coeff_basis_major, dirs):
     out = np.zeros((d.shape[0], 3))
     lib().oracle_eval_sh2(_p(c), _p(d), d.shape[0], _p(out))
     return out
+
+
+def op_rendering_diffuse_octree(rays_d, visited, origin, data: dict, sample_step, trans_th, early_stop,
+                                frame, inverse_near, net_idx, nthreads: int | None = None):
+    """FASTRENDERING.rendering_diffuse_octree_fp16 on reference-format scene data (numpy dict with
+    tile2group, data_voxels, block_IndexMap, nodes_IndexMap, nodes_sampleFlag, voxels_start, centers,
+    num_voxel, voxel_size); frame [n,3], inverse_near [n], net_idx [n] int16 written in place
+    (inverse_near / net_idx only at first hits, as the reference)."""
+    n = rays_d.reshape(-1, 3).shape[0]
+    K = visited.reshape(n, -1).shape[1]
+    voxel = float(data["voxel_size"][0])
+    tile = int(data["num_voxel"][0]) * voxel
+    D = int(data["num_voxel"][0]) // (2 ** int(data["octree_depth"][0])) + 2
+    arr = [np.ascontiguousarray(rays_d, np.float32), np.ascontiguousarray(visited, np.int32)]
+    o = np.ascontiguousarray(origin, np.float32)
+    sc = [np.ascontiguousarray(data["tile2group"], np.int32), np.ascontiguousarray(data["data_voxels"], np.float16).view(np.uint16),
+          np.ascontiguousarray(data["block_IndexMap"], np.int32), np.ascontiguousarray(data["nodes_IndexMap"], np.int16),
+          np.ascontiguousarray(data["nodes_sampleFlag"]).astype(np.uint8),
+          np.ascontiguousarray(data["voxels_start"], np.int64), np.ascontiguousarray(data["centers"], np.float32)]
+    lib().oracle_op_rendering_diffuse_octree(_p(arr[0]), _p(arr[1]), n, K, _p(o), *map(_p, sc), tile, voxel,
+                                             float(sample_step), D, float(trans_th), float(early_stop), _p(frame),
+                                             _p(inverse_near), _p(net_idx), nthreads or threads())

@@ -1315,4 +1315,162 @@ void oracle_op_inference_mlp(int spr, int64_t num_block, float inverse_far, floa
     }
   });
 }
+
+}  // extern "C"
+namespace {
+// ---------------------------------------------------------------------------
+// FASTRENDERING.rendering_diffuse_octree_fp16 (rendering/src/
+// raydiffuse_render_octree_fp16.cu:10-235): per pixel, the visited tiles in
+// order; per tile a DDA over its 4^3 blocks; in a block with a node, samples
+// every sample_step from the block entry, taken where the node's sample flag
+// is set; FP16 trilinear of the node's half4 RGBA through its short index map
+// (half_ope.h:222-296) and FP16 compositing (hexp); early stop on the FP16
+// transmittance; the first sample with transmittance below trans_th records
+// 1/(z + tile entry) and the tile's group.  Each FP16 operation rounds once
+// (round to nearest even); hexp is exp rounded to FP16.  FP32 position
+// arithmetic is written without fused multiply-adds.  Reads outside a node's
+// 18^3 grid (not reached by in-block samples) are skipped.
+struct OctreeView {
+  const int32_t* group_map;    // [NT]
+  const uint16_t* data;        // [Nv][4] FP16
+  const int32_t* block_map;    // [NT][64]
+  const int16_t* node_map;     // [Nn][D^3]
+  const uint8_t* sample_flag;  // [Nn][D^3]
+  const int64_t* vstart;       // [Nn]
+  const float* centers;        // [NT][3]
+  float tile_size, voxel_size, sample_step;
+  int D;                       // dilated voxels per block side (18)
+};
+constexpr int kOctBlocks = 4;
+
+inline float hexp16(float x) { return round_f16((float)std::exp((double)x)); }
+
+void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const int32_t* vis, int K,
+                  float trans_th_h, float early, float out_rgb[3], float* inv_near, int16_t* net) {
+  float col[3] = {0.f, 0.f, 0.f};
+  float T = 1.0f;  // FP16 values held in float
+  const float early_h = round_f16(early);
+  bool first_hit = false;
+  const float bs = V.tile_size / (float)kOctBlocks;
+  const int D = V.D, DD = D * D, D3 = D * D * D;
+  for (int i = 0; i < K; ++i) {
+    const int tile = vis[i];
+    if (tile == -1) break;
+    if (T < early_h) break;
+    const int group = V.group_map[tile];
+    const float* c = V.centers + 3 * (int64_t)tile;
+    const float hs = V.tile_size / 2.0f;
+    const float h3[3] = {hs, hs, hs};
+    const Bound b = ray_aabb(o, d, c, h3);
+    if (b.lo == -1.0f) continue;
+    float ro[3];
+    for (int a = 0; a < 3; ++a) {
+      const float corner = c[a] - hs;
+      ro[a] = (o[a] + b.lo * d[a]) - corner;
+      ro[a] = std::min(std::max(ro[a], 0.0f), V.tile_size - 0.00001f);
+    }
+    // block DDA (raydiffuse_render_octree_fp16.cu:39-131)
+    int cb[3], st[3];
+    float tmax[3], tdel[3];
+    for (int a = 0; a < 3; ++a) {
+      cb[a] = (int)(ro[a] / bs);
+      st[a] = d[a] >= 0.0f ? 1 : -1;
+      float nb = (float)(cb[a] + st[a]) * bs;
+      if (st[a] < 0) nb = nb + bs;
+      tmax[a] = safe_divide(nb - ro[a], d[a]);
+      tdel[a] = safe_divide(bs * (float)st[a], d[a]);
+    }
+    if (cb[0] < 0 || cb[1] < 0 || cb[2] < 0 || cb[0] >= kOctBlocks || cb[1] >= kOctBlocks || cb[2] >= kOctBlocks)
+      continue;  // entry rounded onto the far face: skipped (the reference reads out of range there)
+    float near_ = 0.0f, far_ = std::fmin(std::fmin(tmax[0], tmax[1]), tmax[2]);
+    const int32_t* bmap = V.block_map + (int64_t)tile * kOctBlocks * kOctBlocks * kOctBlocks;
+    for (;;) {
+      const int nidx = bmap[(cb[0] * kOctBlocks + cb[1]) * kOctBlocks + cb[2]];
+      if (nidx != -1) {
+        const int16_t* nodes = V.node_map + (int64_t)nidx * D3;
+        const uint8_t* flags = V.sample_flag + (int64_t)nidx * D3;
+        const uint16_t* vox = V.data + 4 * V.vstart[nidx];
+        float dc[3];
+        for (int a = 0; a < 3; ++a) dc[a] = (float)cb[a] * bs - V.voxel_size;
+        float z = near_;
+        while (z < far_) {
+          float pts[3], rel[3];
+          int vl[3];
+          for (int a = 0; a < 3; ++a) {
+            pts[a] = ro[a] + z * d[a];
+            rel[a] = (pts[a] - dc[a]) / V.voxel_size;
+            vl[a] = (int)rel[a];
+          }
+          const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;
+          if (!inside || !flags[vl[0] * DD + vl[1] * D + vl[2]]) {
+            z = z + V.sample_step;
+            continue;
+          }
+          if (!first_hit && T < trans_th_h) {
+            first_hit = true;
+            *inv_near = 1.0f / (z + b.lo);
+            *net = (int16_t)group;
+          }
+          float f[3];
+          int x0[3];
+          for (int a = 0; a < 3; ++a) {
+            f[a] = rel[a] - 0.5f;
+            x0[a] = (int)f[a];
+          }
+          bool ok = true;
+          for (int a = 0; a < 3; ++a) ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
+          if (ok) {
+            float w[3];
+            for (int a = 0; a < 3; ++a) w[a] = std::max(f[a] - (float)x0[a], 0.0f);
+            // corner k: (dx, dy, dz) = ((k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1) in the reference's v1..v8 order
+            float v[8][4];
+            for (int k = 0; k < 8; ++k) {
+              const int xi = x0[0] + (k & 1), yi = x0[1] + ((k >> 1) & 1), zi = x0[2] + ((k >> 2) & 1);
+              const int idx = nodes[xi * DD + yi * D + zi];
+              for (int q = 0; q < 4; ++q) v[k][q] = f16_to_f32(vox[4 * (int64_t)idx + q]);
+            }
+            auto lerp = [](float a, float bb, float x) {
+              return hadd(hmul(a, h16(1.0f - x)), hmul(bb, h16(x)));
+            };
+            float rgba[4];
+            for (int q = 0; q < 4; ++q) {
+              const float s0 = lerp(lerp(v[0][q], v[1][q], w[0]), lerp(v[2][q], v[3][q], w[0]), w[1]);
+              const float s1 = lerp(lerp(v[4][q], v[5][q], w[0]), lerp(v[6][q], v[7][q], w[0]), w[1]);
+              rgba[q] = lerp(s0, s1, w[2]);
+            }
+            const float interval = std::min(V.sample_step, far_ - z);
+            const float step_h = h16(interval);
+            const float alpha = hsub(1.0f, hexp16(hmul(hmul(rgba[3], -1.0f), step_h)));
+            const float wgt = hmul(alpha, T);
+            for (int a = 0; a < 3; ++a) col[a] = hadd(col[a], hmul(wgt, rgba[a]));
+            T = hmul(T, hsub(1.0f, alpha));
+          }
+          z = z + V.sample_step;
+        }
+      }
+      const int a = dda_axis(tmax);
+      cb[a] += st[a];
+      tmax[a] = tmax[a] + tdel[a];
+      near_ = far_;
+      far_ = std::fmin(std::fmin(tmax[0], tmax[1]), tmax[2]);
+      if (cb[0] < 0 || cb[1] < 0 || cb[2] < 0 || cb[0] >= kOctBlocks || cb[1] >= kOctBlocks || cb[2] >= kOctBlocks) break;
+    }
+  }
+  for (int a = 0; a < 3; ++a) out_rgb[a] = col[a];
+}
+}  // namespace
+extern "C" {
+
+void oracle_op_rendering_diffuse_octree(const float* rays_d, const int32_t* visited, int64_t npix, int K,
+                                        const float* origin, const int32_t* group_map, const uint16_t* data,
+                                        const int32_t* block_map, const int16_t* node_map, const uint8_t* flags,
+                                        const int64_t* vstart, const float* centers, float tile_size,
+                                        float voxel_size, float sample_step, int D, float trans_th, float early,
+                                        float* frame, float* inv_near, int16_t* net, int threads) {
+  OctreeView V{group_map, data, block_map, node_map, flags, vstart, centers, tile_size, voxel_size, sample_step, D};
+  const float th = round_f16(trans_th);
+  parallel_for(npix, threads, [&](int64_t i) {
+    octree_pixel(V, origin, rays_d + 3 * i, visited + i * K, K, th, early, frame + 3 * i, inv_near + i, net + i);
+  });
+}
 }  // extern "C"

@@ -1,0 +1,197 @@
+// Drop-in for the reference's diffuse renderer on its own scene format
+// (FASTRENDERING.rendering_diffuse_octree_fp16,
+// rendering/src/raydiffuse_render_octree_fp16.cu:10-235): per pixel the
+// visited tiles in order; per tile a DDA over its 4^3 blocks; in a block with
+// a node, samples every sample_step from the block entry where the node's
+// sample flag is set; FP16 trilinear of the node's half4 RGBA through its
+// int16 index map and FP16 compositing; early stop on the FP16
+// transmittance; the first sample with transmittance below trans_th records
+// 1/(z + tile entry) and the tile's group.  Every FP16 and FP32 operation
+// rounds on its own (the _rn intrinsics keep the compiler from contracting a
+// multiply and an add into one fused operation; the reference's build may
+// fuse some of them, which changes results by FP16 ulps).  The camera origin is a
+// kernel argument (the reference keeps it in a __constant__ symbol) and the
+// stream is the caller's.  Tile ids outside [0, num_tiles) and reads outside
+// a node's dilated grid are skipped.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "device_common.cuh"
+#include "snisr.h"
+#include "snisr_internal.h"
+
+namespace snisr {
+namespace {
+
+constexpr int kOctBlocks = 4;
+
+__device__ __forceinline__ __half hlerp(__half a, __half b, float x) {  // a * (1 - x) + b * x, FP16
+  return __hadd_rn(__hmul_rn(a, __float2half(fsub(1.0f, x))), __hmul_rn(b, __float2half(x)));
+}
+
+__global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const int32_t* __restrict__ visited,
+                                      int64_t npix, int K, const float* __restrict__ origin,
+                                      const int32_t* __restrict__ group_map, const uint2* __restrict__ data,
+                                      const int32_t* __restrict__ block_map, const int16_t* __restrict__ node_map,
+                                      const uint8_t* __restrict__ flags, const int64_t* __restrict__ vstart,
+                                      const float* __restrict__ centers, int num_tiles, float tile_size,
+                                      float voxel_size, float sample_step, int D, __half trans_th, float early,
+                                      float* frame, float* inv_near, int16_t* net) {
+  const int DD = D * D, D3 = D * D * D;
+  const float bs = fdiv(tile_size, (float)kOctBlocks);
+  const __half early_h = __float2half(early);
+  const __half one = __float2half(1.0f);
+  const float o[3] = {__ldg(origin), __ldg(origin + 1), __ldg(origin + 2)};
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+    const float d[3] = {rays_d[3 * p], rays_d[3 * p + 1], rays_d[3 * p + 2]};
+    __half col[3] = {__float2half(0.f), __float2half(0.f), __float2half(0.f)};
+    __half T = one;
+    bool first_hit = false;
+    const int32_t* vis = visited + p * K;
+    for (int i = 0; i < K; ++i) {
+      const int tile = vis[i];
+      if (tile == -1) break;
+      if (__hlt(T, early_h)) break;
+      if (tile < 0 || tile >= num_tiles) continue;
+      const int group = group_map[tile];
+      const float c[3] = {centers[3 * tile], centers[3 * tile + 1], centers[3 * tile + 2]};
+      const float hs = fdiv(tile_size, 2.0f);
+      const float h3[3] = {hs, hs, hs};
+      const float2 b = slab(o, d, c, h3);
+      if (b.x == -1.0f) continue;
+      float ro[3];
+      int cb[3], st[3];
+      float tmax[3], tdel[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        ro[a] = fsub(fadd(o[a], fmul(b.x, d[a])), fsub(c[a], hs));
+        ro[a] = fminf(fmaxf(ro[a], 0.0f), fsub(tile_size, 0.00001f));
+        cb[a] = (int)fdiv(ro[a], bs);
+        st[a] = d[a] >= 0.0f ? 1 : -1;
+        float nb = fmul((float)(cb[a] + st[a]), bs);
+        if (st[a] < 0) nb = fadd(nb, bs);
+        tmax[a] = safe_div(fsub(nb, ro[a]), d[a]);
+        tdel[a] = safe_div(fmul(bs, (float)st[a]), d[a]);
+      }
+      if (cb[0] < 0 || cb[1] < 0 || cb[2] < 0 || cb[0] >= kOctBlocks || cb[1] >= kOctBlocks || cb[2] >= kOctBlocks)
+        continue;  // entry rounded onto the far face (tile sizes where 1e-5 is below FP32 resolution)
+      float near_ = 0.0f, far_ = fminf(fminf(tmax[0], tmax[1]), tmax[2]);
+      const int32_t* bmap = block_map + (int64_t)tile * kOctBlocks * kOctBlocks * kOctBlocks;
+      for (;;) {
+        const int nidx = bmap[(cb[0] * kOctBlocks + cb[1]) * kOctBlocks + cb[2]];
+        if (nidx != -1) {
+          const int16_t* nodes = node_map + (int64_t)nidx * D3;
+          const uint8_t* fl = flags + (int64_t)nidx * D3;
+          const uint2* vox = data + vstart[nidx];
+          float dc[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) dc[a] = fsub(fmul((float)cb[a], bs), voxel_size);
+          float z = near_;
+          while (z < far_) {
+            float rel[3];
+            int vl[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              rel[a] = fdiv(fsub(fadd(ro[a], fmul(z, d[a])), dc[a]), voxel_size);
+              vl[a] = (int)rel[a];
+            }
+            const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;
+            if (!inside || !fl[vl[0] * DD + vl[1] * D + vl[2]]) {
+              z = fadd(z, sample_step);
+              continue;
+            }
+            if (!first_hit && __hlt(T, trans_th)) {
+              first_hit = true;
+              inv_near[p] = fdiv(1.0f, fadd(z, b.x));
+              net[p] = (int16_t)group;
+            }
+            float f[3];
+            int x0[3];
+            bool ok = true;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              f[a] = fsub(rel[a], 0.5f);
+              x0[a] = (int)f[a];
+              ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
+            }
+            if (ok) {
+              float w[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) w[a] = fmaxf(fsub(f[a], (float)x0[a]), 0.0f);
+              __half v[8][4];
+#pragma unroll
+              for (int k = 0; k < 8; ++k) {
+                const int xi = x0[0] + (k & 1), yi = x0[1] + ((k >> 1) & 1), zi = x0[2] + ((k >> 2) & 1);
+                const uint2 q = __ldg(vox + nodes[xi * DD + yi * D + zi]);
+                v[k][0] = __ushort_as_half((unsigned short)(q.x & 0xFFFFu));
+                v[k][1] = __ushort_as_half((unsigned short)(q.x >> 16));
+                v[k][2] = __ushort_as_half((unsigned short)(q.y & 0xFFFFu));
+                v[k][3] = __ushort_as_half((unsigned short)(q.y >> 16));
+              }
+              __half rgba[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                const __half s0 = hlerp(hlerp(v[0][q], v[1][q], w[0]), hlerp(v[2][q], v[3][q], w[0]), w[1]);
+                const __half s1 = hlerp(hlerp(v[4][q], v[5][q], w[0]), hlerp(v[6][q], v[7][q], w[0]), w[1]);
+                rgba[q] = hlerp(s0, s1, w[2]);
+              }
+              const float interval = fminf(sample_step, fsub(far_, z));
+              const __half alpha =
+                  __hsub_rn(one, hexp(__hmul_rn(__hmul_rn(rgba[3], __float2half(-1.0f)), __float2half(interval))));
+              const __half wgt = __hmul_rn(alpha, T);
+#pragma unroll
+              for (int a = 0; a < 3; ++a) col[a] = __hadd_rn(col[a], __hmul_rn(wgt, rgba[a]));
+              T = __hmul_rn(T, __hsub_rn(one, alpha));
+            }
+            z = fadd(z, sample_step);
+          }
+        }
+        int a = 2;
+        if (tmax[0] < tmax[1]) a = tmax[0] < tmax[2] ? 0 : 2;
+        else a = tmax[1] < tmax[2] ? 1 : 2;
+        cb[a] += st[a];
+        tmax[a] = fadd(tmax[a], tdel[a]);
+        near_ = far_;
+        far_ = fminf(fminf(tmax[0], tmax[1]), tmax[2]);
+        if (cb[a] < 0 || cb[a] >= kOctBlocks) break;
+      }
+    }
+    frame[3 * p] = __half2float(col[0]);
+    frame[3 * p + 1] = __half2float(col[1]);
+    frame[3 * p + 2] = __half2float(col[2]);
+  }
+}
+
+}  // namespace
+}  // namespace snisr
+
+using namespace snisr;
+
+extern "C" snisr_status snisr_op_rendering_diffuse_octree(
+    const float* rays_d, const int32_t* visited, int64_t npix, int32_t K, const float* origin,
+    const int32_t* group_map, const uint16_t* data_voxels, const int32_t* block_map, const int16_t* node_map,
+    const uint8_t* sample_flags, const int64_t* voxels_start, const float* centers, int32_t num_tiles,
+    float tile_size, float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
+    float* frame, float* inverse_near, int16_t* net_idx, void* stream) {
+  if (npix < 0 || K <= 0 || num_tiles <= 0 || dilated_voxels <= 1 || !(tile_size > 0) || !(voxel_size > 0) ||
+      !(sample_step > 0))
+    return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: bad size");
+  if (npix == 0) return SNISR_OK;
+  if (!rays_d || !visited || !origin || !group_map || !data_voxels || !block_map || !node_map ||
+      !sample_flags || !voxels_start || !centers || !frame || !inverse_near || !net_idx)
+    return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: null argument");
+  if (reinterpret_cast<uintptr_t>(data_voxels) % 8 != 0)
+    return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: data_voxels must be 8-byte aligned");
+  const int64_t blocks = (npix + 127) / 128;
+  octree_diffuse_kernel<<<(int)(blocks < (1 << 20) ? blocks : (1 << 20)), 128, 0, (cudaStream_t)stream>>>(
+      rays_d, visited, npix, K, origin, group_map,
+      reinterpret_cast<const uint2*>(data_voxels), block_map, node_map, sample_flags, voxels_start, centers, num_tiles,
+      tile_size, voxel_size, sample_step, dilated_voxels, __float2half(trans_th), early_stop, frame, inverse_near,
+      net_idx);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return set_error(SNISR_CUDA_ERROR, std::string("rendering_diffuse_octree: ") + cudaGetErrorString(e));
+  return SNISR_OK;
+}

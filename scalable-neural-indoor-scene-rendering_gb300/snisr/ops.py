@@ -212,3 +212,40 @@ def inference_mlp(max_samples_per_ray, num_block, num_thread, inverse_far, trans
                                                  group_centers.data_ptr(), samples.data_ptr(), rays_d.data_ptr(),
                                                  params.data_ptr(), sample_results.data_ptr(), err.data_ptr(),
                                                  _stream()))
+
+
+def rendering_diffuse_octree_fp16(rays_d, visitedTiles, origin, groupMap, data_voxels, block_IndexMap,
+                                  nodes_IndexMap, nodes_sampleFlag, voxels_start, centers, tile_size, voxel_size,
+                                  sample_step, num_voxel, num_thread, trans_th, early_stop, soft_hit,
+                                  frame_diffuse, inverse_near, netIdxs):
+    """The reference's FP16 diffuse renderer on its octree scene format
+    (rendering/src/raydiffuse_render_octree_fp16.cu:141-287); num_voxel is the
+    dilated node side (18); outputs written in place."""
+    import torch
+    if soft_hit:
+        raise RuntimeError("rendering_diffuse_octree_fp16: soft_hit is not supported (the reference renderer "
+                           "calls it with False)")
+    _check(rays_d, "rays_d", torch.float32)
+    _check(visitedTiles, "visitedTiles", torch.int32)
+    _check(origin, "origin", torch.float32)
+    _check(groupMap, "groupMap", torch.int32)
+    _check(block_IndexMap, "block_IndexMap", torch.int32)
+    _check(nodes_IndexMap, "nodes_IndexMap", torch.int16)
+    _check(voxels_start, "voxels_start", torch.int64)
+    _check(centers, "centers", torch.float32)
+    _check(frame_diffuse, "frame_diffuse", torch.float32)
+    _check(inverse_near, "inverse_near", torch.float32)
+    _check(netIdxs, "netIdxs", torch.int16)
+    for t, n, dt in ((data_voxels, "data_voxels", torch.float16), (nodes_sampleFlag, "nodes_sampleFlag", torch.bool)):
+        if not t.is_cuda or not t.is_contiguous() or t.dtype != dt:
+            raise RuntimeError(f"{n} must be a contiguous CUDA {dt} tensor")
+    npix = frame_diffuse.numel() // 3
+    K = visitedTiles.shape[-1]
+    if rays_d.numel() != npix * 3 or visitedTiles.numel() != npix * K or inverse_near.numel() != npix:
+        raise RuntimeError("rendering_diffuse_octree_fp16: pixel counts disagree")
+    _lib.check(_lib.lib().snisr_op_rendering_diffuse_octree(
+        rays_d.data_ptr(), visitedTiles.data_ptr(), npix, K, origin.data_ptr(), groupMap.data_ptr(),
+        data_voxels.data_ptr(), block_IndexMap.data_ptr(), nodes_IndexMap.data_ptr(), nodes_sampleFlag.data_ptr(),
+        voxels_start.data_ptr(), centers.data_ptr(), centers.shape[0], float(tile_size), float(voxel_size),
+        float(sample_step), int(num_voxel), float(trans_th), float(early_stop), frame_diffuse.data_ptr(),
+        inverse_near.data_ptr(), netIdxs.data_ptr(), _stream()))
