@@ -480,6 +480,109 @@ def specular_bench(dev, steps: int, warmup: int, flush):
             "l2": "flushed before each frame"}
 
 
+PIPE_WORKLOAD = ("the reference's whole frame (FRender.render, rendering/src/__init__.py:247-334) through the drop-in "
+                 "ops at 1280x720: compute_rays -> tracing_tiles -> FP16 octree diffuse renderer on renderData format "
+                 "(16 tiles of 64^3, converted synthetic scene) -> specular pass at reflection scale 2 (batching, "
+                 "4 x [inverse-z sampling, reflection MLP, compositing]) -> bilinear upsampling -> clamp(diffuse + "
+                 "specular); no CNN")
+
+
+def reference_pipeline_bench(dev, steps: int, warmup: int, flush):
+    """The reference renderer's per-frame op chain on this library's drop-ins."""
+    import numpy as np
+    import torch
+    import torch.nn.functional as F
+
+    import snisr
+    from snisr import octree, ops
+    cfg = snisr.CFG2.replace(res=64, with_mesh=False)
+    synth = snisr.SynthScene(cfg)
+    data = octree.from_synth(synth, groups=synth.desc.num_tiles, seed=5)
+    T = octree.to_device(data, dev)
+    der = octree.derived(data)
+    cams = [synth.camera(p) for p in range(cfg.poses)]
+    H, W, K = cfg.height, cfg.width, 30
+    DH, DW = H // 2, W // 2
+    far = der["far"]
+    scene_size = torch.tensor(der["scene_size"], dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def frame(cam, record=False):
+        intr = torch.tensor([cam.cx, cam.cy, cam.inv_focal], dtype=torch.float32, device=dev)
+        rot = torch.tensor([[cam.c2w[0], cam.c2w[1], cam.c2w[2]], [cam.c2w[4], cam.c2w[5], cam.c2w[6]],
+                            [cam.c2w[8], cam.c2w[9], cam.c2w[10]]], dtype=torch.float32, device=dev)
+        origin = torch.tensor([cam.c2w[3], cam.c2w[7], cam.c2w[11]], dtype=torch.float32, device=dev)
+        if record:
+            ev[0].record(stream)
+        rays_d = torch.full((H, W, 3), -1.0, device=dev)
+        visited = torch.full((H, W, K), -1, dtype=torch.int32, device=dev)
+        diffuse = torch.full((H, W, 3), -1.0, device=dev)
+        inv_near = torch.full((H, W), 1e-8, device=dev)
+        net = torch.full((H, W), -1, dtype=torch.int16, device=dev)
+        ops.compute_rays(intr, rot, 0, rays_d)
+        ops.tracing_tiles(rays_d, T["tile_IndexMap"], origin, T["tile_shape"], T["scene_min_corner"], scene_size,
+                          der["tile_size"], 0, visited)
+        ops.rendering_diffuse_octree_fp16(rays_d, visited, origin, T["tile2group"], T["data_voxels"],
+                                          T["block_IndexMap"], T["nodes_IndexMap"], T["nodes_sampleFlag"],
+                                          T["voxels_start"], T["centers"], der["tile_size"], der["voxel_size"],
+                                          der["sample_step"], der["block_num_voxel"], 256, 0.8, 0.01, False,
+                                          diffuse, inv_near, net)
+        if record:
+            ev[1].record(stream)
+        inv_s = inv_near[::2, ::2].contiguous()
+        net_s = net[::2, ::2].flatten().contiguous()
+        rays_s = rays_d[::2, ::2].contiguous()
+        npix = DH * DW
+        q = torch.arange(npix, dtype=torch.int32, device=dev)
+        ps = torch.arange(npix, dtype=torch.int32, device=dev)
+        num_net = ops.sort_by_key(net_s, q, ps)
+        end = torch.full((1,), npix, dtype=torch.int32, device=dev)
+        counts = torch.cat([ps[1:num_net], end]) - ps[:num_net]
+        bs = torch.cat([torch.zeros(1, dtype=torch.int32, device=dev), torch.cumsum(torch.ceil(counts / 64), 0).int()])
+        nb = int(bs[-1])
+        new_net = torch.empty(nb, dtype=torch.int16, device=dev)
+        new_ps = torch.empty(nb, dtype=torch.int32, device=dev)
+        ops.assign_pixels(net_s[:num_net].contiguous(), torch.cat([ps[:num_net], end]), bs, 0, new_net, new_ps)
+        new_ps = torch.cat([new_ps, end])
+        sample_far = 1.0 / inv_s + far
+        inv_bound = ((1.0 / sample_far - inv_s) / 63).contiguous()
+        trans = torch.ones(DH, DW, 1, device=dev)
+        spec = torch.zeros(DH, DW, 3, device=dev)
+        for step in range(0, 64, 16):
+            res = torch.zeros(DH, DW, 16, 4, device=dev)
+            pts = torch.full((DH, DW, 16, 3), -1.0, device=dev)
+            isteps = torch.zeros(DH, DW, 16, device=dev)
+            ops.inverse_z_sampling(origin, rays_s, inv_s, inv_bound, 0, step, 16, pts, isteps)
+            ops.inference_mlp(16, nb, 0, 1.0 / far, 0.01, new_net, trans, q, new_ps, T["group_centers"], pts, rays_s,
+                              T["net_params"], res)
+            ops.integrate_points(res, isteps, 0, 0.01, trans, spec)
+        spec_up = F.interpolate(spec[None].permute(0, 3, 1, 2), scale_factor=2, mode="bilinear",
+                                align_corners=True)[0].permute(1, 2, 0)
+        final = torch.clamp(diffuse + spec_up, 0, 1)
+        if record:
+            ev[2].record(stream)
+        return final
+
+    for i in range(warmup):
+        frame(cams[i % len(cams)])
+    torch.cuda.synchronize()
+    ops.check_errors()
+    total = diff_ms = 0.0
+    for i in range(steps):
+        flush.zero_()
+        frame(cams[i % len(cams)], record=True)
+        torch.cuda.synchronize()
+        total += ev[0].elapsed_time(ev[2])
+        diff_ms += ev[0].elapsed_time(ev[1])
+    ops.check_errors()
+    ms = total / steps
+    return {"workload": PIPE_WORKLOAD, "unit": "FPS", "value": round(1e3 / ms, 2), "ms_per_step": round(ms, 4),
+            "diffuse_ms": round(diff_ms / steps, 4), "mrays_s": round(H * W / ms / 1e3, 3),
+            "note": "includes sort_by_key's host synchronisation (it returns a count, as the reference's op does)",
+            "l2": "flushed before each frame"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -511,7 +614,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-train", action="store_true")
     ap.add_argument("--no-large", action="store_true")
-    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular"], default=None,
+    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular", "pipeline"],
+                    default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
     args = ap.parse_args()
@@ -528,10 +632,10 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run in ("train", "batched", "large", "specular"):
+    if args.profile_run in ("train", "batched", "large", "specular", "pipeline"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
         fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench,
-              "specular": specular_bench}[args.profile_run]
+              "specular": specular_bench, "pipeline": reference_pipeline_bench}[args.profile_run]
         res = fn(dev, args.steps, args.warmup, flush)
         print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
@@ -687,6 +791,7 @@ def main():
     if not args.no_large:
         large = large_scene_bench(dev, min(32, max(4, args.steps // 4)), 3, flush)
     specular = specular_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
+    pipeline = reference_pipeline_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -716,6 +821,7 @@ def main():
             "train_batched": batched,
             "large_scene": large,
             "specular_pass": specular,
+            "reference_pipeline": pipeline,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

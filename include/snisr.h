@@ -315,7 +315,9 @@ snisr_status snisr_op_inference_mlp(int32_t samples_per_ray, int32_t num_block, 
  * [NT][64], node_map [Nn][D^3] int16, sample_flags [Nn][D^3] bytes (bool),
  * voxels_start [Nn] int64, centers [NT][3]; D = num_voxel / 4 + 2 (18).
  * Writes frame [npix][3]; inverse_near [npix] and net_idx [npix] only at
- * pixels with a first hit (transmittance below trans_th), as the reference.
+ * pixels with a first hit (transmittance below trans_th), as the reference;
+ * with soft_hit != 0 a pixel without a first hit whose last examined tile has
+ * a group takes that group and 1 / (the tile's exit distance).
  * FP16 trilinear and compositing with the CUDA half intrinsics; tile ids
  * outside [0, num_tiles) are skipped. */
 snisr_status snisr_op_rendering_diffuse_octree(
@@ -324,7 +326,7 @@ snisr_status snisr_op_rendering_diffuse_octree(
     const int32_t* block_map_dev, const int16_t* node_map_dev, const uint8_t* sample_flags_dev,
     const int64_t* voxels_start_dev, const float* centers_dev, int32_t num_tiles, float tile_size,
     float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
-    float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
+    int32_t soft_hit, float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Seeded synthetic scenes (input generation for tests and benchmarks).      */

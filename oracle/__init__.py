@@ -64,8 +64,8 @@ def lib() -> C.CDLL:
             "oracle_op_integrate": (None, [P, P, C.c_int64, C.c_float, P, P]),
             "oracle_op_sort_by_key": (C.c_int64, [P, P, P, C.c_int64]),
             "oracle_op_rendering_diffuse_octree": (None, [P, P, C.c_int64, C.c_int, P, P, P, P, P, P, P, P, C.c_float,
-                                                          C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, P, P, P,
-                                                          C.c_int]),
+                                                          C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int,
+                                                          P, P, P, C.c_int]),
             "oracle_eval_sh2": (None, [P, P, C.c_int64, P]),
             "oracle_op_assign_pixels": (None, [P, P, P, C.c_int64, P, P]),
             "oracle_op_inference_mlp": (None, [C.c_int, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P, P, P, P,
@@ -310,7 +310,7 @@ def eval_sh2(coeff_basis_major, dirs):
 
 
 def op_rendering_diffuse_octree(rays_d, visited, origin, data: dict, sample_step, trans_th, early_stop,
-                                frame, inverse_near, net_idx, nthreads: int | None = None):
+                                frame, inverse_near, net_idx, nthreads: int | None = None, soft_hit: bool = False):
     """FASTRENDERING.rendering_diffuse_octree_fp16 on reference-format scene data (numpy dict with
     tile2group, data_voxels, block_IndexMap, nodes_IndexMap, nodes_sampleFlag, voxels_start, centers,
     num_voxel, voxel_size); frame [n,3], inverse_near [n], net_idx [n] int16 written in place
@@ -327,5 +327,6 @@ def op_rendering_diffuse_octree(rays_d, visited, origin, data: dict, sample_step
           np.ascontiguousarray(data["nodes_sampleFlag"]).astype(np.uint8),
           np.ascontiguousarray(data["voxels_start"], np.int64), np.ascontiguousarray(data["centers"], np.float32)]
     lib().oracle_op_rendering_diffuse_octree(_p(arr[0]), _p(arr[1]), n, K, _p(o), *map(_p, sc), tile, voxel,
-                                             float(sample_step), D, float(trans_th), float(early_stop), _p(frame),
+                                             float(sample_step), D, float(trans_th), float(early_stop), int(soft_hit),
+                                             _p(frame),
                                              _p(inverse_near), _p(net_idx), nthreads or threads())

@@ -1326,7 +1326,9 @@ namespace {
 // is set; FP16 trilinear of the node's half4 RGBA through its short index map
 // (half_ope.h:222-296) and FP16 compositing (hexp); early stop on the FP16
 // transmittance; the first sample with transmittance below trans_th records
-// 1/(z + tile entry) and the tile's group.  Each FP16 operation rounds once
+// 1/(z + tile entry) and the tile's group; with soft_hit a pixel without a
+// first hit takes the last examined tile's group and 1/(its exit distance)
+// (:223-228).  Each FP16 operation rounds once
 // (round to nearest even); hexp is exp rounded to FP16.  FP32 position
 // arithmetic is written without fused multiply-adds.  Reads outside a node's
 // 18^3 grid (not reached by in-block samples) are skipped.
@@ -1346,11 +1348,13 @@ constexpr int kOctBlocks = 4;
 inline float hexp16(float x) { return round_f16((float)std::exp((double)x)); }
 
 void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const int32_t* vis, int K,
-                  float trans_th_h, float early, float out_rgb[3], float* inv_near, int16_t* net) {
+                  float trans_th_h, float early, bool soft_hit, float out_rgb[3], float* inv_near, int16_t* net) {
   float col[3] = {0.f, 0.f, 0.f};
   float T = 1.0f;  // FP16 values held in float
   const float early_h = round_f16(early);
   bool first_hit = false;
+  int last_group = -1;
+  float last_exit = 0.0f;
   const float bs = V.tile_size / (float)kOctBlocks;
   const int D = V.D, DD = D * D, D3 = D * D * D;
   for (int i = 0; i < K; ++i) {
@@ -1362,6 +1366,8 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
     const float hs = V.tile_size / 2.0f;
     const float h3[3] = {hs, hs, hs};
     const Bound b = ray_aabb(o, d, c, h3);
+    last_group = group;
+    last_exit = b.hi;
     if (b.lo == -1.0f) continue;
     float ro[3];
     for (int a = 0; a < 3; ++a) {
@@ -1456,6 +1462,10 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
       if (cb[0] < 0 || cb[1] < 0 || cb[2] < 0 || cb[0] >= kOctBlocks || cb[1] >= kOctBlocks || cb[2] >= kOctBlocks) break;
     }
   }
+  if (soft_hit && !first_hit && last_group != -1) {
+    *inv_near = 1.0f / last_exit;
+    *net = (int16_t)last_group;
+  }
   for (int a = 0; a < 3; ++a) out_rgb[a] = col[a];
 }
 }  // namespace
@@ -1466,11 +1476,12 @@ void oracle_op_rendering_diffuse_octree(const float* rays_d, const int32_t* visi
                                         const int32_t* block_map, const int16_t* node_map, const uint8_t* flags,
                                         const int64_t* vstart, const float* centers, float tile_size,
                                         float voxel_size, float sample_step, int D, float trans_th, float early,
-                                        float* frame, float* inv_near, int16_t* net, int threads) {
+                                        int soft_hit, float* frame, float* inv_near, int16_t* net, int threads) {
   OctreeView V{group_map, data, block_map, node_map, flags, vstart, centers, tile_size, voxel_size, sample_step, D};
   const float th = round_f16(trans_th);
   parallel_for(npix, threads, [&](int64_t i) {
-    octree_pixel(V, origin, rays_d + 3 * i, visited + i * K, K, th, early, frame + 3 * i, inv_near + i, net + i);
+    octree_pixel(V, origin, rays_d + 3 * i, visited + i * K, K, th, early, soft_hit != 0, frame + 3 * i, inv_near + i,
+                 net + i);
   });
 }
 }  // extern "C"

@@ -6,7 +6,9 @@
 // sample flag is set; FP16 trilinear of the node's half4 RGBA through its
 // int16 index map and FP16 compositing; early stop on the FP16
 // transmittance; the first sample with transmittance below trans_th records
-// 1/(z + tile entry) and the tile's group.  Every FP16 and FP32 operation
+// 1/(z + tile entry) and the tile's group; with soft_hit a pixel without a
+// first hit takes the last examined tile's group and 1/(its exit distance)
+// (:223-228).  Every FP16 and FP32 operation
 // rounds on its own (the _rn intrinsics keep the compiler from contracting a
 // multiply and an add into one fused operation; the reference's build may
 // fuse some of them, which changes results by FP16 ulps).  The camera origin is a
@@ -38,7 +40,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
                                       const uint8_t* __restrict__ flags, const int64_t* __restrict__ vstart,
                                       const float* __restrict__ centers, int num_tiles, float tile_size,
                                       float voxel_size, float sample_step, int D, __half trans_th, float early,
-                                      float* frame, float* inv_near, int16_t* net) {
+                                      bool soft_hit, float* frame, float* inv_near, int16_t* net) {
   const int DD = D * D, D3 = D * D * D;
   const float bs = fdiv(tile_size, (float)kOctBlocks);
   const __half early_h = __float2half(early);
@@ -49,6 +51,8 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
     __half col[3] = {__float2half(0.f), __float2half(0.f), __float2half(0.f)};
     __half T = one;
     bool first_hit = false;
+    int last_group = -1;
+    float last_exit = 0.0f;
     const int32_t* vis = visited + p * K;
     for (int i = 0; i < K; ++i) {
       const int tile = vis[i];
@@ -60,6 +64,8 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
       const float hs = fdiv(tile_size, 2.0f);
       const float h3[3] = {hs, hs, hs};
       const float2 b = slab(o, d, c, h3);
+      last_group = group;
+      last_exit = b.y;
       if (b.x == -1.0f) continue;
       float ro[3];
       int cb[3], st[3];
@@ -158,6 +164,10 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
         if (cb[a] < 0 || cb[a] >= kOctBlocks) break;
       }
     }
+    if (soft_hit && !first_hit && last_group != -1) {
+      inv_near[p] = fdiv(1.0f, last_exit);
+      net[p] = (int16_t)last_group;
+    }
     frame[3 * p] = __half2float(col[0]);
     frame[3 * p + 1] = __half2float(col[1]);
     frame[3 * p + 2] = __half2float(col[2]);
@@ -174,7 +184,7 @@ extern "C" snisr_status snisr_op_rendering_diffuse_octree(
     const int32_t* group_map, const uint16_t* data_voxels, const int32_t* block_map, const int16_t* node_map,
     const uint8_t* sample_flags, const int64_t* voxels_start, const float* centers, int32_t num_tiles,
     float tile_size, float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
-    float* frame, float* inverse_near, int16_t* net_idx, void* stream) {
+    int32_t soft_hit, float* frame, float* inverse_near, int16_t* net_idx, void* stream) {
   if (npix < 0 || K <= 0 || num_tiles <= 0 || dilated_voxels <= 1 || !(tile_size > 0) || !(voxel_size > 0) ||
       !(sample_step > 0))
     return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: bad size");
@@ -188,8 +198,8 @@ extern "C" snisr_status snisr_op_rendering_diffuse_octree(
   octree_diffuse_kernel<<<(int)(blocks < (1 << 20) ? blocks : (1 << 20)), 128, 0, (cudaStream_t)stream>>>(
       rays_d, visited, npix, K, origin, group_map,
       reinterpret_cast<const uint2*>(data_voxels), block_map, node_map, sample_flags, voxels_start, centers, num_tiles,
-      tile_size, voxel_size, sample_step, dilated_voxels, __float2half(trans_th), early_stop, frame, inverse_near,
-      net_idx);
+      tile_size, voxel_size, sample_step, dilated_voxels, __float2half(trans_th), early_stop, soft_hit != 0, frame,
+      inverse_near, net_idx);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return set_error(SNISR_CUDA_ERROR, std::string("rendering_diffuse_octree: ") + cudaGetErrorString(e));

@@ -134,7 +134,7 @@ _SIGNATURES = {
     "snisr_op_inference_mlp_param_count": (C.c_int32, []),
     "snisr_op_rendering_diffuse_octree": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32,
                                                     C.c_float, C.c_float, C.c_float, C.c_int32, C.c_float, C.c_float,
-                                                    P, P, P, P]),
+                                                    C.c_int32, P, P, P, P]),
     "snisr_op_inference_mlp": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, P, C.c_int32, P, P, P, P, P, P, P,
                                          P, P, P]),
     "snisr_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(P), C.POINTER(SceneDesc)]),

@@ -222,9 +222,6 @@ def rendering_diffuse_octree_fp16(rays_d, visitedTiles, origin, groupMap, data_v
     (rendering/src/raydiffuse_render_octree_fp16.cu:141-287); num_voxel is the
     dilated node side (18); outputs written in place."""
     import torch
-    if soft_hit:
-        raise RuntimeError("rendering_diffuse_octree_fp16: soft_hit is not supported (the reference renderer "
-                           "calls it with False)")
     _check(rays_d, "rays_d", torch.float32)
     _check(visitedTiles, "visitedTiles", torch.int32)
     _check(origin, "origin", torch.float32)
@@ -247,5 +244,6 @@ def rendering_diffuse_octree_fp16(rays_d, visitedTiles, origin, groupMap, data_v
         rays_d.data_ptr(), visitedTiles.data_ptr(), npix, K, origin.data_ptr(), groupMap.data_ptr(),
         data_voxels.data_ptr(), block_IndexMap.data_ptr(), nodes_IndexMap.data_ptr(), nodes_sampleFlag.data_ptr(),
         voxels_start.data_ptr(), centers.data_ptr(), centers.shape[0], float(tile_size), float(voxel_size),
-        float(sample_step), int(num_voxel), float(trans_th), float(early_stop), frame_diffuse.data_ptr(),
+        float(sample_step), int(num_voxel), float(trans_th), float(early_stop), int(bool(soft_hit)),
+        frame_diffuse.data_ptr(),
         inverse_near.data_ptr(), netIdxs.data_ptr(), _stream()))

@@ -63,3 +63,15 @@ def test_oracle_renders_converted_scene():
     assert (net >= 0).mean() > 0.5 and frame.max() > 0.3
     hit = net >= 0
     assert (inv[hit] > 0).all() and (inv[hit] < 10).all()
+    # soft_hit: first hits unchanged
+    f2, i2 = np.zeros((n, 3), np.float32), np.full(n, 1e-8, np.float32)
+    n2 = np.full(n, -1, np.int16)
+    oracle.op_rendering_diffuse_octree(d, vis, o, D, der["sample_step"], 0.8, 0.01, f2, i2, n2, soft_hit=True)
+    assert np.array_equal(f2, frame) and np.array_equal(n2[hit], net[hit]) and np.array_equal(i2[hit], inv[hit])
+    # trans_th 0 (no first hits): with soft_hit every pixel that examined a tile gets a network
+    f3, i3 = np.zeros((n, 3), np.float32), np.full(n, 1e-8, np.float32)
+    n3 = np.full(n, -1, np.int16)
+    oracle.op_rendering_diffuse_octree(d, vis, o, D, der["sample_step"], 0.0, 0.01, f3, i3, n3, soft_hit=True)
+    some = vis[:, 0] >= 0
+    assert some.sum() > n // 2 and np.array_equal(f3, frame)
+    assert (n3[some] >= 0).all() and (i3[some] != 1e-8).all() and (n3[~some] == -1).all()

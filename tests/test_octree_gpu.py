@@ -2,7 +2,9 @@
 format (FASTRENDERING.rendering_diffuse_octree_fp16) against the oracle's
 restatement, on synthetic scenes converted to renderData format (1 tile and
 16 tiles of 64^3), called with the reference's arguments after the
-compute_rays and tracing_tiles drop-ins.
+compute_rays and tracing_tiles drop-ins, with soft_hit off (the reference
+renderer's setting, first-hit threshold 0.8) and on (threshold 0, so every
+pixel takes the soft-hit path).
 
 Both round every FP16 and FP32 operation on its own, and CUDA's hexp equals
 exp rounded to FP16 on the inputs used: colour, first-hit inverse depth and
@@ -22,9 +24,11 @@ def _t(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
+@pytest.mark.parametrize("soft", [False, True], ids=["hard", "soft"])
 @pytest.mark.parametrize("cfg", [snisr.CFG1, snisr.CFG2.replace(res=64, with_mesh=False)], ids=["1tile", "16tiles"])
-def test_octree_diffuse_vs_oracle(cuda, cfg):
+def test_octree_diffuse_vs_oracle(cuda, cfg, soft):
     import torch
+    th = 0.0 if soft else 0.8
     s = snisr.SynthScene(cfg)
     D = octree.from_synth(s, groups=min(4, s.desc.num_tiles))
     der = octree.derived(D)
@@ -46,7 +50,7 @@ def test_octree_diffuse_vs_oracle(cuda, cfg):
     ops.rendering_diffuse_octree_fp16(rays_d, visited, origin, T["tile2group"], T["data_voxels"],
                                       T["block_IndexMap"], T["nodes_IndexMap"], T["nodes_sampleFlag"],
                                       T["voxels_start"], T["centers"], der["tile_size"], der["voxel_size"],
-                                      der["sample_step"], der["block_num_voxel"], 256, 0.8, 0.01, False,
+                                      der["sample_step"], der["block_num_voxel"], 256, th, 0.01, soft,
                                       frame, inv, net)
     torch.cuda.synchronize()
     n = H * W
@@ -55,7 +59,8 @@ def test_octree_diffuse_vs_oracle(cuda, cfg):
     fo = np.zeros((n, 3), np.float32)
     io = np.full(n, 1e-8, np.float32)
     no = np.full(n, -1, np.int16)
-    oracle.op_rendering_diffuse_octree(rd, vis, origin.cpu().numpy(), D, der["sample_step"], 0.8, 0.01, fo, io, no)
+    oracle.op_rendering_diffuse_octree(rd, vis, origin.cpu().numpy(), D, der["sample_step"], th, 0.01, fo, io, no,
+                                       soft_hit=soft)
     fg, ig, ng = frame.cpu().numpy().reshape(n, 3), inv.cpu().numpy().reshape(n), net.cpu().numpy().reshape(n)
     diff = np.abs(fg - fo).max(axis=1)
     same = (ig == io) & (ng == no)
