@@ -583,6 +583,97 @@ def reference_pipeline_bench(dev, steps: int, warmup: int, flush):
             "l2": "flushed before each frame"}
 
 
+PRUNE_WORKLOAD = ("occupancy pruning of one 128^3 tile of the 4x4x1-tile scene after an epoch (Tile.pruning, "
+                  "training/scripts/tile/tile.py:297-395): transparency statistic of every camera ray of 8 "
+                  "1280x720 views that crosses the tile (step 0.1 voxel), 3^3 max filter + block-maximum "
+                  "thresholds (initial flags = the current occupancy) + border dilation, packing into occupancy "
+                  "words")
+
+
+def pruning_bench(dev, steps: int, warmup: int, flush):
+    """Tile.pruning's device work on one tile: rays resident in HBM."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import oracle
+    import snisr
+    from snisr import ops, prune
+    from snisr.scene import camera_rays
+    s = snisr.SynthScene(snisr.CFG2)
+    a = s.arrays()
+    t = 5
+    sig_d, vsig, flags = prune.grids_from_arrays(s.desc, a, t)
+    center_np = prune.tile_centers(s.desc, a)[t]
+    tile = float(s.desc.tile_size)
+    N = int(s.desc.res)
+    D = N + 2
+    vs = tile / N
+    step = vs * 0.1
+    c = torch.from_numpy(center_np).to(dev)
+    ro, rd = [], []
+    for v in range(8):
+        cam = s.camera(v)
+        d = camera_rays(cam, dev.index or 0).reshape(-1, 3)
+        o = torch.tensor([cam.c2w[3], cam.c2w[7], cam.c2w[11]], dtype=torch.float32, device=dev).expand_as(d)
+        inv = 1.0 / d
+        t0, t1 = (c - tile / 2 - o) * inv, (c + tile / 2 - o) * inv
+        lo = torch.minimum(t0, t1).nan_to_num(-1e30).amax(1)
+        hi = torch.maximum(t0, t1).nan_to_num(1e30).amin(1)
+        keep = hi > lo.clamp_min(0)
+        ro.append(o[keep].contiguous())
+        rd.append(d[keep].contiguous())
+    ro, rd = torch.cat(ro).contiguous(), torch.cat(rd).contiguous()
+    nrays = ro.shape[0]
+    init = np.where(flags[1:-1, 1:-1, 1:-1] == 1, 1, -1).astype(np.int16)  # the current occupancy
+    sig_t, vsig_t, flags_t, init_t = (torch.from_numpy(x).to(dev) for x in (sig_d, vsig, flags, init))
+    T = torch.zeros(D, D, D, dtype=torch.float32, device=dev)
+    out = torch.empty_like(flags_t)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def once(record=False):
+        T.zero_()
+        if record:
+            ev[0].record(stream)
+        ops.transparency_statistic(ro, rd, D, c, tile, vs, step, sig_t, flags_t, T)
+        if record:
+            ev[1].record(stream)
+        ops.prune_flags(T, vsig_t, init_t, 4, 0.5, 0.01, out)
+        w, n = ops.pack_occupancy(out)
+        if record:
+            ev[2].record(stream)
+        return n
+
+    for _ in range(warmup):
+        once()
+    torch.cuda.synchronize()
+    tot = st = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        n = once(True)
+        torch.cuda.synchronize()
+        tot += ev[0].elapsed_time(ev[2])
+        st += ev[0].elapsed_time(ev[1])
+    kept = int(n)
+    # CPU: the oracle's statistic (one thread) on a bounded sample of the rays
+    k = min(nrays, 20000)
+    idx = torch.linspace(0, nrays - 1, k, device=dev).long()
+    o_s, d_s = ro[idx].cpu().numpy(), rd[idx].cpu().numpy()
+    ref = np.zeros((D, D, D), np.float32)
+    t0 = time.perf_counter()
+    oracle.op_transparency_statistic(o_s, d_s, D, center_np, tile, vs, step, sig_d, flags, ref)
+    cpu_s = time.perf_counter() - t0
+    ms = tot / steps
+    return {"workload": PRUNE_WORKLOAD, "unit": "Mrays/s", "value": round(nrays / ms / 1e3, 2),
+            "ms_per_step": round(ms, 4), "statistic_ms": round(st / steps, 4), "rays": nrays,
+            "voxels_before": int((flags == 1).sum()), "voxels_after": kept,
+            "cpu_oracle": {"value": round(k / cpu_s / 1e6, 3), "unit": "Mrays/s", "cores": 1,
+                           "sample": f"{k} of the rays, transparency statistic only"},
+            "l2": "flushed before each step"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -614,7 +705,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-train", action="store_true")
     ap.add_argument("--no-large", action="store_true")
-    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular", "pipeline"],
+    ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular", "pipeline",
+                                              "pruning"],
                     default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
@@ -632,10 +724,11 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run in ("train", "batched", "large", "specular", "pipeline"):
+    if args.profile_run in ("train", "batched", "large", "specular", "pipeline", "pruning"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
         fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench,
-              "specular": specular_bench, "pipeline": reference_pipeline_bench}[args.profile_run]
+              "specular": specular_bench, "pipeline": reference_pipeline_bench,
+              "pruning": pruning_bench}[args.profile_run]
         res = fn(dev, args.steps, args.warmup, flush)
         print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
@@ -792,6 +885,7 @@ def main():
         large = large_scene_bench(dev, min(32, max(4, args.steps // 4)), 3, flush)
     specular = specular_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
     pipeline = reference_pipeline_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
+    pruning = pruning_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -822,6 +916,7 @@ def main():
             "large_scene": large,
             "specular_pass": specular,
             "reference_pipeline": pipeline,
+            "pruning": pruning,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

@@ -329,6 +329,43 @@ snisr_status snisr_op_rendering_diffuse_octree(
     int32_t soft_hit, float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Pruning after a training epoch, on the reference's dilated per-tile grids  */
+/* (D = N + 2 cells per side, [x][y][z] order, one cell of border).          */
+
+/* CUDA_EXT.transparency_statistic (training/src/Helper_kernel.cu:108-172,
+ * 272-303): rays_start/rays_dir [n][3]; tile_center [3] (device); voxels
+ * [D^3] density per unit length; nodes [D^3] int16 flags (samples only where
+ * 1); T_voxels [D^3] is max-combined in place with transmittance x trilinear
+ * weight at the 8 corners of every sample.  num_voxel is D (<= 1024).  Flagged cells
+ * on the grid border (where the reference asserts) contribute nothing. */
+snisr_status snisr_op_transparency_statistic(const float* rays_start_dev, const float* rays_dir_dev, int64_t n,
+                                             int32_t num_voxel, const float* tile_center_dev, float tile_size,
+                                             float voxel_size, float sample_step, const float* voxels_dev,
+                                             const int16_t* nodes_dev, float* T_voxels_dev, void* stream);
+
+/* CUDA_EXT.dilate_boundary (training/src/Helper_kernel.cu:174-270): in
+ * place on nodes_flag [D^3] int16 (num_voxel = D): -1 cells with a 1 cell in
+ * their 3^3 neighbourhood become 0.  Allocates nothing. */
+snisr_status snisr_op_dilate_boundary(int16_t* nodes_flag_dev, int32_t num_voxel, void* stream);
+
+/* The flag update of Tile.pruning (training/scripts/tile/tile.py:337-372)
+ * after the model query: nodes_flag [D^3] (D = num_voxel + 2) gets -1 on the
+ * border; inside, init_flags [N^3] (NULL = all 1) with -1 where
+ * exp(-max of voxel_sigma [N^3] over the voxel's block^3 block) > th or where
+ * the 3^3 maximum of T_voxels [D^3] <= T_th; then dilate_boundary.
+ * num_voxel must be a multiple of block. */
+snisr_status snisr_op_prune_flags(const float* T_voxels_dev, const float* voxel_sigma_dev,
+                                  const int16_t* init_flags_dev, int32_t num_voxel, int32_t block, float th,
+                                  float T_th, int16_t* nodes_flag_dev, void* stream);
+
+/* The 1 cells of nodes_flag's inner N^3 (N = num_voxel) as this library's
+ * occupancy words (snisr_scene_desc.occupancy layout: voxel v = (x*N + y)*N
+ * + z is bit v % 64 of word v / 64); words [ceil(N^3 / 64)], *count_dev =
+ * number of set bits (device int64). */
+snisr_status snisr_op_pack_occupancy(const int16_t* nodes_flag_dev, int32_t num_voxel, uint64_t* words_dev,
+                                     int64_t* count_dev, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Seeded synthetic scenes (input generation for tests and benchmarks).      */
 /* ------------------------------------------------------------------------ */
 typedef struct snisr_synth_params {

@@ -67,6 +67,11 @@ def lib() -> C.CDLL:
                                                           C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int,
                                                           P, P, P, C.c_int]),
             "oracle_eval_sh2": (None, [P, P, C.c_int64, P]),
+            "oracle_op_transparency_statistic": (None, [P, P, C.c_int64, C.c_int, P, C.c_float, C.c_float, C.c_float,
+                                                        P, P, P]),
+            "oracle_op_dilate_boundary": (None, [P, C.c_int]),
+            "oracle_op_prune_flags": (None, [P, P, P, C.c_int, C.c_int, C.c_float, C.c_float, P]),
+            "oracle_op_pack_occupancy": (C.c_int64, [P, C.c_int, P]),
             "oracle_op_assign_pixels": (None, [P, P, P, C.c_int64, P, P]),
             "oracle_op_inference_mlp": (None, [C.c_int, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P, P, P, P,
                                                C.c_int, C.c_int]),
@@ -330,3 +335,40 @@ def op_rendering_diffuse_octree(rays_d, visited, origin, data: dict, sample_step
                                              float(sample_step), D, float(trans_th), float(early_stop), int(soft_hit),
                                              _p(frame),
                                              _p(inverse_near), _p(net_idx), nthreads or threads())
+
+
+def op_transparency_statistic(rays_o, rays_d, D, center, tile_size, voxel_size, sample_step, voxels, nodes, T_voxels):
+    """CUDA_EXT.transparency_statistic; T_voxels [D,D,D] float32 updated in place."""
+    o = np.ascontiguousarray(rays_o, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(rays_d, np.float32).reshape(-1, 3)
+    c = np.ascontiguousarray(center, np.float32)
+    v = np.ascontiguousarray(voxels, np.float32)
+    nd = np.ascontiguousarray(nodes, np.int16)
+    assert T_voxels.dtype == np.float32 and T_voxels.flags.c_contiguous
+    lib().oracle_op_transparency_statistic(_p(o), _p(d), o.shape[0], int(D), _p(c), float(tile_size),
+                                           float(voxel_size), float(sample_step), _p(v), _p(nd), _p(T_voxels))
+
+
+def op_dilate_boundary(flags):
+    """CUDA_EXT.dilate_boundary on a contiguous int16 [D,D,D] array, in place."""
+    assert flags.dtype == np.int16 and flags.flags.c_contiguous
+    lib().oracle_op_dilate_boundary(_p(flags), flags.shape[0])
+
+
+def op_prune_flags(T_voxels, voxel_sigma, init_flags, N, block, th, T_th):
+    """Flag update of Tile.pruning; returns int16 [N+2]^3."""
+    out = np.empty((N + 2,) * 3, np.int16)
+    T = np.ascontiguousarray(T_voxels, np.float32)
+    s = np.ascontiguousarray(voxel_sigma, np.float32)
+    i = None if init_flags is None else np.ascontiguousarray(init_flags, np.int16)
+    lib().oracle_op_prune_flags(_p(T), _p(s), None if i is None else _p(i), int(N), int(block), float(th),
+                                float(T_th), _p(out))
+    return out
+
+
+def op_pack_occupancy(flags, N):
+    """(words uint64 [ceil(N^3/64)], count)."""
+    f = np.ascontiguousarray(flags, np.int16)
+    words = np.zeros((N ** 3 + 63) // 64, np.uint64)
+    n = lib().oracle_op_pack_occupancy(_p(f), int(N), _p(words))
+    return words, int(n)

@@ -822,6 +822,7 @@ static void uniform_v3(float* z, float* dist, float near_, float far_, int n) {
 void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const int16_t* flags, float cx, float cy,
                              float cz, float tile, int N, int ns, float* zv, float* dv) {
   const float half = tile * 0.5f, vs = tile / (float)N;
+  const float inv_vs = 1.0f / vs;  // float3 / float multiplies by the reciprocal (cutil_math.h:396-400)
   const float center[3] = {cx, cy, cz};
   float minc[3];
   for (int a = 0; a < 3; ++a) minc[a] = center[a] - half;
@@ -839,7 +840,7 @@ void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const 
     for (int a = 0; a < 3; ++a) {
       loc[a] = (o[a] + near_ * d[a]) - minc[a];
       loc[a] = std::min(std::max(loc[a], 0.0f), tile - 0.000001f);
-      cur[a] = std::min(std::max((int)(loc[a] / vs), 0), N - 1);
+      cur[a] = std::min(std::max((int)(loc[a] * inv_vs), 0), N - 1);
       st[a] = d[a] >= 0 ? 1 : -1;
       nb[a] = (float)(cur[a] + st[a]) * vs;
       if (st[a] < 0) nb[a] = nb[a] + vs;
@@ -868,7 +869,7 @@ void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const 
     }
     if (total == 0.0f) continue;
     for (int a = 0; a < 3; ++a) {
-      cur[a] = std::min(std::max((int)(loc[a] / vs), 0), N - 1);
+      cur[a] = std::min(std::max((int)(loc[a] * inv_vs), 0), N - 1);
       tmax[a] = safe_divide(nb[a] - loc[a], d[a]);
     }
     int count = 0, bsm = 4;
@@ -1356,6 +1357,8 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
   int last_group = -1;
   float last_exit = 0.0f;
   const float bs = V.tile_size / (float)kOctBlocks;
+  // float3 / float multiplies by the reciprocal (cutil_math.h:397-401)
+  const float inv_bs = 1.0f / bs, inv_vs = 1.0f / V.voxel_size;
   const int D = V.D, DD = D * D, D3 = D * D * D;
   for (int i = 0; i < K; ++i) {
     const int tile = vis[i];
@@ -1379,7 +1382,7 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
     int cb[3], st[3];
     float tmax[3], tdel[3];
     for (int a = 0; a < 3; ++a) {
-      cb[a] = (int)(ro[a] / bs);
+      cb[a] = (int)(ro[a] * inv_bs);
       st[a] = d[a] >= 0.0f ? 1 : -1;
       float nb = (float)(cb[a] + st[a]) * bs;
       if (st[a] < 0) nb = nb + bs;
@@ -1404,7 +1407,7 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
           int vl[3];
           for (int a = 0; a < 3; ++a) {
             pts[a] = ro[a] + z * d[a];
-            rel[a] = (pts[a] - dc[a]) / V.voxel_size;
+            rel[a] = (pts[a] - dc[a]) * inv_vs;
             vl[a] = (int)rel[a];
           }
           const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;
@@ -1483,5 +1486,146 @@ void oracle_op_rendering_diffuse_octree(const float* rays_d, const int32_t* visi
     octree_pixel(V, origin, rays_d + 3 * i, visited + i * K, K, th, early, soft_hit != 0, frame + 3 * i, inv_near + i,
                  net + i);
   });
+}
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Pruning after a training epoch, on the reference's dilated [x][y][z] grids
+// (D = N + 2 cells per side).
+//   transparency_statistic: transparency_statistic_cuda_kernel and
+//     transparency_interpolation (training/src/Helper_kernel.cu:30-172):
+//     per ray a march at sample_step from the tile entry; at samples whose
+//     cell ((pts - tile corner + voxel) * (1/voxel), truncated) is flagged 1
+//     the 8 corner cells of the trilinear cell ((pts - tile corner) *
+//     (1/voxel) + 0.5) get max(T_voxels, T * w); then T *= exp(-sigma *
+//     step) through alpha = 1 - exp(-sigma * step); stop when T < 1e-8.
+//     Rays run one after another (max-combining is order-free).
+//   dilate_boundary: dilate_boundary_cuda_kernel (Helper_kernel.cu:174-226).
+//   prune_flags: training/scripts/tile/tile.py:337-372 (with the density at
+//     the voxel centres given): block maximum, exp(-s) > th -> -1, 3^3 max
+//     filter of T_voxels <= T_th -> -1, then dilate_boundary.
+//   pack_occupancy: flags == 1 of the inner N^3 as 64-bit words.
+// Float operations round one at a time (no fused multiply-add); exp is
+// std::exp in single precision.
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void oracle_op_transparency_statistic(const float* ro, const float* rd, int64_t n, int D, const float* center,
+                                      float tile_size, float vs, float step, const float* sigma,
+                                      const int16_t* nodes, float* T_voxels) {
+  const int DD = D * D;
+  const float hs = tile_size / 2.0f;
+  const float h3[3] = {hs, hs, hs};
+  const float inv_vs = 1.0f / vs;
+  float tcorner[3], dcorner[3];
+  for (int a = 0; a < 3; ++a) {
+    tcorner[a] = center[a] - hs;
+    dcorner[a] = tcorner[a] - vs;
+  }
+  for (int64_t r = 0; r < n; ++r) {
+    const float* o = ro + 3 * r;
+    const float* d = rd + 3 * r;
+    const Bound b = ray_aabb(o, d, center, h3);
+    float z = b.lo, T = 1.0f;
+    while (z < b.hi) {
+      float pts[3];
+      int p[3];
+      for (int a = 0; a < 3; ++a) {
+        pts[a] = o[a] + z * d[a];
+        p[a] = (int)((pts[a] - dcorner[a]) * inv_vs);
+      }
+      if (p[0] < 0 || p[1] < 0 || p[2] < 0 || p[0] >= D || p[1] >= D || p[2] >= D ||
+          nodes[p[0] * DD + p[1] * D + p[2]] != 1) {
+        z = z + step;
+        continue;
+      }
+      float x[3];
+      int x0[3];
+      bool ok = true;
+      for (int a = 0; a < 3; ++a) {
+        const float f = (pts[a] - tcorner[a]) * inv_vs + 0.5f;
+        x0[a] = (int)f;
+        x[a] = f - (float)x0[a];
+        ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
+      }
+      if (!ok) {
+        z = z + step;
+        continue;
+      }
+      const float ux = 1.0f - x[0], uy = 1.0f - x[1], uz = 1.0f - x[2];
+      const float w[8] = {(ux * uy) * uz,     (ux * uy) * x[2],     (ux * x[1]) * uz,     (ux * x[1]) * x[2],
+                          (x[0] * uy) * uz,   (x[0] * uy) * x[2],   (x[0] * x[1]) * uz,   (x[0] * x[1]) * x[2]};
+      const int v000 = x0[0] * DD + x0[1] * D + x0[2];
+      const int off[8] = {0, 1, D, D + 1, DD, DD + 1, DD + D, DD + D + 1};
+      float s = 0.0f;
+      for (int k = 0; k < 8; ++k) {
+        const float t = T * w[k];
+        float& slot = T_voxels[v000 + off[k]];
+        if (t > slot) slot = t;
+        s = k == 0 ? sigma[v000] * w[0] : s + sigma[v000 + off[k]] * w[k];
+      }
+      const float alpha = 1.0f - std::exp((-1.0f * s) * step);
+      T = T * (1.0f - alpha);
+      if (T < 0.00000001f) break;
+      z = z + step;
+    }
+  }
+}
+
+void oracle_op_dilate_boundary(int16_t* flags, int D) {
+  const int64_t total = (int64_t)D * D * D;
+  std::vector<int16_t> out(flags, flags + total);
+  for (int64_t i = 0; i < total; ++i) {
+    if (flags[i] != -1) continue;
+    const int x = (int)(i / ((int64_t)D * D)), y = (int)(i / D % D), z = (int)(i % D);
+    for (int a = std::max(x - 1, 0); a <= std::min(x + 1, D - 1); ++a)
+      for (int b = std::max(y - 1, 0); b <= std::min(y + 1, D - 1); ++b)
+        for (int c = std::max(z - 1, 0); c <= std::min(z + 1, D - 1); ++c)
+          if (flags[((int64_t)a * D + b) * D + c] == 1) out[i] = 0;
+  }
+  std::memcpy(flags, out.data(), sizeof(int16_t) * total);
+}
+
+void oracle_op_prune_flags(const float* T_voxels, const float* voxel_sigma, const int16_t* init_flags, int N,
+                           int block, float th, float T_th, int16_t* flags) {
+  const int D = N + 2;
+  for (int x = 0; x < D; ++x)
+    for (int y = 0; y < D; ++y)
+      for (int z = 0; z < D; ++z) {
+        int16_t& f = flags[((int64_t)x * D + y) * D + z];
+        if (x == 0 || y == 0 || z == 0 || x == D - 1 || y == D - 1 || z == D - 1) {
+          f = -1;
+          continue;
+        }
+        const int vx = x - 1, vy = y - 1, vz = z - 1;
+        f = init_flags ? init_flags[((int64_t)vx * N + vy) * N + vz] : (int16_t)1;
+        float smax = voxel_sigma[((int64_t)(vx / block * block) * N + vy / block * block) * N + vz / block * block];
+        for (int a = vx / block * block; a < vx / block * block + block; ++a)
+          for (int b = vy / block * block; b < vy / block * block + block; ++b)
+            for (int c = vz / block * block; c < vz / block * block + block; ++c)
+              smax = std::max(smax, voxel_sigma[((int64_t)a * N + b) * N + c]);
+        if (std::exp(-smax) > th) f = -1;
+        float tmax = T_voxels[((int64_t)(x - 1) * D + (y - 1)) * D + (z - 1)];
+        for (int a = x - 1; a <= x + 1; ++a)
+          for (int b = y - 1; b <= y + 1; ++b)
+            for (int c = z - 1; c <= z + 1; ++c) tmax = std::max(tmax, T_voxels[((int64_t)a * D + b) * D + c]);
+        if (tmax <= T_th) f = -1;
+      }
+  oracle_op_dilate_boundary(flags, D);
+}
+
+int64_t oracle_op_pack_occupancy(const int16_t* flags, int N, uint64_t* words) {
+  const int D = N + 2;
+  const int64_t nvox = (int64_t)N * N * N;
+  std::memset(words, 0, sizeof(uint64_t) * ((nvox + 63) / 64));
+  int64_t count = 0;
+  for (int64_t v = 0; v < nvox; ++v) {
+    const int x = (int)(v / ((int64_t)N * N)), y = (int)(v / N % N), z = (int)(v % N);
+    if (flags[((int64_t)(x + 1) * D + (y + 1)) * D + (z + 1)] == 1) {
+      words[v >> 6] |= 1ull << (v & 63);
+      ++count;
+    }
+  }
+  return count;
 }
 }  // extern "C"

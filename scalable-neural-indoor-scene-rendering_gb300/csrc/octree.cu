@@ -43,6 +43,8 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
                                       bool soft_hit, float* frame, float* inv_near, int16_t* net) {
   const int DD = D * D, D3 = D * D * D;
   const float bs = fdiv(tile_size, (float)kOctBlocks);
+  // float3 / float multiplies by the reciprocal (cutil_math.h:397-401)
+  const float inv_bs = fdiv(1.0f, bs), inv_vs = fdiv(1.0f, voxel_size);
   const __half early_h = __float2half(early);
   const __half one = __float2half(1.0f);
   const float o[3] = {__ldg(origin), __ldg(origin + 1), __ldg(origin + 2)};
@@ -74,7 +76,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
       for (int a = 0; a < 3; ++a) {
         ro[a] = fsub(fadd(o[a], fmul(b.x, d[a])), fsub(c[a], hs));
         ro[a] = fminf(fmaxf(ro[a], 0.0f), fsub(tile_size, 0.00001f));
-        cb[a] = (int)fdiv(ro[a], bs);
+        cb[a] = (int)fmul(ro[a], inv_bs);
         st[a] = d[a] >= 0.0f ? 1 : -1;
         float nb = fmul((float)(cb[a] + st[a]), bs);
         if (st[a] < 0) nb = fadd(nb, bs);
@@ -100,7 +102,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
             int vl[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-              rel[a] = fdiv(fsub(fadd(ro[a], fmul(z, d[a])), dc[a]), voxel_size);
+              rel[a] = fmul(fsub(fadd(ro[a], fmul(z, d[a])), dc[a]), inv_vs);
               vl[a] = (int)rel[a];
             }
             const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;

@@ -104,6 +104,7 @@ __global__ void op_sample_sparse_kernel(const float* __restrict__ ro, const floa
                                         int N, int ns, float* zv, float* dv) {
   const float half = fmul(tile, 0.5f);
   const float vs = fdiv(tile, (float)N);
+  const float inv_vs = fdiv(1.0f, vs);  // float3 / float is a multiply by the reciprocal (cutil_math.h:396-400)
   const float center[3] = {cx, cy, cz};
   float minc[3];
   for (int a = 0; a < 3; ++a) minc[a] = fsub(center[a], half);
@@ -121,7 +122,7 @@ __global__ void op_sample_sparse_kernel(const float* __restrict__ ro, const floa
     for (int a = 0; a < 3; ++a) {
       loc[a] = fsub(fadd(o[a], fmul(near, d[a])), minc[a]);
       loc[a] = fminf(fmaxf(loc[a], 0.0f), fsub(tile, 0.000001f));
-      cur[a] = min(max((int)fdiv(loc[a], vs), 0), N - 1);
+      cur[a] = min(max((int)fmul(loc[a], inv_vs), 0), N - 1);
       st[a] = d[a] >= 0 ? 1 : -1;
       nb[a] = fmul((float)(cur[a] + st[a]), vs);
       if (st[a] < 0) nb[a] = fadd(nb[a], vs);
@@ -148,7 +149,7 @@ __global__ void op_sample_sparse_kernel(const float* __restrict__ ro, const floa
     }
     if (total == 0.0f) continue;
     for (int a = 0; a < 3; ++a) {
-      cur[a] = min(max((int)fdiv(loc[a], vs), 0), N - 1);
+      cur[a] = min(max((int)fmul(loc[a], inv_vs), 0), N - 1);
       tmax[a] = safe_div(fsub(nb[a], loc[a]), d[a]);
     }
     int count = 0;

@@ -135,6 +135,11 @@ _SIGNATURES = {
     "snisr_op_rendering_diffuse_octree": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32,
                                                     C.c_float, C.c_float, C.c_float, C.c_int32, C.c_float, C.c_float,
                                                     C.c_int32, P, P, P, P]),
+    "snisr_op_transparency_statistic": (C.c_int, [P, P, C.c_int64, C.c_int32, P, C.c_float, C.c_float, C.c_float, P,
+                                                  P, P, P]),
+    "snisr_op_dilate_boundary": (C.c_int, [P, C.c_int32, P]),
+    "snisr_op_prune_flags": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_float, C.c_float, P, P]),
+    "snisr_op_pack_occupancy": (C.c_int, [P, C.c_int32, P, P, P]),
     "snisr_op_inference_mlp": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, P, C.c_int32, P, P, P, P, P, P, P,
                                          P, P, P]),
     "snisr_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(P), C.POINTER(SceneDesc)]),

@@ -247,3 +247,76 @@ def rendering_diffuse_octree_fp16(rays_d, visitedTiles, origin, groupMap, data_v
         float(sample_step), int(num_voxel), float(trans_th), float(early_stop), int(bool(soft_hit)),
         frame_diffuse.data_ptr(),
         inverse_near.data_ptr(), netIdxs.data_ptr(), _stream()))
+
+
+# ---------------------------------------------------------------------------
+# Pruning after a training epoch (CUDA_EXT helpers and the flag update of
+# Tile.pruning), on dilated [x][y][z] grids of D = N + 2 cells per side
+# ---------------------------------------------------------------------------
+def transparency_statistic(rays_start, rays_dir, num_voxel, tile_center, tile_size, voxel_size, sample_step,
+                           voxels, nodes, T_voxels):
+    """training/src/Helper.cpp:29-56 / Helper_kernel.cu:108-172: T_voxels
+    [D,D,D] max-combined in place with transmittance x trilinear weight at
+    the samples of every ray in flagged (== 1) cells; num_voxel = D."""
+    import torch
+    _check(rays_start, "rays_start", torch.float32, 2)
+    _check(rays_dir, "rays_dir", torch.float32, 2)
+    _check(tile_center, "tile_center", torch.float32, 1)
+    _check(voxels, "voxels", torch.float32, 3)
+    _check(nodes, "nodes", torch.int16, 3)
+    _check(T_voxels, "T_voxels", torch.float32, 3)
+    D = int(num_voxel)
+    for t, n in ((voxels, "voxels"), (nodes, "nodes"), (T_voxels, "T_voxels")):
+        if tuple(t.shape) != (D, D, D):
+            raise RuntimeError(f"transparency_statistic: {n} must be {D}^3")
+    if rays_start.shape != rays_dir.shape or rays_start.shape[1] != 3:
+        raise RuntimeError("transparency_statistic: rays must be [B,3]")
+    _lib.check(_lib.lib().snisr_op_transparency_statistic(
+        rays_start.data_ptr(), rays_dir.data_ptr(), rays_start.shape[0], D, tile_center.data_ptr(),
+        float(tile_size), float(voxel_size), float(sample_step), voxels.data_ptr(), nodes.data_ptr(),
+        T_voxels.data_ptr(), _stream()))
+
+
+def dilate_boundary(nodes_flag, num_voxel):
+    """training/src/Helper.cpp:6-13 / Helper_kernel.cu:174-270, in place."""
+    import torch
+    _check(nodes_flag, "nodes_flag", torch.int16, 3)
+    if nodes_flag.numel() != int(num_voxel) ** 3:
+        raise RuntimeError("dilate_boundary: nodes_flag must hold num_voxel^3 entries")
+    _lib.check(_lib.lib().snisr_op_dilate_boundary(nodes_flag.data_ptr(), int(num_voxel), _stream()))
+
+
+def prune_flags(T_voxels, voxel_sigma, init_flags, block, th, T_th, nodes_flag):
+    """The flag update of Tile.pruning (training/scripts/tile/tile.py:337-372)
+    after its model query: T_voxels [D,D,D], voxel_sigma [N,N,N] (density at
+    the voxel centres), init_flags [N,N,N] int16 or None (all 1); nodes_flag
+    [D,D,D] int16 is overwritten (D = N + 2)."""
+    import torch
+    _check(T_voxels, "T_voxels", torch.float32, 3)
+    _check(voxel_sigma, "voxel_sigma", torch.float32, 3)
+    _check(nodes_flag, "nodes_flag", torch.int16, 3)
+    N = voxel_sigma.shape[0]
+    if tuple(voxel_sigma.shape) != (N, N, N) or tuple(T_voxels.shape) != (N + 2,) * 3 or \
+            tuple(nodes_flag.shape) != (N + 2,) * 3:
+        raise RuntimeError("prune_flags: shapes must be N^3 (voxel_sigma, init_flags) and (N+2)^3")
+    ip = None
+    if init_flags is not None:
+        _check(init_flags, "init_flags", torch.int16, 3)
+        if tuple(init_flags.shape) != (N, N, N):
+            raise RuntimeError("prune_flags: init_flags must be N^3")
+        ip = init_flags.data_ptr()
+    _lib.check(_lib.lib().snisr_op_prune_flags(T_voxels.data_ptr(), voxel_sigma.data_ptr(), ip, N, int(block),
+                                               float(th), float(T_th), nodes_flag.data_ptr(), _stream()))
+
+
+def pack_occupancy(nodes_flag):
+    """Occupancy words (int64 view of this library's uint64 layout) and the
+    number of occupied voxels (a 0-dim device tensor) of a [N+2]^3 flag grid."""
+    import torch
+    _check(nodes_flag, "nodes_flag", torch.int16, 3)
+    N = nodes_flag.shape[0] - 2
+    words = torch.empty((N ** 3 + 63) // 64, dtype=torch.int64, device=nodes_flag.device)
+    count = torch.empty((), dtype=torch.int64, device=nodes_flag.device)
+    _lib.check(_lib.lib().snisr_op_pack_occupancy(nodes_flag.data_ptr(), N, words.data_ptr(), count.data_ptr(),
+                                                  _stream()))
+    return words, count
