@@ -329,6 +329,73 @@ snisr_status snisr_op_rendering_diffuse_octree(
     int32_t soft_hit, float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Training-ray preparation of one tile from posed views (get_trainData_v3,  */
+/* training/src/cuda_func.cu:1341-1686).  All buffers are device memory.     */
+
+/* computing_rays_kernel (cuda_func.cu:15-50, get_rays in
+ * training/src/include/cuda_utils.h:143-155): K [9] row-major intrinsics,
+ * c2w [12] row-major 3x4; pixel (x, y) -> rays_d = R ((x - K[2]) / K[0],
+ * (y - K[5]) / K[4], 1) (not normalised), rays_o = t; [height*width][3]. */
+snisr_status snisr_op_train_rays(const float* K_dev, const float* c2w_dev, int32_t height, int32_t width,
+                                 float* rays_o_dev, float* rays_d_dev, void* stream);
+
+/* tracingTile_kernel (cuda_func.cu:52-128): visited [n][K] sparse tile ids
+ * (-1 padded) of the tile DDA of the normalised direction from the origin,
+ * or from its entry into the scene box, clamped into the scene.  The
+ * normalisation uses a correctly rounded 1/sqrt (the reference: rsqrtf). */
+snisr_status snisr_op_train_tracing_tiles(const float* rays_o_dev, const float* rays_d_dev, int64_t n,
+                                          const int32_t* index_map_dev, const int32_t tile_shape[3],
+                                          const float scene_min_corner[3], float tile_size, int32_t K,
+                                          int32_t* visited_dev, void* stream);
+
+/* ray_doubleHit_inTile_kernel (cuda_func.cu:284-444) on the scene's proxy
+ * BVH: double_hits [n][K][2] = the two nearest hits (t along rays_d, with
+ * multiplicity) whose points lie in visited tile j (+-1e-5), -1 where
+ * missing.  The reference walks per-block face lists; here the BVH is
+ * clipped to the tile box (each triangle is counted once). */
+snisr_status snisr_scene_double_hits(snisr_scene* scene, const float* rays_o_dev, const float* rays_d_dev,
+                                     const int32_t* visited_dev, int64_t n, int32_t K, float* double_hits_dev,
+                                     void* stream);
+
+/* get_trainData_kernel (cuda_func.cu:587-663): valid [n] = 1 where the
+ * training tile is visited at or before the first tile with a hit;
+ * bgdepth [n] = the next hit then (-1 if none; -1 where not valid, where the
+ * reference leaves the previous view's value). */
+snisr_status snisr_op_train_bgdepth(int32_t train_tile, const int32_t* visited_dev, const float* double_hits_dev,
+                                    int64_t n, int32_t K, float* bgdepth_dev, int32_t* valid_dev, void* stream);
+
+/* gen_diffuse_in_tile_kernel (cuda_func.cu:1197-1339): for pixels with a
+ * hit in the training tile, diffuse [H*W][3] = the (1 - cos)^2-weighted mean
+ * of the bilinear colours of the hit point in the views that see it (depth
+ * test 0.01); bgdepth set to -1 where no view sees the background point.
+ * origins [num_images][3], images [num_images][H*W][3] float, depths
+ * [num_images][H*W], proj [num_images][12] (compute_project_matrix). */
+snisr_status snisr_op_gen_diffuse(const float* origins_dev, int32_t train_tile, const float* rays_o_dev,
+                                  const float* rays_d_dev, const float* double_hits_dev, const int32_t* visited_dev,
+                                  const float* images_dev, const float* depths_dev, const float* proj_dev, int32_t K,
+                                  int32_t num_images, int32_t height, int32_t width, float* diffuse_dev,
+                                  float* bgdepth_dev, void* stream);
+
+/* CUDA_EXT.Sample_bg (training/src/Sample_kernel.cu:481-542): z_vals
+ * [n][nsamples] uniform over bg +- range / 2, moved behind the tile's exit
+ * when that interval starts inside the tile; rows with bg == -1 untouched. */
+snisr_status snisr_op_sample_bg(const float* rays_o_dev, const float* rays_d_dev, const float* bg_zval_dev,
+                                int64_t n, int32_t nsamples, float sample_range, const float* tile_center_dev,
+                                float tile_size, float* z_vals_dev, void* stream);
+
+/* Patch rows of get_trainData_v3 (cuda_func.cu:1545-1600): odd patch_size P,
+ * patch centres (half + iP, half + jP) below (H - P, W - P); patches with a
+ * valid pixel are written in order as P*P rows of 14 floats (rays_o, rays_d,
+ * bgdepth, gt_rgb, diffuse, valid).  snisr_op_patch_capacity gives the
+ * number of patch positions C (or -1): rows holds C*P*P*14 floats, scratch
+ * 2*C int32; *num_patches_dev (int64) receives the count written. */
+int64_t snisr_op_patch_capacity(int32_t height, int32_t width, int32_t patch_size);
+snisr_status snisr_op_patch_rows(const int32_t* valid_dev, int32_t height, int32_t width, int32_t patch_size,
+                                 const float* rays_o_dev, const float* rays_d_dev, const float* bgdepth_dev,
+                                 const float* gt_rgb_dev, const float* diffuse_dev, int32_t* scratch_dev,
+                                 float* rows_dev, int64_t* num_patches_dev, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Pruning after a training epoch, on the reference's dilated per-tile grids  */
 /* (D = N + 2 cells per side, [x][y][z] order, one cell of border).          */
 

@@ -67,6 +67,15 @@ def lib() -> C.CDLL:
                                                           C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int,
                                                           P, P, P, C.c_int]),
             "oracle_eval_sh2": (None, [P, P, C.c_int64, P]),
+            "oracle_project_matrix": (None, [P, P, P]),
+            "oracle_train_rays": (None, [P, P, C.c_int, C.c_int, P, P]),
+            "oracle_train_tracing": (None, [P, P, C.c_int64, P, P, P, C.c_float, C.c_int, P]),
+            "oracle_double_hits": (None, [P, P, P, P, C.c_int64, C.c_int, P, C.c_int]),
+            "oracle_train_bgdepth": (None, [C.c_int, P, P, C.c_int64, C.c_int, P, P]),
+            "oracle_gen_diffuse": (None, [P, C.c_int, P, P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P,
+                                          C.c_int]),
+            "oracle_sample_bg": (None, [P, P, P, C.c_int64, C.c_int, C.c_float, P, C.c_float, P]),
+            "oracle_patch_rows": (C.c_int64, [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P]),
             "oracle_op_transparency_statistic": (None, [P, P, C.c_int64, C.c_int, P, C.c_float, C.c_float, C.c_float,
                                                         P, P, P]),
             "oracle_op_dilate_boundary": (None, [P, C.c_int]),
@@ -132,6 +141,16 @@ class OracleScene:
         tri = np.zeros(n, np.int32)
         lib().oracle_proxy(self._h, _p(o), _p(d), n, _p(ts), _p(th), _p(tri), nthreads or threads())
         return ts, th, tri
+
+    def double_hits(self, ro, rd, visited, nthreads: int | None = None):
+        """[n, K, 2] two nearest proxy hits per (ray, visited tile), -1 where missing."""
+        ro = np.ascontiguousarray(ro, np.float32).reshape(-1, 3)
+        rd = np.ascontiguousarray(rd, np.float32).reshape(-1, 3)
+        vis = np.ascontiguousarray(visited, np.int32)
+        n, K = vis.shape
+        out = np.zeros((n, K, 2), np.float32)
+        lib().oracle_double_hits(self._h, _p(ro), _p(rd), _p(vis), n, K, _p(out), nthreads or threads())
+        return out
 
     def trace(self, o, d, t_start, K: int, nthreads: int | None = None):
         n = o.shape[0]
@@ -372,3 +391,69 @@ def op_pack_occupancy(flags, N):
     words = np.zeros((N ** 3 + 63) // 64, np.uint64)
     n = lib().oracle_op_pack_occupancy(_p(f), int(N), _p(words))
     return words, int(n)
+
+
+# --- training-ray preparation ---------------------------------------------
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+def project_matrix(K, c2w):
+    m = np.zeros(12, np.float32)
+    lib().oracle_project_matrix(_p(_f32(K, 9)), _p(_f32(c2w, 12)), _p(m))
+    return m
+
+
+def train_rays(K, c2w, H, W):
+    ro = np.zeros((H * W, 3), np.float32)
+    rd = np.zeros((H * W, 3), np.float32)
+    lib().oracle_train_rays(_p(_f32(K, 9)), _p(_f32(c2w, 12)), H, W, _p(ro), _p(rd))
+    return ro, rd
+
+
+def train_tracing(ro, rd, imap, shape, smin, tile, K):
+    ro, rd = _f32(ro, (-1, 3)), _f32(rd, (-1, 3))
+    n = ro.shape[0]
+    vis = np.zeros((n, K), np.int32)
+    lib().oracle_train_tracing(_p(ro), _p(rd), n, _p(np.ascontiguousarray(imap, np.int32).reshape(-1)),
+                               _p(np.ascontiguousarray(shape, np.int32)), _p(_f32(smin)), float(tile), K, _p(vis))
+    return vis
+
+
+def train_bgdepth(train_tile, visited, hits):
+    vis = np.ascontiguousarray(visited, np.int32)
+    n, K = vis.shape
+    bg = np.zeros(n, np.float32)
+    valid = np.zeros(n, np.int32)
+    lib().oracle_train_bgdepth(int(train_tile), _p(vis), _p(_f32(hits)), n, K, _p(bg), _p(valid))
+    return bg, valid
+
+
+def gen_diffuse(origins, train_tile, ro, rd, hits, visited, images, depths, ms, H, W, bgdepth):
+    """Returns diffuse [H*W,3]; bgdepth (float32 [H*W]) is updated in place."""
+    vis = np.ascontiguousarray(visited, np.int32)
+    K = vis.shape[1]
+    nimg = int(np.asarray(ms).reshape(-1, 12).shape[0])
+    out = np.zeros((H * W, 3), np.float32)
+    assert bgdepth.dtype == np.float32 and bgdepth.flags.c_contiguous
+    lib().oracle_gen_diffuse(_p(_f32(origins)), int(train_tile), _p(_f32(ro)), _p(_f32(rd)), _p(_f32(hits)), _p(vis),
+                             _p(_f32(images)), _p(_f32(depths)), _p(_f32(ms)), K, nimg, H, W, _p(out), _p(bgdepth),
+                             threads())
+    return out
+
+
+def sample_bg(ro, rd, bgz, ns, sample_range, center, tile, z):
+    ro, rd = _f32(ro, (-1, 3)), _f32(rd, (-1, 3))
+    assert z.dtype == np.float32 and z.flags.c_contiguous
+    lib().oracle_sample_bg(_p(ro), _p(rd), _p(_f32(bgz)), ro.shape[0], int(ns), float(sample_range),
+                           _p(_f32(center)), float(tile), _p(z))
+
+
+def patch_rows(valid, H, W, P, ro, rd, bgdepth, gt, diffuse):
+    half = P // 2
+    cnt = lambda L: (L - P - half + P - 1) // P if L - P > half else 0
+    rows = np.zeros((cnt(H) * cnt(W) * P * P, 14), np.float32)
+    n = lib().oracle_patch_rows(_p(np.ascontiguousarray(valid, np.int32)), H, W, P, _p(_f32(ro)), _p(_f32(rd)),
+                                _p(_f32(bgdepth)), _p(_f32(gt)), _p(_f32(diffuse)), _p(rows))
+    return rows[:n * P * P].reshape(n, P * P, 14)

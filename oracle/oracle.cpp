@@ -1629,3 +1629,313 @@ int64_t oracle_op_pack_occupancy(const int16_t* flags, int N, uint64_t* words) {
   return count;
 }
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Training-ray preparation (get_trainData_v3, training/src/cuda_func.cu:
+// 1341-1686): get_rays (training/src/include/cuda_utils.h:143-155),
+// tracingTile_kernel (cuda_func.cu:52-128), ray_doubleHit_inTile_kernel
+// (:284-444) as the two nearest hits with the same two-sided triangle test
+// as the proxy hit and the hit point inside the tile +- 1e-5, get_trainData_
+// kernel (:587-663), gen_diffuse_in_tile_kernel (:1197-1339), Sample_bg
+// (training/src/Sample_kernel.cu:481-542), the patch loop (:1545-1600) and
+// compute_project_matrix (cuda_utils.h:37-58).  Normalisation uses
+// 1 / sqrt in double rounded once to float (the reference: rsqrtf).
+// ---------------------------------------------------------------------------
+namespace {
+inline float rinv_sqrt(float x) { return (float)(1.0 / std::sqrt((double)x)); }
+inline void normalize3(const float v[3], float out[3]) {
+  const float inv = rinv_sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  for (int a = 0; a < 3; ++a) out[a] = v[a] * inv;
+}
+const float kThreshPrep = 0.00001f;
+inline int patch_count(int L, int P) {
+  const int half = P / 2;
+  return L - P > half ? (L - P - half + P - 1) / P : 0;
+}
+}  // namespace
+
+extern "C" {
+
+void oracle_project_matrix(const float* K, const float* C, float* m) {
+  const float fx = K[0], fy = K[4], cx = K[2], cy = K[5];
+  const float t1 = -1.0f * ((C[0] * C[3] + C[4] * C[7]) + C[8] * C[11]);
+  const float t2 = -1.0f * ((C[1] * C[3] + C[5] * C[7]) + C[9] * C[11]);
+  const float t3 = -1.0f * ((C[2] * C[3] + C[6] * C[7]) + C[10] * C[11]);
+  m[0] = fx * C[0] + cx * C[2];
+  m[1] = fx * C[4] + cx * C[6];
+  m[2] = fx * C[8] + cx * C[10];
+  m[3] = fx * t1 + cx * t3;
+  m[4] = fy * C[1] + cy * C[2];
+  m[5] = fy * C[5] + cy * C[6];
+  m[6] = fy * C[9] + cy * C[10];
+  m[7] = fy * t2 + cy * t3;
+  m[8] = C[2];
+  m[9] = C[6];
+  m[10] = C[10];
+  m[11] = t3;
+}
+
+void oracle_train_rays(const float* K, const float* C, int H, int W, float* ro, float* rd) {
+  for (int64_t i = 0; i < (int64_t)H * W; ++i) {
+    const int y = (int)(i / W), x = (int)(i % W);
+    const float u = ((float)x - K[2]) / K[0], v = ((float)y - K[5]) / K[4];
+    for (int a = 0; a < 3; ++a) {
+      rd[3 * i + a] = (C[4 * a] * u + C[4 * a + 1] * v) + C[4 * a + 2];
+      ro[3 * i + a] = C[4 * a + 3];
+    }
+  }
+}
+
+void oracle_train_tracing(const float* ro, const float* rd, int64_t n, const int32_t* imap, const int32_t* shape,
+                          const float* smin, float tile, int K, int32_t* visited) {
+  float size[3], c[3], h[3];
+  for (int a = 0; a < 3; ++a) {
+    size[a] = (float)shape[a] * tile;
+    h[a] = size[a] * 0.5f;
+    c[a] = smin[a] + h[a];
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t* vis = visited + i * K;
+    for (int j = 0; j < K; ++j) vis[j] = -1;
+    const float* o = ro + 3 * i;
+    float d[3], p[3];
+    normalize3(rd + 3 * i, d);
+    for (int a = 0; a < 3; ++a) p[a] = o[a] - smin[a];
+    if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
+      const Bound b = ray_aabb(o, d, c, h);
+      for (int a = 0; a < 3; ++a) p[a] = p[a] + b.lo * d[a];
+    }
+    for (int a = 0; a < 3; ++a) p[a] = std::max(0.0f, std::min(p[a], size[a] - 0.000001f));
+    // voxel_traversal with the start cell clamped into the grid (p / tile can
+    // round up to the grid size at the far face)
+    int cur[3], st[3];
+    float tmax[3], tdel[3];
+    for (int a = 0; a < 3; ++a) {
+      cur[a] = std::min(std::max((int)std::floor(p[a] / tile), 0), shape[a] - 1);
+      st[a] = d[a] >= 0 ? 1 : -1;
+      float nb = (float)(cur[a] + st[a]) * tile;
+      if (st[a] < 0) nb = nb + tile;
+      tmax[a] = d[a] != 0 ? (nb - p[a]) / d[a] : kInf;
+      tdel[a] = d[a] != 0 ? (tile / d[a]) * (float)st[a] : kInf;
+    }
+    int idx = 0;
+    int id = imap[((int64_t)cur[0] * shape[1] + cur[1]) * shape[2] + cur[2]];
+    if (id != -1) vis[idx++] = id;
+    while (idx < K) {
+      const int a = dda_axis(tmax);
+      cur[a] += st[a];
+      tmax[a] = tmax[a] + tdel[a];
+      if (cur[a] < 0 || cur[a] >= shape[a]) break;
+      id = imap[((int64_t)cur[0] * shape[1] + cur[1]) * shape[2] + cur[2]];
+      if (id != -1) vis[idx++] = id;
+    }
+  }
+}
+
+void oracle_double_hits(const oracle_scene* os, const float* ro, const float* rd, const int32_t* visited, int64_t n,
+                        int K, float* hits, int threads) {
+  const Scene& s = *reinterpret_cast<const Scene*>(os);
+  const snisr_scene_desc* D = s.d;
+  const float hs = s.tile / 2.0f;
+  // per tile: triangles whose bounding box meets the tile box +- 2e-5 (a
+  // conservative prefilter; the hit test below decides)
+  std::vector<std::vector<int64_t>> cand((size_t)s.NT);
+  for (int64_t t = 0; t < D->num_triangles; ++t) {
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = hi[a] = D->mesh_vertices[3 * (int64_t)D->mesh_faces[3 * t] + a];
+      for (int k = 1; k < 3; ++k) {
+        const float v = D->mesh_vertices[3 * (int64_t)D->mesh_faces[3 * t + k] + a];
+        lo[a] = std::min(lo[a], v);
+        hi[a] = std::max(hi[a], v);
+      }
+    }
+    for (int tile = 0; tile < s.NT; ++tile) {
+      bool meet = true;
+      for (int a = 0; a < 3; ++a) {
+        const float c = s.centers[(size_t)tile * 3 + a];
+        meet = meet && hi[a] >= (c - hs) - 2.0f * kThreshPrep && lo[a] <= (c + hs) + 2.0f * kThreshPrep;
+      }
+      if (meet) cand[(size_t)tile].push_back(t);
+    }
+  }
+  parallel_for(n * K, threads, [&](int64_t i) {
+    float* out = hits + 2 * i;
+    out[0] = out[1] = -1.0f;
+    const int tile = visited[i];
+    if (tile < 0 || tile >= s.NT || D->num_triangles == 0) return;
+    const int64_t r = i / K;
+    const float* o = ro + 3 * r;
+    const float* d = rd + 3 * r;
+    const float* c = s.centers.data() + (size_t)tile * 3;
+    float near1 = kInf, near2 = kInf;
+    for (int64_t t : cand[(size_t)tile]) {
+      const float* A = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t];
+      const float* B = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 1];
+      const float* Cc = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 2];
+      float th;
+      if (!tri_hit(o, d, A, B, Cc, th) || !(th < near2)) continue;
+      bool in = true;
+      for (int a = 0; a < 3; ++a) in = in && std::fabs((o[a] + th * d[a]) - c[a]) - hs <= kThreshPrep;
+      if (!in) continue;
+      if (th < near1) {
+        near2 = near1;
+        near1 = th;
+      } else {
+        near2 = th;
+      }
+    }
+    if (near1 != kInf) {
+      out[0] = near1;
+      if (near2 != kInf) out[1] = near2;
+    }
+  });
+}
+
+void oracle_train_bgdepth(int train_tile, const int32_t* visited, const float* hits, int64_t n, int K,
+                          float* bgdepth, int32_t* valid) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* h = hits + 2 * i * K;
+    const int32_t* vis = visited + i * K;
+    float first = -1.0f, second = -1.0f;
+    int ff = -1;
+    for (int j = 0; j < K; ++j)
+      if (h[2 * j] != -1.0f) {
+        if (ff == -1) {
+          ff = j;
+          first = h[2 * j];
+        } else {
+          second = h[2 * j];
+          break;
+        }
+      }
+    bgdepth[i] = -1.0f;
+    valid[i] = 0;
+    for (int j = 0; j <= ff; ++j)
+      if (vis[j] == train_tile) {
+        bgdepth[i] = j == ff ? second : first;
+        valid[i] = 1;
+        break;
+      }
+  }
+}
+
+void oracle_gen_diffuse(const float* origins, int train_tile, const float* ro, const float* rd, const float* hits,
+                        const int32_t* visited, const float* images, const float* depths, const float* ms, int K,
+                        int nimg, int H, int W, float* diffuse, float* bgdepth, int threads) {
+  const int64_t npix = (int64_t)H * W;
+  auto project = [&](const float* m, const float p[3], float& z, float& px, float& py) {
+    const float x = ((m[0] * p[0] + m[1] * p[1]) + m[2] * p[2]) + m[3];
+    const float y = ((m[4] * p[0] + m[5] * p[1]) + m[6] * p[2]) + m[7];
+    z = ((m[8] * p[0] + m[9] * p[1]) + m[10] * p[2]) + m[11];
+    if (z <= 0.0f) return false;
+    px = x / z;
+    py = y / z;
+    return !(px < 0.0f || px >= (float)(W - 1) || py < 0.0f || py >= (float)(H - 1));
+  };
+  parallel_for(npix, threads, [&](int64_t i) {
+    const float* h = hits + 2 * i * K;
+    const int32_t* vis = visited + i * K;
+    const float* o = ro + 3 * i;
+    const float* d = rd + 3 * i;
+    diffuse[3 * i] = diffuse[3 * i + 1] = diffuse[3 * i + 2] = 0.0f;
+    float first = -1.0f;
+    for (int j = 0; j < K; ++j)
+      if (h[2 * j] != -1.0f && vis[j] == train_tile) {
+        first = h[2 * j];
+        break;
+      }
+    if (first == -1.0f) return;
+    if (bgdepth[i] != -1.0f) {
+      float p[3];
+      for (int a = 0; a < 3; ++a) p[a] = o[a] + bgdepth[i] * d[a];
+      bool visible = false;
+      for (int j = 0; j < nimg && !visible; ++j) {
+        float z, px, py;
+        if (!project(ms + 12 * j, p, z, px, py)) continue;
+        const float dep = depths[(int64_t)j * npix + (int64_t)(int)((double)py + 0.5) * W + (int)((double)px + 0.5)];
+        if (std::fabs(z - dep) > 0.01f) continue;
+        visible = true;
+      }
+      if (!visible) bgdepth[i] = -1.0f;
+    }
+    float hp[3], dn[3];
+    for (int a = 0; a < 3; ++a) hp[a] = o[a] + first * d[a];
+    normalize3(d, dn);
+    float sum[3] = {0.0f, 0.0f, 0.0f}, weight = 0.0f;
+    for (int j = 0; j < nimg; ++j) {
+      float z, px, py;
+      if (!project(ms + 12 * j, hp, z, px, py)) continue;
+      const float dep = depths[(int64_t)j * npix + (int64_t)(int)((double)py + 0.5) * W + (int)((double)px + 0.5)];
+      if (std::fabs(z - dep) > 0.01f) continue;
+      float v[3], vp[3];
+      for (int a = 0; a < 3; ++a) v[a] = hp[a] - origins[3 * j + a];
+      normalize3(v, vp);
+      const int x0 = (int)px, y0 = (int)py;
+      const float fx = px - (float)x0, fy = py - (float)y0;
+      const float w00 = (1.0f - fx) * (1.0f - fy), w11 = fx * fy, w01 = (1.0f - fx) * fy, w10 = fx * (1.0f - fy);
+      const int64_t i00 = (int64_t)j * npix + (int64_t)y0 * W + x0, i10 = i00 + 1, i01 = i00 + W, i11 = i01 + 1;
+      float wc = 1.0f - ((dn[0] * vp[0] + dn[1] * vp[1]) + dn[2] * vp[2]);
+      wc = wc * wc;
+      for (int a = 0; a < 3; ++a) {
+        const float c = ((images[3 * i00 + a] * w00 + images[3 * i01 + a] * w01) + images[3 * i10 + a] * w10) +
+                        images[3 * i11 + a] * w11;
+        sum[a] = sum[a] + wc * c;
+      }
+      weight = weight + wc;
+    }
+    if (weight != 0.0f) {
+      const float inv = 1.0f / weight;
+      for (int a = 0; a < 3; ++a) diffuse[3 * i + a] = sum[a] * inv;
+    }
+  });
+}
+
+void oracle_sample_bg(const float* ro, const float* rd, const float* bgz, int64_t n, int ns, float range,
+                      const float* center, float tile, float* z) {
+  const float hs = tile / 2.0f;
+  const float h3[3] = {hs, hs, hs};
+  for (int64_t i = 0; i < n; ++i) {
+    const float bg = bgz[i];
+    if (bg == -1.0f) continue;
+    const float half = range / 2.0f;
+    const Bound b = ray_aabb(ro + 3 * i, rd + 3 * i, center, h3);
+    float near_ = bg - half, far_ = bg + half;
+    if (near_ <= b.hi) {
+      near_ = b.hi + 0.00001f;
+      far_ = near_ + range;
+    }
+    const float interval = (far_ - near_) / (float)(ns - 1);
+    for (int k = 0; k < ns; ++k) z[i * ns + k] = near_ + (float)k * interval;
+  }
+}
+
+int64_t oracle_patch_rows(const int32_t* valid, int H, int W, int P, const float* ro, const float* rd,
+                          const float* bgdepth, const float* gt, const float* diffuse, float* rows) {
+  const int half = P / 2, ny = patch_count(H, P), nx = patch_count(W, P);
+  int64_t count = 0;
+  for (int qy = 0; qy < ny; ++qy)
+    for (int qx = 0; qx < nx; ++qx) {
+      const int y = half + qy * P, x = half + qx * P;
+      bool any = false;
+      for (int dy = -half; dy <= half && !any; ++dy)
+        for (int dx = -half; dx <= half && !any; ++dx) any = valid[(int64_t)(y + dy) * W + (x + dx)] != 0;
+      if (!any) continue;
+      for (int dy = -half; dy <= half; ++dy)
+        for (int dx = -half; dx <= half; ++dx) {
+          const int64_t idx = (int64_t)(y + dy) * W + (x + dx);
+          float* r = rows + (count * P * P + (dy + half) * P + (dx + half)) * 14;
+          for (int a = 0; a < 3; ++a) {
+            r[a] = ro[3 * idx + a];
+            r[3 + a] = rd[3 * idx + a];
+            r[7 + a] = gt[3 * idx + a];
+            r[10 + a] = diffuse[3 * idx + a];
+          }
+          r[6] = bgdepth[idx];
+          r[13] = (float)valid[idx];
+        }
+      ++count;
+    }
+  return count;
+}
+}  // extern "C"

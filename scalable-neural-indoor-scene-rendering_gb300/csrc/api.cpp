@@ -565,6 +565,18 @@ snisr_status snisr_proxy_hit(snisr_scene* sc, const float* origins, const float*
   return SNISR_OK;
 }
 
+snisr_status snisr_scene_double_hits(snisr_scene* sc, const float* rays_o, const float* rays_d,
+                                    const int32_t* visited, int64_t n, int32_t K, float* double_hits, void* stream) {
+  if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;
+  if (n < 0 || K <= 0) return set_error(SNISR_INVALID_ARG, "double_hits: bad size");
+  if (n == 0) return SNISR_OK;
+  if (!rays_o || !rays_d || !visited || !double_hits) return set_error(SNISR_INVALID_ARG, "double_hits: null argument");
+  if (!sc->S.has_mesh) return set_error(SNISR_INVALID_ARG, "double_hits: the scene has no proxy mesh");
+  DeviceGuard guard(sc->device);
+  CUDA_TRY(launch_double_hits(sc->S, rays_o, rays_d, visited, n, K, double_hits, (cudaStream_t)stream), "double_hits");
+  return SNISR_OK;
+}
+
 snisr_status snisr_trace_voxels(snisr_scene* sc, const float* origins, const float* dirs, int64_t n, int32_t K,
                                 int32_t* visited, int32_t* count, void* stream) {
   if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;

@@ -42,6 +42,35 @@ __device__ __forceinline__ float2 slab(const float o[3], const float d[3], const
   return make_float2(lo, hi);
 }
 
+// voxel_traversal (rendering/src/include/cuda_utils.h:158-238) over the tile
+// grid: p is the start in scene-local coordinates, the visited sparse ids
+// (dense cells mapping to -1 are skipped) go to vis[0..K).
+__device__ __forceinline__ void tile_grid_walk(const float p[3], const float d[3], const int32_t* imap,
+                                               const int M[3], float tile, int K, int32_t* vis) {
+  int cur[3], st[3];
+  float tmax[3], tdel[3];
+  for (int a = 0; a < 3; ++a) {
+    cur[a] = (int)floorf(fdiv(p[a], tile));
+    cur[a] = min(max(cur[a], 0), M[a] - 1);
+    st[a] = d[a] >= 0 ? 1 : -1;
+    float nb = fmul((float)(cur[a] + st[a]), tile);
+    if (st[a] < 0) nb = fadd(nb, tile);
+    tmax[a] = d[a] != 0 ? fdiv(fsub(nb, p[a]), d[a]) : SNISR_INF;
+    tdel[a] = d[a] != 0 ? fmul(fdiv(tile, d[a]), (float)st[a]) : SNISR_INF;
+  }
+  int idx = 0;
+  int id = imap[(cur[0] * M[1] + cur[1]) * M[2] + cur[2]];
+  if (id != -1) vis[idx++] = id;
+  while (idx < K) {
+    int a = (tmax[0] < tmax[1]) ? ((tmax[0] < tmax[2]) ? 0 : 2) : ((tmax[1] < tmax[2]) ? 1 : 2);
+    cur[a] += st[a];
+    tmax[a] = fadd(tmax[a], tdel[a]);
+    if (cur[a] < 0 || cur[a] >= M[a]) break;
+    id = imap[(cur[0] * M[1] + cur[1]) * M[2] + cur[2]];
+    if (id != -1) vis[idx++] = id;
+  }
+}
+
 __device__ __forceinline__ bool occupied(const SceneDev& S, int tile, int vid, uint32_t& rec) {
   const OccWord* w = S.occ + (size_t)tile * S.words_per_tile + (vid >> 6);
   uint4 raw = __ldg(reinterpret_cast<const uint4*>(w));

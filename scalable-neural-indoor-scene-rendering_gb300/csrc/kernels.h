@@ -77,6 +77,9 @@ cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int 
                          int32_t* count, cudaStream_t st);
 cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t,
                          int32_t* tri, cudaStream_t st);
+// Two nearest proxy hits per (ray, visited tile) (trainprep.cu).
+cudaError_t launch_double_hits(const SceneDev& S, const float* ro, const float* rd, const int32_t* visited,
+                               int64_t n, int K, float* hits, cudaStream_t st);
 // Tensor-core training MLP (forward colours / backward with recomputation).
 struct TrainTcArgs {
   const float* vfeat;

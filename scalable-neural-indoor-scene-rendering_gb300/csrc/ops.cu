@@ -59,28 +59,7 @@ __global__ void op_tracing_tiles_kernel(const float* __restrict__ rays_d, int64_
       }
     }
     const int M[3] = {shape[0], shape[1], shape[2]};
-    int cur[3], st[3];
-    float tmax[3], tdel[3];
-    for (int a = 0; a < 3; ++a) {
-      cur[a] = (int)floorf(fdiv(p[a], tile));
-      cur[a] = min(max(cur[a], 0), M[a] - 1);
-      st[a] = d[a] >= 0 ? 1 : -1;
-      float nb = fmul((float)(cur[a] + st[a]), tile);
-      if (st[a] < 0) nb = fadd(nb, tile);
-      tmax[a] = d[a] != 0 ? fdiv(fsub(nb, p[a]), d[a]) : SNISR_INF;
-      tdel[a] = d[a] != 0 ? fmul(fdiv(tile, d[a]), (float)st[a]) : SNISR_INF;
-    }
-    int idx = 0;
-    int id = imap[(cur[0] * M[1] + cur[1]) * M[2] + cur[2]];
-    if (id != -1) vis[idx++] = id;
-    while (idx < K) {
-      int a = (tmax[0] < tmax[1]) ? ((tmax[0] < tmax[2]) ? 0 : 2) : ((tmax[1] < tmax[2]) ? 1 : 2);
-      cur[a] += st[a];
-      tmax[a] = fadd(tmax[a], tdel[a]);
-      if (cur[a] < 0 || cur[a] >= M[a]) break;
-      id = imap[(cur[0] * M[1] + cur[1]) * M[2] + cur[2]];
-      if (id != -1) vis[idx++] = id;
-    }
+    tile_grid_walk(p, d, imap, M, tile, K, vis);
   }
 }
 

@@ -135,6 +135,16 @@ _SIGNATURES = {
     "snisr_op_rendering_diffuse_octree": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32,
                                                     C.c_float, C.c_float, C.c_float, C.c_int32, C.c_float, C.c_float,
                                                     C.c_int32, P, P, P, P]),
+    "snisr_op_train_rays": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P, P]),
+    "snisr_op_train_tracing_tiles": (C.c_int, [P, P, C.c_int64, P, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                               C.c_float, C.c_int32, P, P]),
+    "snisr_scene_double_hits": (C.c_int, [P, P, P, P, C.c_int64, C.c_int32, P, P]),
+    "snisr_op_train_bgdepth": (C.c_int, [C.c_int32, P, P, C.c_int64, C.c_int32, P, P, P]),
+    "snisr_op_gen_diffuse": (C.c_int, [P, C.c_int32, P, P, P, P, P, P, P, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_int32, P, P, P]),
+    "snisr_op_sample_bg": (C.c_int, [P, P, P, C.c_int64, C.c_int32, C.c_float, P, C.c_float, P, P]),
+    "snisr_op_patch_capacity": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32]),
+    "snisr_op_patch_rows": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, P, P, P, P]),
     "snisr_op_transparency_statistic": (C.c_int, [P, P, C.c_int64, C.c_int32, P, C.c_float, C.c_float, C.c_float, P,
                                                   P, P, P]),
     "snisr_op_dilate_boundary": (C.c_int, [P, C.c_int32, P]),

@@ -320,3 +320,32 @@ def pack_occupancy(nodes_flag):
     _lib.check(_lib.lib().snisr_op_pack_occupancy(nodes_flag.data_ptr(), N, words.data_ptr(), count.data_ptr(),
                                                   _stream()))
     return words, count
+
+
+# ---------------------------------------------------------------------------
+# Training-ray preparation: background sampling (CUDA_EXT.Sample_bg)
+# ---------------------------------------------------------------------------
+def Sample_bg(rays_start, rays_dir, bg_zval, tile_center, tile_size, sample_range, z_vals):
+    """training/src/Sample.cpp:81-105 / Sample_kernel.cu:481-542: z_vals
+    [B,Ns] uniform over bg +- range/2 (behind the tile's exit if that range
+    starts inside it); rows with bg == -1 are left as they are."""
+    import torch
+    _check(rays_start, "rays_start", torch.float32, 2)
+    _check(rays_dir, "rays_dir", torch.float32, 2)
+    _check(bg_zval, "bg_zval", torch.float32, 2)
+    _check(tile_center, "tile_center", torch.float32, 1)
+    _check(z_vals, "z_vals", torch.float32, 2)
+    B, ns = z_vals.shape
+    if rays_start.shape[0] != B or rays_dir.shape[0] != B or bg_zval.numel() != B:
+        raise RuntimeError("Sample_bg: inconsistent batch sizes")
+    _lib.check(_lib.lib().snisr_op_sample_bg(rays_start.data_ptr(), rays_dir.data_ptr(), bg_zval.data_ptr(), B, ns,
+                                             float(sample_range), tile_center.data_ptr(), float(tile_size),
+                                             z_vals.data_ptr(), _stream()))
+
+
+def sampling_background(rays_o, rays_d, bgdepth, tile_center, tile_size, nsamples, sample_range):
+    """training/scripts/utils.py:815-820: z_vals pre-filled with -1."""
+    import torch
+    z = torch.full((rays_o.shape[0], nsamples), -1, dtype=torch.float32, device=rays_o.device)
+    Sample_bg(rays_o, rays_d, bgdepth, tile_center, tile_size, sample_range, z)
+    return z
