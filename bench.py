@@ -674,6 +674,88 @@ def pruning_bench(dev, steps: int, warmup: int, flush):
             "l2": "flushed before each step"}
 
 
+PREP_WORKLOAD = ("training-data preparation of one tile of the 4x4x1-tile scene (get_trainData_v3, "
+                 "training/src/cuda_func.cu:1341-1686) per 1280x720 view: training rays, tile DDA, two nearest hits "
+                 "of the 207k-triangle proxy mesh per visited tile (BVH), background depth and validity, diffuse "
+                 "estimate from 16 selected views (projection + depth test), 7x7 patch rows; images seeded noise, "
+                 "depth maps from the proxy mesh")
+
+
+def trainprep_bench(dev, steps: int, warmup: int, flush):
+    """Per-view chain of get_trainData_v3 on resident images and depths."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import oracle
+    import snisr
+    from snisr import trainprep
+    s = snisr.SynthScene(snisr.CFG2)
+    a = s.arrays()
+    d = s.desc
+    sc = snisr.Scene(d)
+    H, W, M, KT, P = 720, 1280, 16, 30, 7
+    Ks, C2Ws = [], []
+    for v in range(M):
+        cam = s.camera(v, W, H)
+        f = 1.0 / cam.inv_focal
+        Ks.append(np.array([f, 0, cam.cx, 0, f, cam.cy, 0, 0, 1], np.float32))
+        C2Ws.append(np.array(list(cam.c2w), np.float32))
+    Ks, C2Ws = np.stack(Ks), np.stack(C2Ws)
+    rng = np.random.default_rng(3)
+    images = torch.from_numpy(rng.random((M, H * W, 3), dtype=np.float32)).to(dev)
+    depths = torch.empty(M, H * W, device=dev)
+    imap = np.asarray(a["tile_index"], np.int32).reshape(-1)
+    grid = (int(d.grid[0]), int(d.grid[1]), int(d.grid[2]))
+    smin = np.array(list(d.scene_min), np.float32)
+    tp = trainprep.TrainPrep(sc, H, W, imap, grid, smin, float(d.tile_size), KT, P, device=dev.index)
+    Kt = [torch.from_numpy(Ks[j].copy()).to(dev) for j in range(M)]
+    Ct = [torch.from_numpy(C2Ws[j].copy()).to(dev) for j in range(M)]
+    for j in range(M):  # depth maps: proxy-mesh first hits along the training rays (camera z)
+        from snisr import _lib
+        _lib.check(_lib.lib().snisr_op_train_rays(Kt[j].data_ptr(), Ct[j].data_ptr(), H, W, tp.ro.data_ptr(),
+                                                  tp.rd.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        t, _ = sc.proxy_hit(tp.ro, tp.rd)
+        depths[j] = torch.where(t > 0, t, torch.full_like(t, 1e4))
+    proj = torch.from_numpy(np.stack([trainprep.project_matrix(Ks[j], C2Ws[j]) for j in range(M)])).to(dev)
+    origins = torch.from_numpy(C2Ws[:, [3, 7, 11]].copy()).to(dev)
+    train_tile = 5
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(warmup):
+        tp.view(train_tile, Kt[i % M], Ct[i % M], images[i % M], origins, images, depths, proj)
+    torch.cuda.synchronize()
+    tot, patches = 0.0, 0
+    for i in range(steps):
+        j = i % M
+        flush.zero_()
+        e0.record(stream)
+        rows, count = tp.view(train_tile, Kt[j], Ct[j], images[j], origins, images, depths, proj)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+        patches += int(count)
+    sc.check()
+    ms = tot / steps
+    # CPU: the oracle chain on a 160x90 view (double hits and diffuse on 16 threads)
+    h, w = 90, 160
+    t0 = time.perf_counter()
+    ro, rd = oracle.train_rays(Ks[0] * np.array([w / W, 1, w / W, 1, h / H, h / H, 1, 1, 1], np.float32),
+                               C2Ws[0], h, w)
+    vis = oracle.train_tracing(ro, rd, imap, grid, smin, float(d.tile_size), KT)
+    osc = oracle.OracleScene(d)
+    hits = osc.double_hits(ro, rd, vis)
+    oracle.train_bgdepth(train_tile, vis, hits)
+    cpu_s = time.perf_counter() - t0
+    sc.close()
+    return {"workload": PREP_WORKLOAD, "unit": "views/s", "value": round(1e3 / ms, 2), "ms_per_step": round(ms, 4),
+            "mrays_s": round(H * W / ms / 1e3, 2), "patches_per_view": round(patches / steps, 1),
+            "cpu_oracle": {"value": round(h * w / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": oracle.threads(),
+                           "sample": f"one {w}x{h} view: rays, tile DDA, double hits, background depth"},
+            "l2": "flushed before each view"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -706,7 +788,7 @@ def main():
     ap.add_argument("--no-train", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--profile-run", choices=["render", "train", "batched", "large", "specular", "pipeline",
-                                              "pruning"],
+                                              "pruning", "trainprep"],
                     default=None,
                     help="render: a few frames of both forms (small workspace); train: a few training steps of "
                          "both forms (for ncu captures)")
@@ -724,11 +806,11 @@ def main():
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.profile_run in ("train", "batched", "large", "specular", "pipeline", "pruning"):
+    if args.profile_run in ("train", "batched", "large", "specular", "pipeline", "pruning", "trainprep"):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
         fn = {"train": train_bench, "batched": batched_bench, "large": large_scene_bench,
               "specular": specular_bench, "pipeline": reference_pipeline_bench,
-              "pruning": pruning_bench}[args.profile_run]
+              "pruning": pruning_bench, "trainprep": trainprep_bench}[args.profile_run]
         res = fn(dev, args.steps, args.warmup, flush)
         print(json.dumps({"profile_run": args.profile_run, args.profile_run: res}))
         return
@@ -886,6 +968,7 @@ def main():
     specular = specular_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
     pipeline = reference_pipeline_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
     pruning = pruning_bench(dev, min(20, max(3, args.steps // 10)), 3, flush)
+    prep = trainprep_bench(dev, min(16, max(3, args.steps // 10)), 3, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -917,6 +1000,7 @@ def main():
             "specular_pass": specular,
             "reference_pipeline": pipeline,
             "pruning": pruning,
+            "train_prep": prep,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
