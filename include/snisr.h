@@ -219,7 +219,8 @@ snisr_status snisr_train_forward(snisr_scene* scene, const float* vfeat_dev,
  * scene and rays: per-ray reverse compositing with suffix sums, per-sample
  * recomputation of features and MLP activations.  grad_rgb_dev [n*3] =
  * dL/drgb; rgb_dev (the forward output) may be NULL.  Gradients are
- * ACCUMULATED (+=) into gvfeat_dev [NV][F], gvdens_dev [NV], gmlp_dev [NT][P]. */
+ * ACCUMULATED (+=) into gvfeat_dev [NV][F] (16-byte aligned), gvdens_dev [NV],
+ * gmlp_dev [NT][P]. */
 snisr_status snisr_train_backward(snisr_scene* scene, const float* vfeat_dev,
                                   const float* vdens_dev, const float* mlp_dev,
                                   const float* origins_dev, const float* dirs_dev,

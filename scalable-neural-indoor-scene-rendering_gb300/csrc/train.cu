@@ -399,7 +399,8 @@ __global__ void __launch_bounds__(128) tr_mlp_bwd_plain(SceneDev S, const float*
 #pragma unroll
     for (int k = 0; k < 8; ++k)
 #pragma unroll
-      for (int q = 0; q < F; ++q) atomicAdd(gvfeat + (size_t)c[k] * F + q, w[k] * dx[q]);
+      for (int q = 0; q < F; q += 4)
+        red_add_v4(gvfeat + (size_t)c[k] * F + q, w[k] * dx[q], w[k] * dx[q + 1], w[k] * dx[q + 2], w[k] * dx[q + 3]);
   }
 }
 
@@ -655,6 +656,8 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   if (!vfeat || !mlp || !dirs || !grad_rgb || !gvfeat || !gvdens || !gmlp)
     return set_error(SNISR_INVALID_ARG, "train_backward: null pointer argument");
   if (form != SNISR_FORM_PLAIN_FP32 && form != SNISR_FORM_TC) return set_error(SNISR_INVALID_ARG, "train_backward: bad form");
+  if (reinterpret_cast<uintptr_t>(gvfeat) % 16 != 0)
+    return set_error(SNISR_INVALID_ARG, "train_backward: gvfeat must be 16-byte aligned (vector reductions)");
   cudaStream_t st = (cudaStream_t)stream;
   SceneDev S;
   TrainWS* T = nullptr;

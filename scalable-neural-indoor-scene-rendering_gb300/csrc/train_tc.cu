@@ -631,9 +631,10 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
           const int cn[8] = {my_ca.x, my_ca.y, my_ca.z, my_ca.w, my_cb.x, my_cb.y, my_cb.z, my_cb.w};
 #pragma unroll
           for (int k = 0; k < 8; ++k) {
-            float* g = gvfeat + (size_t)cn[k] * F;
+            float* g = gvfeat + (size_t)cn[k] * F;  // 16-byte aligned rows (F a multiple of 4)
 #pragma unroll
-            for (int q = 0; q < F; ++q) atomicAdd(g + q, wk[k] * dx[q]);
+            for (int q = 0; q < F; q += 4)
+              red_add_v4(g + q, wk[k] * dx[q], wk[k] * dx[q + 1], wk[k] * dx[q + 2], wk[k] * dx[q + 3]);
           }
         }
       }
