@@ -176,28 +176,30 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
 // rows; view encoding copied from the per-ray split table.  Loads are issued
 // in stages across the lane's rows (records, then corner ids and encodings,
 // then features) so that each stage waits for memory once, not once per row.
-template <int F>
+template <int F, int NW = 4>
 __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restrict__ vfeat,
                                          const TrainRecT* __restrict__ recs, int row0, int cnt,
                                          const uint4* __restrict__ enc, uint8_t* Xhi, uint8_t* Xlo, int warp, int lane) {
-  constexpr int G = F / 8, RPI = 32 / G;
+  // NW warps share the 128 rows: RPW rows per warp, RPI rows per lane pass
+  constexpr int G = F / 8, RPI = 32 / G, RPW = 128 / NW, ITS = RPW / RPI;
+  static_assert(RPW % RPI == 0, "rows per warp must be a multiple of rows per pass");
   const int my_g = lane / RPI, my_row = lane % RPI;
   const uint4 z = make_uint4(0, 0, 0, 0);
-  uint4 head[G], fr[G];  // {rec, ray, tile, pad}, {f0, f1, f2, dv}
+  uint4 head[ITS], fr[ITS];  // {rec, ray, tile, pad}, {f0, f1, f2, dv}
 #pragma unroll
-  for (int it = 0; it < G; ++it) {
-    const int r = warp * 32 + it * RPI + my_row;
+  for (int it = 0; it < ITS; ++it) {
+    const int r = warp * RPW + it * RPI + my_row;
     if (r < cnt) {
       const uint4* src = reinterpret_cast<const uint4*>(recs + row0 + r);
       head[it] = __ldg(src);
       fr[it] = __ldg(src + 1);
     }
   }
-  int4 ca[G], cb[G];
-  uint4 eh[G], el[G];
+  int4 ca[ITS], cb[ITS];
+  uint4 eh[ITS], el[ITS];
 #pragma unroll
-  for (int it = 0; it < G; ++it) {
-    const int r = warp * 32 + it * RPI + my_row;
+  for (int it = 0; it < ITS; ++it) {
+    const int r = warp * RPW + it * RPI + my_row;
     if (r < cnt) {
       const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)head[it].x * 8);
       ca[it] = __ldg(cn);
@@ -209,8 +211,8 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
     }
   }
 #pragma unroll
-  for (int it = 0; it < G; ++it) {
-    const int r = warp * 32 + it * RPI + my_row;
+  for (int it = 0; it < ITS; ++it) {
+    const int r = warp * RPW + it * RPI + my_row;
     if (r < cnt) {
       const float f[3] = {__uint_as_float(fr[it].x), __uint_as_float(fr[it].y), __uint_as_float(fr[it].z)};
       float w[8];
@@ -281,6 +283,29 @@ __device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* dst_hi, 
       if (dst_lo)
         *reinterpret_cast<uint4*>(dst_lo + tc::sw128_offset(row, 4 * half + q)) = make_uint4(l[0], l[1], l[2], l[3]);
     }
+  }
+}
+
+// The same for one of NP column parts of the accumulator (H / NP columns,
+// a multiple of 16): part p covers columns [p H / NP, (p + 1) H / NP).
+template <int H, int NP>
+__device__ __forceinline__ void epi_relu_split_part(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_lo, int row,
+                                                    int part) {
+  constexpr int CP = H / NP;
+  static_assert(CP % 16 == 0, "column parts of 16");
+  float v[CP];
+#pragma unroll
+  for (int j = 0; j < CP; j += 16) tc::tmem_ld16(taddr + part * CP + j, v + j);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int q = 0; q < CP / 8; ++q) {
+    const int chunk = part * (CP / 8) + q;
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], l[j]);
+    *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, chunk)) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (dst_lo) *reinterpret_cast<uint4*>(dst_lo + tc::sw128_offset(row, chunk)) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -426,7 +451,7 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
 // lanes 64..127 (output units that do not exist) and are never read.
 // ---------------------------------------------------------------------------
 template <int F, int H, int L>
-__global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float* __restrict__ vfeat,
+__global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float* __restrict__ vfeat,
                                                         const TrainRecT* __restrict__ recs,
                                                         const int32_t* __restrict__ tstart,
                                                         const int32_t* __restrict__ coff, int* work,
@@ -449,7 +474,10 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 2048);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
+  // 8 warps: warps w and w + 4 read the same tensor-memory lane quarter
+  // (rows 32 (w % 4) ..) and split the accumulator columns (part = w / 4)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = tid & 127, part = tid >> 7;
   const int NT = S.num_tiles;
   Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
   if (tid == 0) {
@@ -461,13 +489,13 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
     tc::tmem_relinquish();
   }
-  for (int k = tid; k < 64; k += 128) {
+  for (int k = tid; k < 64; k += 256) {
     reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16Eighth, kBf16Eighth, kBf16Eighth, kBf16Eighth);
     reinterpret_cast<uint4*>(ones + 1024)[k] = make_uint4(kBf16One, kBf16One, kBf16One, kBf16One);
   }
   // all tiles start zeroed: DO columns beyond 3 and the columns beyond H of
   // the activation / delta tiles are never written afterwards
-  for (int k = tid; k < kTiles * 16384 / 16; k += 128) reinterpret_cast<uint4*>(base)[k] = make_uint4(0, 0, 0, 0);
+  for (int k = tid; k < kTiles * 16384 / 16; k += 256) reinterpret_cast<uint4*>(base)[k] = make_uint4(0, 0, 0, 0);
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -481,9 +509,10 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   const int total = coff[NT];
   int cur_tile = -1;
   bool failed = false, have_acc = false;
-  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 
   // flush the weight/bias gradient accumulators of `tile` to global memory
+  // (lanes = output units: threads 0..fo-1 of the first part)
   auto flush = [&](int tile) {
     float* G = gmlp + (size_t)tile * S.params_per_tile;
     int64_t off = 0;
@@ -524,23 +553,22 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     // this thread's own row: output gradient, and the record and corner ids
     // the feature-gradient scatter needs at the end of the chunk (loaded now,
     // consumed after the MMA chain)
-    const bool mine = tid < cp.cnt;
+    const bool mine = row < cp.cnt;
     float4 dmine = make_float4(0.f, 0.f, 0.f, 0.f);
     uint4 my_fr = make_uint4(0, 0, 0, 0);
-    int4 my_ca = make_int4(0, 0, 0, 0), my_cb = make_int4(0, 0, 0, 0);
+    int4 my_cn = make_int4(0, 0, 0, 0);  // corners 4 part .. 4 part + 3 (each part scatters four)
     if (mine) {
-      dmine = __ldg(dout + cp.row0 + tid);
-      const uint4* src = reinterpret_cast<const uint4*>(recs + cp.row0 + tid);
+      if (part == 0) dmine = __ldg(dout + cp.row0 + row);
+      const uint4* src = reinterpret_cast<const uint4*>(recs + cp.row0 + row);
       const uint32_t my_rec = __ldg(src).x;
       my_fr = __ldg(src + 1);
-      const int4* cn = reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8);
-      my_ca = __ldg(cn);
-      my_cb = __ldg(cn + 1);
+      my_cn = __ldg(reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8) + part);
     }
-    gather_x<F>(S, vfeat, recs, cp.row0, cp.cnt, enc, Xt, LoA, warp, lane);
+    gather_x<F, 8>(S, vfeat, recs, cp.row0, cp.cnt, enc, Xt, LoA, warp, lane);
     // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
-    *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(tid, 0)) =
-        make_uint2(pack_bf2(dmine.x, dmine.y), pack_bf2(dmine.z, 0.f));
+    if (part == 0)
+      *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(row, 0)) =
+          make_uint2(pack_bf2(dmine.x, dmine.y), pack_bf2(dmine.z, 0.f));
     tc::fence_proxy_async();
     __syncthreads();
     if (new_w) {
@@ -562,7 +590,7 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
         tc::mma_commit(B.mbar);
       }
       if (!wait_mma(B, tid)) { failed = true; break; }
-      epi_relu_split<H>(taddr, Ht + l * 16384, l + 1 < L ? lo_out : nullptr, tid);
+      epi_relu_split_part<H, 2>(taddr, Ht + l * 16384, l + 1 < L ? lo_out : nullptr, row, part);
       tc::fence_proxy_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -595,26 +623,26 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       }
       if (!wait_mma(B, tid)) { failed = true; break; }
       if (l > 0) {
-        // delta of layer l-1's output = (delta W_l) * [act > 0], BF16 into D
+        // delta of layer l-1's output = (delta W_l) * [act > 0], BF16 into D;
+        // this thread's part: columns [part H/2, (part+1) H/2)
+        constexpr int CP = H / 2;
+        float v[CP];
 #pragma unroll
-        for (int half = 0; half < H / 32; ++half) {
-          float v[32];
-          tc::tmem_ld16(taddr + 32 * half, v);
-          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
-          tc::tmem_wait_ld();
+        for (int j = 0; j < CP; j += 16) tc::tmem_ld16(taddr + part * CP + j, v + j);
+        tc::tmem_wait_ld();
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const uint4 hv = *reinterpret_cast<const uint4*>(Ht + (l - 1) * 16384 + tc::sw128_offset(tid, 4 * half + q));
-            const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
-            uint32_t o[4];
+        for (int q = 0; q < CP / 8; ++q) {
+          const int chunk = part * (CP / 8) + q;
+          const uint4 hv = *reinterpret_cast<const uint4*>(Ht + (l - 1) * 16384 + tc::sw128_offset(row, chunk));
+          const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+          uint32_t o[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              const float a0 = pos_lo(hw[j]) ? v[8 * q + 2 * j] : 0.f;
-              const float a1 = pos_hi(hw[j]) ? v[8 * q + 2 * j + 1] : 0.f;
-              o[j] = pack_bf2(a0, a1);
-            }
-            *reinterpret_cast<uint4*>(Dt + tc::sw128_offset(tid, 4 * half + q)) = make_uint4(o[0], o[1], o[2], o[3]);
+          for (int j = 0; j < 4; ++j) {
+            const float a0 = pos_lo(hw[j]) ? v[8 * q + 2 * j] : 0.f;
+            const float a1 = pos_hi(hw[j]) ? v[8 * q + 2 * j + 1] : 0.f;
+            o[j] = pack_bf2(a0, a1);
           }
+          *reinterpret_cast<uint4*>(Dt + tc::sw128_offset(row, chunk)) = make_uint4(o[0], o[1], o[2], o[3]);
         }
         tc::fence_proxy_async();
       } else {
@@ -628,13 +656,14 @@ __global__ void __launch_bounds__(128, 1) tr_mlp_bwd_tc(SceneDev S, const float*
           const float f[3] = {__uint_as_float(my_fr.x), __uint_as_float(my_fr.y), __uint_as_float(my_fr.z)};
           float wk[8];
           trilinear_weights(f, wk);
-          const int cn[8] = {my_ca.x, my_ca.y, my_ca.z, my_ca.w, my_cb.x, my_cb.y, my_cb.z, my_cb.w};
+          const int cn[4] = {my_cn.x, my_cn.y, my_cn.z, my_cn.w};
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
+          for (int k = 0; k < 4; ++k) {
+            const float wkk = wk[4 * part + k];
             float* g = gvfeat + (size_t)cn[k] * F;  // 16-byte aligned rows (F a multiple of 4)
 #pragma unroll
             for (int q = 0; q < F; q += 4)
-              red_add_v4(g + q, wk[k] * dx[q], wk[k] * dx[q + 1], wk[k] * dx[q + 2], wk[k] * dx[q + 3]);
+              red_add_v4(g + q, wkk * dx[q], wkk * dx[q + 1], wkk * dx[q + 2], wkk * dx[q + 3]);
           }
         }
       }
@@ -698,7 +727,7 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
       return cudaFuncSetAttribute(tr_mlp_bwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     });
     if (e != cudaSuccess) return e;
-    tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
+    tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 256, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                          a.work, a.enc, a.wimg, a.img_stride, a.dout, a.gvfeat,
                                                          a.gmlp);
   }
