@@ -29,8 +29,10 @@ namespace {
 
 constexpr int kOctBlocks = 4;
 
-__device__ __forceinline__ __half hlerp(__half a, __half b, float x) {  // a * (1 - x) + b * x, FP16
-  return __hadd_rn(__hmul_rn(a, __float2half(fsub(1.0f, x))), __hmul_rn(b, __float2half(x)));
+// a * (1 - x) + b * x on both FP16 lanes (r, g) or (b, a): the same
+// per-lane operations and roundings as the scalar form, half the instructions
+__device__ __forceinline__ __half2 hlerp2(__half2 a, __half2 b, __half2 one_minus_x, __half2 x) {
+  return __hadd2_rn(__hmul2_rn(a, one_minus_x), __hmul2_rn(b, x));
 }
 
 __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const int32_t* __restrict__ visited,
@@ -125,26 +127,31 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
               ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
             }
             if (ok) {
-              float w[3];
+              __half2 wx[3], ux[3];  // x and 1 - x in FP16 on both lanes
 #pragma unroll
-              for (int a = 0; a < 3; ++a) w[a] = fmaxf(fsub(f[a], (float)x0[a]), 0.0f);
-              __half v[8][4];
+              for (int a = 0; a < 3; ++a) {
+                const float w = fmaxf(fsub(f[a], (float)x0[a]), 0.0f);
+                wx[a] = __float2half2_rn(w);
+                ux[a] = __float2half2_rn(fsub(1.0f, w));
+              }
+              __half2 rg[8], ba[8];  // corner k = (dx, dy, dz) = (k & 1, (k >> 1) & 1, (k >> 2) & 1)
 #pragma unroll
               for (int k = 0; k < 8; ++k) {
                 const int xi = x0[0] + (k & 1), yi = x0[1] + ((k >> 1) & 1), zi = x0[2] + ((k >> 2) & 1);
                 const uint2 q = __ldg(vox + nodes[xi * DD + yi * D + zi]);
-                v[k][0] = __ushort_as_half((unsigned short)(q.x & 0xFFFFu));
-                v[k][1] = __ushort_as_half((unsigned short)(q.x >> 16));
-                v[k][2] = __ushort_as_half((unsigned short)(q.y & 0xFFFFu));
-                v[k][3] = __ushort_as_half((unsigned short)(q.y >> 16));
+                rg[k] = *reinterpret_cast<const __half2*>(&q.x);
+                ba[k] = *reinterpret_cast<const __half2*>(&q.y);
               }
-              __half rgba[4];
-#pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                const __half s0 = hlerp(hlerp(v[0][q], v[1][q], w[0]), hlerp(v[2][q], v[3][q], w[0]), w[1]);
-                const __half s1 = hlerp(hlerp(v[4][q], v[5][q], w[0]), hlerp(v[6][q], v[7][q], w[0]), w[1]);
-                rgba[q] = hlerp(s0, s1, w[2]);
-              }
+              const __half2 rg0 = hlerp2(hlerp2(rg[0], rg[1], ux[0], wx[0]), hlerp2(rg[2], rg[3], ux[0], wx[0]), ux[1],
+                                         wx[1]);
+              const __half2 rg1 = hlerp2(hlerp2(rg[4], rg[5], ux[0], wx[0]), hlerp2(rg[6], rg[7], ux[0], wx[0]), ux[1],
+                                         wx[1]);
+              const __half2 ba0 = hlerp2(hlerp2(ba[0], ba[1], ux[0], wx[0]), hlerp2(ba[2], ba[3], ux[0], wx[0]), ux[1],
+                                         wx[1]);
+              const __half2 ba1 = hlerp2(hlerp2(ba[4], ba[5], ux[0], wx[0]), hlerp2(ba[6], ba[7], ux[0], wx[0]), ux[1],
+                                         wx[1]);
+              const __half2 rgm = hlerp2(rg0, rg1, ux[2], wx[2]), bam = hlerp2(ba0, ba1, ux[2], wx[2]);
+              const __half rgba[4] = {__low2half(rgm), __high2half(rgm), __low2half(bam), __high2half(bam)};
               const float interval = fminf(sample_step, fsub(far_, z));
               const __half alpha =
                   __hsub_rn(one, hexp(__hmul_rn(__hmul_rn(rgba[3], __float2half(-1.0f)), __float2half(interval))));
