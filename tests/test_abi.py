@@ -117,3 +117,64 @@ def test_synthetic_mesh_cfg2_sizes():
     assert 150_000 < d.num_triangles < 260_000
     a = s.arrays()
     assert a["mesh_faces"].max() < d.num_mesh_vertices
+
+
+def test_op_argument_validation_without_cuda():
+    """The drop-in ops reject bad sizes and null buffers (and return at once
+    for empty inputs) before any CUDA call."""
+    L = snisr.lib()
+    OK, BAD = _lib.OK, _lib.INVALID_ARG
+    P = C.c_void_p
+    fake = P(16)  # never dereferenced: every call below returns before a launch
+    cnt = C.c_int64(-1)
+    # sort_by_key / assign_pixels / inference_mlp (specular pass)
+    assert L.snisr_op_sort_by_key(None, None, None, 0, C.byref(cnt), None) == OK and cnt.value == 0
+    assert L.snisr_op_sort_by_key(None, None, None, 5, C.byref(cnt), None) == BAD
+    assert L.snisr_op_sort_by_key(fake, fake, fake, -1, C.byref(cnt), None) == BAD
+    assert L.snisr_op_assign_pixels(None, None, None, 0, None, None, None) == OK
+    assert L.snisr_op_assign_pixels(None, None, None, 3, None, None, None) == BAD
+    bufs = [None] * 9  # transparency, qpix, pixel_starts, centers, samples, rays_d, params, results, err
+    assert len(_lib._SIGNATURES["snisr_op_inference_mlp"][1]) == 16
+    assert L.snisr_op_inference_mlp(16, 0, 0.1, 0.01, None, 16, *bufs, None) == OK
+    assert L.snisr_op_inference_mlp(0, 4, 0.1, 0.01, None, 16, *bufs, None) == BAD
+    assert L.snisr_op_inference_mlp(16, 4, 0.1, 0.01, None, 16, *bufs, None) == BAD
+    # FP16 octree diffuse renderer
+    oct_args = lambda npix, K, tile: (None, None, npix, K) + (None,) * 8 + (1, tile, 0.1, 0.02, 18, 0.8, 0.01, 0,
+                                                                           None, None, None, None)
+    assert L.snisr_op_rendering_diffuse_octree(*oct_args(0, 30, 6.4)) == OK
+    assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 6.4)) == BAD  # null buffers
+    assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 0, 6.4)) == BAD
+    assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 0.0)) == BAD
+    # pruning
+    assert L.snisr_op_transparency_statistic(None, None, 0, 18, None, 1.0, 0.0625, 0.006, None, None, None,
+                                             None) == OK
+    assert L.snisr_op_transparency_statistic(None, None, 5, 18, None, 1.0, 0.0625, 0.006, None, None, None,
+                                             None) == BAD
+    assert L.snisr_op_transparency_statistic(fake, fake, 5, 2000, fake, 1.0, 0.0625, 0.006, fake, fake, fake,
+                                             None) == BAD
+    assert L.snisr_op_dilate_boundary(None, 18, None) == BAD
+    assert L.snisr_op_dilate_boundary(fake, 0, None) == BAD
+    assert L.snisr_op_prune_flags(fake, fake, None, 18, 4, 0.5, 0.0, fake, None) == BAD  # 18 % 4 != 0
+    assert L.snisr_op_prune_flags(None, fake, None, 16, 4, 0.5, 0.0, fake, None) == BAD
+    assert L.snisr_op_pack_occupancy(fake, 16, None, fake, None) == BAD
+    # training-ray preparation
+    assert L.snisr_op_train_rays(fake, fake, 0, 640, fake, fake, None) == BAD
+    assert L.snisr_op_train_rays(None, fake, 480, 640, fake, fake, None) == BAD
+    shape = (C.c_int32 * 3)(4, 4, 1)
+    smin = (C.c_float * 3)(0, 0, 0)
+    assert L.snisr_op_train_tracing_tiles(None, None, 0, None, shape, smin, 3.0, 30, None, None) == OK
+    assert L.snisr_op_train_tracing_tiles(fake, fake, 8, fake, shape, smin, 3.0, 0, fake, None) == BAD
+    assert L.snisr_op_train_tracing_tiles(fake, fake, 8, fake, (C.c_int32 * 3)(0, 4, 1), smin, 3.0, 30, fake,
+                                          None) == BAD
+    assert L.snisr_op_train_bgdepth(0, None, None, 0, 30, None, None, None) == OK
+    assert L.snisr_op_train_bgdepth(0, None, None, 8, 30, None, None, None) == BAD
+    assert L.snisr_op_gen_diffuse(None, 0, fake, fake, fake, fake, None, None, None, 30, 4, 1, 640, fake, fake,
+                                  None) == BAD
+    assert L.snisr_op_gen_diffuse(None, 0, fake, fake, fake, fake, None, None, None, 30, 4, 480, 640, fake, fake,
+                                  None) == BAD  # images missing for 4 views
+    assert L.snisr_op_sample_bg(None, None, None, 0, 16, 0.5, None, 3.0, None, None) == OK
+    assert L.snisr_op_sample_bg(fake, fake, fake, 8, 1, 0.5, fake, 3.0, fake, None) == BAD
+    assert L.snisr_op_patch_capacity(720, 1280, 7) == ((720 - 7 - 3 + 6) // 7) * ((1280 - 7 - 3 + 6) // 7)
+    assert L.snisr_op_patch_capacity(720, 1280, 6) == -1 and L.snisr_op_patch_capacity(5, 5, 7) == 0
+    assert L.snisr_op_patch_rows(fake, 720, 1280, 8, fake, fake, fake, fake, fake, fake, fake, fake, None) == BAD
+    assert L.snisr_scene_double_hits(None, fake, fake, fake, 8, 30, fake, None) == BAD
