@@ -151,6 +151,17 @@ snisr_status snisr_render(snisr_scene* scene, const snisr_camera* cam, int32_t f
 snisr_status snisr_render_host(snisr_scene* scene, const snisr_camera* cam, int32_t form,
                                float* rgb_host, float* depth_host, float* opacity_host,
                                void* stream);
+/* Pipelined form for frame sequences: renders on `stream` into one of two
+ * device staging slots and enqueues the device->host copies on a stream of
+ * the scene, then returns without waiting, so that the copies of frame i
+ * overlap the rendering of frame i+1.  The host buffers of a call are
+ * complete after the second following call on the scene returns or after
+ * snisr_render_host_wait; they must not be touched before. */
+snisr_status snisr_render_host_async(snisr_scene* scene, const snisr_camera* cam, int32_t form,
+                                     float* rgb_host, float* depth_host, float* opacity_host,
+                                     void* stream);
+/* Waits until every copy enqueued by snisr_render_host_async has landed. */
+snisr_status snisr_render_host_wait(snisr_scene* scene);
 
 /* Plain FP32 render of at most 32768 rays that allocates no device memory
  * (no counterpart in the reference).  For callers that may not call

@@ -55,6 +55,12 @@ struct snisr_scene {
   cudaEvent_t ev[8] = {};
   float* out_bufs = nullptr;          // staging for render_host
   uint32_t* fp_bits = nullptr;        // footprint bitmaps (voxels, vertices) + 2 counters, lazily
+  // render_host_async: two device staging slots, a copy stream, per-slot
+  // events (render done -> copy may start; copy done -> slot may be reused)
+  float* async_bufs = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t render_done[2] = {}, copy_done[2] = {};
+  int async_slot = 0;
 };
 
 namespace {
@@ -98,6 +104,14 @@ void free_scene(snisr_scene* sc) {
   if (sc->err_host) cudaFreeHost(sc->err_host);
   for (cudaEvent_t e : sc->ev)
     if (e) cudaEventDestroy(e);
+  for (int k = 0; k < 2; ++k) {
+    if (sc->render_done[k]) cudaEventDestroy(sc->render_done[k]);
+    if (sc->copy_done[k]) cudaEventDestroy(sc->copy_done[k]);
+  }
+  if (sc->copy_stream) {
+    cudaStreamSynchronize(sc->copy_stream);
+    cudaStreamDestroy(sc->copy_stream);
+  }
   cudaSetDevice(prev);
   delete sc;
 }
@@ -550,6 +564,58 @@ snisr_status snisr_render_host(snisr_scene* sc, const snisr_camera* cam, int32_t
   CUDA_TRY(cudaMemcpyAsync(depth_h, ddep, (size_t)n * 4, cudaMemcpyDeviceToHost, st), "render_host: copy depth");
   CUDA_TRY(cudaMemcpyAsync(opac_h, dop, (size_t)n * 4, cudaMemcpyDeviceToHost, st), "render_host: copy opacity");
   CUDA_TRY(cudaStreamSynchronize(st), "render_host: synchronise");
+  return SNISR_OK;
+}
+
+snisr_status snisr_render_host_async(snisr_scene* sc, const snisr_camera* cam, int32_t form, float* rgb_h,
+                                     float* depth_h, float* opac_h, void* stream) {
+  if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;
+  if (!cam || !rgb_h || !depth_h || !opac_h) return set_error(SNISR_INVALID_ARG, "render_host_async: null argument");
+  const int64_t n = (int64_t)cam->width * cam->height;
+  if (n <= 0 || n > sc->ws.max_rays)
+    return set_error(SNISR_INVALID_ARG, "render_host_async: frame exceeds the workspace");
+  DeviceGuard guard(sc->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t cap = sc->ws.max_rays;
+  if (!sc->async_bufs) {
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, (size_t)cap * 5 * 4 * 2), "render_host_async: output staging");
+    sc->async_bufs = static_cast<float*>(p);
+    sc->allocs.push_back(p);
+    sc->info.device_bytes += cap * 40;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sc->copy_stream, cudaStreamNonBlocking), "render_host_async: copy stream");
+    for (int k = 0; k < 2; ++k) {
+      CUDA_TRY(cudaEventCreateWithFlags(&sc->render_done[k], cudaEventDisableTiming), "render_host_async: events");
+      CUDA_TRY(cudaEventCreateWithFlags(&sc->copy_done[k], cudaEventDisableTiming), "render_host_async: events");
+      CUDA_TRY(cudaEventRecord(sc->copy_done[k], sc->copy_stream), "render_host_async: events");
+    }
+  }
+  const int k = sc->async_slot;
+  sc->async_slot ^= 1;
+  float* drgb = sc->async_bufs + (size_t)k * cap * 5;
+  float* ddep = drgb + 3 * cap;
+  float* dop = ddep + cap;
+  // the slot's previous copy must be done before this frame overwrites it
+  CUDA_TRY(cudaStreamWaitEvent(st, sc->copy_done[k], 0), "render_host_async: order");
+  snisr_status s = snisr_render(sc, cam, form, drgb, ddep, dop, stream);
+  if (s != SNISR_OK) return s;
+  CUDA_TRY(cudaEventRecord(sc->render_done[k], st), "render_host_async: order");
+  CUDA_TRY(cudaStreamWaitEvent(sc->copy_stream, sc->render_done[k], 0), "render_host_async: order");
+  CUDA_TRY(cudaMemcpyAsync(rgb_h, drgb, (size_t)n * 12, cudaMemcpyDeviceToHost, sc->copy_stream),
+           "render_host_async: copy rgb");
+  CUDA_TRY(cudaMemcpyAsync(depth_h, ddep, (size_t)n * 4, cudaMemcpyDeviceToHost, sc->copy_stream),
+           "render_host_async: copy depth");
+  CUDA_TRY(cudaMemcpyAsync(opac_h, dop, (size_t)n * 4, cudaMemcpyDeviceToHost, sc->copy_stream),
+           "render_host_async: copy opacity");
+  CUDA_TRY(cudaEventRecord(sc->copy_done[k], sc->copy_stream), "render_host_async: order");
+  return SNISR_OK;
+}
+
+snisr_status snisr_render_host_wait(snisr_scene* sc) {
+  if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;
+  if (!sc->copy_stream) return SNISR_OK;
+  DeviceGuard guard(sc->device);
+  CUDA_TRY(cudaStreamSynchronize(sc->copy_stream), "render_host_wait");
   return SNISR_OK;
 }
 

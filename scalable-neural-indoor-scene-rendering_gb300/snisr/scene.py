@@ -193,6 +193,16 @@ class Scene:
         _lib.check(_lib.lib().snisr_render_host(self._h, C.byref(cam), form, _ptr(rgb_h), _ptr(depth_h),
                                                 _ptr(opac_h), _stream(stream)))
 
+    def render_host_async(self, cam: _lib.Camera, form: int, rgb_h, depth_h, opac_h, stream=None):
+        """Pipelined host-output render (see snisr_render_host_async): the host
+        tensors of a call are complete after the second following call or
+        after render_host_wait()."""
+        _lib.check(_lib.lib().snisr_render_host_async(self._h, C.byref(cam), form, _ptr(rgb_h), _ptr(depth_h),
+                                                      _ptr(opac_h), _stream(stream)))
+
+    def render_host_wait(self):
+        _lib.check(_lib.lib().snisr_render_host_wait(self._h))
+
     def render_rays(self, origins, dirs, form: int = _lib.FORM_TC, stream=None):
         import torch
         n = origins.shape[0]

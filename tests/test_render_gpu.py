@@ -175,3 +175,24 @@ def test_render_cfg2_full_frame_forms_agree(cfg2):
     assert float(np.sqrt(((prgb - trgb) ** 2).mean())) <= TC_RMSE
     assert np.abs(_np(p[2]) - _np(t[2])).max() <= PLAIN_MAX_ABS
     assert (_np(t[2]) > 0.5).mean() > 0.5  # most rays hit a surface
+
+
+def test_render_host_async_matches_device_render(cuda):
+    """The pipelined host-output render writes the same frames as snisr_render."""
+    import torch
+    s = snisr.SynthScene(snisr.CFG1)
+    sc = snisr.Scene(s.desc)
+    try:
+        cams = [s.camera(p) for p in range(4)]
+        n = cams[0].width * cams[0].height
+        hb = [tuple(torch.empty(*shape, pin_memory=True) for shape in ((n, 3), (n,), (n,))) for _ in range(4)]
+        for cam, bufs in zip(cams, hb):
+            sc.render_host_async(cam, snisr.FORM_TC, *bufs)
+        sc.render_host_wait()
+        for cam, bufs in zip(cams, hb):
+            ref = [t.cpu() for t in sc.render(cam, snisr.FORM_TC)]
+            assert float((bufs[0] - ref[0]).abs().max()) <= 1e-6  # colour: atomics in any order
+            assert torch.equal(bufs[1], ref[1]) and torch.equal(bufs[2], ref[2])
+        sc.check()
+    finally:
+        sc.close()
