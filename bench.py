@@ -896,8 +896,9 @@ def main():
     img = TC_IMAGE_BYTES
     mlp_bytes = samples * (GATHER_BYTES_PER_SAMPLE + 32 + 64 + 12) + chunks * img
     # compulsory-bytes variant: every distinct trilinear corner once per frame
-    # (FP16 features + density), plus records, encodings, colours and images
-    mlp_bytes_compulsory = dvert * (32 + 1) * 2 + samples * (32 + 64 + 12) + chunks * img
+    # (FP16 features + density), every sample record once, every ray's view
+    # encoding and colour once, every tile's weight image once
+    mlp_bytes_compulsory = dvert * (32 + 1) * 2 + samples * 32 + n * (64 + 12) + synth.desc.num_tiles * img
     mlp_flop = samples * MLP_FLOP_PER_SAMPLE
     trav_bytes = vsteps * 8 + samples * (32 + 32) + n * (32 + 8)
     t_mlp = stages["mlp_tc"] * 1e-3
