@@ -351,8 +351,11 @@ __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S
 
 // Stage 2: per-tile offsets and 128-sample chunk offsets (one thread; the
 // tile count is small).  Layout after the header: count[NT], off[NT+1],
-// coff[NT+1], cursor[NT].
-__global__ void scan_kernel(int* ctrl, int NT) {
+// coff[NT+1], cursor[NT].  When the frame produced more samples than the
+// buffer holds (the traversal has flagged the overflow), every offset and
+// the chunk count are zero: the scatter stays inside the buffer and the MLP
+// does no work for the invalid frame.
+__global__ void scan_kernel(int* ctrl, int NT, uint32_t cap) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   int* cnt = ctrl + CTRL_HEADER;
   int* off = cnt + NT;
@@ -370,6 +373,10 @@ __global__ void scan_kernel(int* ctrl, int NT) {
   coff[NT] = c;
   ctrl[CTRL_CHUNKS] = c;
   ctrl[CTRL_SAMPLES] = o;
+  if ((uint32_t)o > cap) {
+    for (int t = 0; t <= NT; ++t) off[t] = coff[t] = 0;
+    ctrl[CTRL_CHUNKS] = ctrl[CTRL_SAMPLES] = 0;
+  }
 }
 
 // Stage 3: move samples into per-tile order.  A CTA takes a slab of
@@ -798,7 +805,7 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
                                                                      ws.blk_count, ws.ctrl, depth, opac);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
-  scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles);
+  scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles, ws.cap);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
   scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, kScatThreads, 2 * S.num_tiles * (int)sizeof(uint32_t),

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "kernels.h"
+#include "scan.cuh"
 #include "snisr.h"
 #include "snisr_internal.h"
 #include "tc_ptx.cuh"
@@ -52,94 +53,6 @@ __global__ void sort_hist_kernel(const int16_t* __restrict__ keys, int64_t n, in
   hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];  // digit-major
 }
 
-// Exclusive scan of m values in place, in three launches: per-tile sums
-// (4096 values per 1024-thread block, 4 consecutive values per thread so a
-// warp reads 512 contiguous bytes), one block scanning the tile sums, and a
-// per-tile scan that adds the tile's offset.
-constexpr int kScanThreads = 1024, kScanPer = 4, kScanTile = kScanThreads * kScanPer;
-
-// Exclusive scan of one value per thread over a 1024-thread block; *total
-// receives the block sum.  Uses 33 words of shared memory.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* warp_tot, uint32_t& total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t v = x;
-#pragma unroll
-  for (int s = 1; s < 32; s <<= 1) {
-    const uint32_t u = __shfl_up_sync(kFull, v, s);
-    if (lane >= s) v += u;
-  }
-  if (lane == 31) warp_tot[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = warp_tot[lane];
-#pragma unroll
-    for (int s = 1; s < 32; s <<= 1) {
-      const uint32_t u = __shfl_up_sync(kFull, w, s);
-      if (lane >= s) w += u;
-    }
-    warp_tot[lane] = w;  // inclusive
-    if (lane == 31) warp_tot[32] = w;
-  }
-  __syncthreads();
-  const uint32_t before = (warp > 0 ? warp_tot[warp - 1] : 0u) + v - x;
-  total = warp_tot[32];
-  __syncthreads();
-  return before;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t* __restrict__ v, int64_t m,
-                                                                   uint32_t* sums) {
-  __shared__ uint32_t wt[33];
-  const int64_t b = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
-  uint32_t s = 0;
-#pragma unroll
-  for (int j = 0; j < kScanPer; ++j) s += b + j < m ? v[b + j] : 0u;
-  uint32_t total;
-  block_exclusive_scan(s, wt, total);
-  if (threadIdx.x == 0) sums[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(uint32_t* sums, int nb) {
-  __shared__ uint32_t wt[33];
-  uint32_t carry = 0;
-  for (int base = 0; base < nb; base += kScanThreads) {
-    const int i = base + threadIdx.x;
-    const uint32_t x = i < nb ? sums[i] : 0u;
-    uint32_t total;
-    const uint32_t before = block_exclusive_scan(x, wt, total);
-    if (i < nb) sums[i] = carry + before;
-    carry += total;
-  }
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t* v, int64_t m,
-                                                                  const uint32_t* __restrict__ sums) {
-  __shared__ uint32_t wt[33];
-  const int64_t b = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
-  uint32_t x[kScanPer], s = 0;
-#pragma unroll
-  for (int j = 0; j < kScanPer; ++j) {
-    x[j] = b + j < m ? v[b + j] : 0u;
-    s += x[j];
-  }
-  uint32_t total;
-  uint32_t run = sums[blockIdx.x] + block_exclusive_scan(s, wt, total);
-#pragma unroll
-  for (int j = 0; j < kScanPer; ++j) {
-    if (b + j < m) v[b + j] = run;
-    run += x[j];
-  }
-}
-
-inline int scan_tiles(int64_t m) { return (int)((m + kScanTile - 1) / kScanTile); }
-
-inline void scan_u32(uint32_t* v, int64_t m, uint32_t* sums, cudaStream_t st) {
-  const int nb = scan_tiles(m);
-  if (nb <= 0) return;
-  scan_reduce_kernel<<<nb, kScanThreads, 0, st>>>(v, m, sums);
-  scan_sums_kernel<<<1, kScanThreads, 0, st>>>(sums, nb);
-  scan_apply_kernel<<<nb, kScanThreads, 0, st>>>(v, m, sums);
-}
 
 __global__ void sort_scatter_kernel(const int16_t* __restrict__ kin, const int32_t* __restrict__ vin, int64_t n,
                                     int pass, const uint32_t* __restrict__ offs, int nblocks, int16_t* kout,
@@ -483,7 +396,7 @@ cudaError_t launch_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, 
   const int nblocks = (int)((n + kSortBlock - 1) / kSortBlock);
   const size_t hist_n = (size_t)256 * nblocks;
   // temporaries: keys x2, values, starts copy, flags/positions, histogram, count, scan tile sums
-  const int scan_nb = max(scan_tiles((int64_t)hist_n), scan_tiles(n));
+  const int scan_nb = max(scan::tiles((int64_t)hist_n), scan::tiles(n));
   const size_t bytes = (size_t)n * 2 * 2 + (size_t)n * 4 * 3 + hist_n * 4 + 64 + (size_t)scan_nb * 4 + 16;
   void* tmp = nullptr;
   cudaError_t e = cudaMallocAsync(&tmp, bytes, st);
@@ -503,13 +416,13 @@ cudaError_t launch_sort_by_key(int16_t* keys, int32_t* values, int32_t* starts, 
     if ((e = cudaMemcpyAsync(s_copy, starts, (size_t)n * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) break;
     // pass 0: keys/values -> k1/v1; pass 1: k1/v1 -> k2/values
     sort_hist_kernel<<<nblocks, kSortThreads, 0, st>>>(keys, n, 0, hist, nblocks);
-    scan_u32(hist, (int64_t)hist_n, scan_sums, st);
+    scan::exclusive(hist, (int64_t)hist_n, scan_sums, st);
     sort_scatter_kernel<<<nblocks, kSortThreads, 0, st>>>(keys, values, n, 0, hist, nblocks, k1, v1);
     sort_hist_kernel<<<nblocks, kSortThreads, 0, st>>>(k1, n, 1, hist, nblocks);
-    scan_u32(hist, (int64_t)hist_n, scan_sums, st);
+    scan::exclusive(hist, (int64_t)hist_n, scan_sums, st);
     sort_scatter_kernel<<<nblocks, kSortThreads, 0, st>>>(k1, v1, n, 1, hist, nblocks, k2, values);
     run_flags_kernel<<<g, 256, 0, st>>>(k2, n, pos);
-    scan_u32(pos, n, scan_sums, st);
+    scan::exclusive(pos, n, scan_sums, st);
     run_compact_kernel<<<g, 256, 0, st>>>(k2, s_copy, pos, n, keys, starts);
     run_keys_kernel<<<g, 256, 0, st>>>(k2, pos, n, keys, cnt);
     if ((e = cudaGetLastError()) != cudaSuccess) break;

@@ -196,3 +196,22 @@ def test_render_host_async_matches_device_render(cuda):
         sc.check()
     finally:
         sc.close()
+
+
+def test_sample_buffer_overflow_is_reported_and_contained(cuda):
+    """A frame with more samples than the buffer holds (one slot per ray here)
+    is flagged by snisr_scene_check; the stages after the traversal skip the
+    frame instead of indexing past the buffers, and the scene stays usable."""
+    import torch
+    s = snisr.SynthScene(snisr.CFG2, max_pixels=320 * 180, max_samples_per_ray=1)
+    sc = snisr.Scene(s.desc)
+    try:
+        cam = s.camera(0, 320, 180)
+        sc.render(cam, snisr.FORM_TC)
+        with pytest.raises(snisr.SnisrError):
+            sc.check()
+        torch.cuda.synchronize()
+        sc.render(cam, snisr.FORM_PLAIN_FP32)  # the plain form needs no sample buffer
+        sc.check()
+    finally:
+        sc.close()
