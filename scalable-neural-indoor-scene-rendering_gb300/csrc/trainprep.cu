@@ -161,25 +161,27 @@ __device__ float2 bvh_two_nearest_in_box(const SceneDev& S, const float o[3], co
   return make_float2(near1, near2);
 }
 
+// One thread per ray, looping over its visited tiles (a ray visits a few of
+// its K slots; one thread per slot would leave most lanes of a warp idle).
 __global__ void double_hits_kernel(SceneDev S, const float* __restrict__ ro, const float* __restrict__ rd,
                                    const int32_t* __restrict__ visited, int64_t n, int K, float2* hits) {
   const float hs = fdiv(S.tile_size, 2.0f);
-  const int64_t total = n * K;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    float2 out = make_float2(-1.0f, -1.0f);
-    const int tile = visited[i];
-    if (tile >= 0 && tile < S.num_tiles && S.has_mesh) {
-      const int64_t r = i / K;
-      const float o[3] = {ro[3 * r], ro[3 * r + 1], ro[3 * r + 2]};
-      const float d[3] = {rd[3 * r], rd[3 * r + 1], rd[3 * r + 2]};
-      const float c[3] = {S.tile_center[3 * tile], S.tile_center[3 * tile + 1], S.tile_center[3 * tile + 2]};
-      const float2 t = bvh_two_nearest_in_box(S, o, d, c, hs);
-      if (t.x != SNISR_INF) {
-        out.x = t.x;
-        if (t.y != SNISR_INF) out.y = t.y;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const float o[3] = {ro[3 * r], ro[3 * r + 1], ro[3 * r + 2]};
+    const float d[3] = {rd[3 * r], rd[3 * r + 1], rd[3 * r + 2]};
+    for (int j = 0; j < K; ++j) {
+      float2 out = make_float2(-1.0f, -1.0f);
+      const int tile = visited[r * K + j];
+      if (tile >= 0 && tile < S.num_tiles && S.has_mesh) {
+        const float c[3] = {S.tile_center[3 * tile], S.tile_center[3 * tile + 1], S.tile_center[3 * tile + 2]};
+        const float2 t = bvh_two_nearest_in_box(S, o, d, c, hs);
+        if (t.x != SNISR_INF) {
+          out.x = t.x;
+          if (t.y != SNISR_INF) out.y = t.y;
+        }
       }
+      hits[r * K + j] = out;
     }
-    hits[i] = out;
   }
 }
 
@@ -414,7 +416,7 @@ __global__ void patch_rows_kernel(const int32_t* __restrict__ flags, const int32
 
 cudaError_t launch_double_hits(const SceneDev& S, const float* ro, const float* rd, const int32_t* visited,
                                int64_t n, int K, float* hits, cudaStream_t st) {
-  double_hits_kernel<<<grid_n(n * K, 128), 128, 0, st>>>(S, ro, rd, visited, n, K, reinterpret_cast<float2*>(hits));
+  double_hits_kernel<<<grid_n(n, 128), 128, 0, st>>>(S, ro, rd, visited, n, K, reinterpret_cast<float2*>(hits));
   return cudaGetLastError();
 }
 
