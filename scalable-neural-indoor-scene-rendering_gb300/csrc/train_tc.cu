@@ -450,6 +450,8 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
 // DO the second atom is the next tile, whose products land in accumulator
 // lanes 64..127 (output units that do not exist) and are never read.
 // ---------------------------------------------------------------------------
+constexpr int kBwdRun = 4;
+
 template <int F, int H, int L>
 __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float* __restrict__ vfeat,
                                                         const TrainRecT* __restrict__ recs,
@@ -510,6 +512,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   int cur_tile = -1;
   bool failed = false, have_acc = false;
   const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  int run_c = 0, run_left = 0;
 
   // flush the weight/bias gradient accumulators of `tile` to global memory
   // (lanes = output units: threads 0..fo-1 of the first part)
@@ -532,9 +535,17 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   };
 
   for (;;) {
-    if (tid == 0) *chunk_slot = atomicAdd(work, 1);
-    __syncthreads();
-    const int c = *chunk_slot;
+    // chunks are claimed in runs of kBwdRun consecutive ones (mostly of one
+    // tile), so that the weight-gradient accumulators are flushed less often
+    if (run_left == 0) {
+      if (tid == 0) *chunk_slot = atomicAdd(work, kBwdRun);
+      __syncthreads();
+      run_c = *chunk_slot;
+      run_left = kBwdRun;
+      __syncthreads();  // every thread has read the slot before it is claimed again
+    }
+    const int c = run_c++;
+    --run_left;
     if (c >= total) break;
     const ChunkPos cp = chunk_pos(c, coff, tstart, NT);
     const bool new_w = cp.tile != cur_tile;
