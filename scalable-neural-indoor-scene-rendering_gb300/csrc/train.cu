@@ -191,10 +191,12 @@ __global__ void scan_pass3(const int32_t* cnt, int64_t n, const int32_t* bsum, i
   if (i < n) off[i] = bsum[blockIdx.x] + e;
 }
 
-// per-tile sample ranges (rays sorted by tile): start[t] = off[first ray with tile >= t]
+// per-tile sample ranges (rays sorted by tile): start[t] = off[first ray
+// with tile >= t], by the first block; every block checks its share of the
+// tile-order precondition
 __global__ void tile_ranges_kernel(const int32_t* __restrict__ ray_tile, const int32_t* __restrict__ off, int64_t n,
                                    const int32_t* total, int NT, int64_t cap, int32_t* start, uint32_t* err) {
-  for (int t = threadIdx.x; t <= NT; t += blockDim.x) {
+  for (int t = threadIdx.x; blockIdx.x == 0 && t <= NT; t += blockDim.x) {
     int64_t lo = 0, hi = n;  // first index with ray_tile >= t
     while (lo < hi) {
       int64_t mid = (lo + hi) >> 1;
@@ -204,7 +206,7 @@ __global__ void tile_ranges_kernel(const int32_t* __restrict__ ray_tile, const i
     start[t] = (int32_t)(v < cap ? v : cap);  // records beyond the capacity were not written
   }
   // rays must be grouped by tile (non-decreasing ids)
-  for (int64_t i = threadIdx.x + 1; i < n; i += blockDim.x)
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1; i < n; i += (int64_t)gridDim.x * blockDim.x)
     if (ray_tile[i] < ray_tile[i - 1]) atomicOr(err, ERR_OVERFLOW);
 }
 
@@ -601,7 +603,8 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
   tr_march_kernel<<<gridn(n, mt), mt, 0, st>>>(S, T->dcache, orig, dirs, ray_tile, n, T->cnt, T->off, nullptr,
                                                T->recs, T->cap, 1);
   TR_TRY(cudaGetLastError(), "train: compact");
-  tile_ranges_kernel<<<1, 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->cap, T->tstart, S.err);
+  tile_ranges_kernel<<<gridn(n, 256), 256, 0, st>>>(ray_tile, T->off, n, T->total, S.num_tiles, T->cap, T->tstart,
+                                                     S.err);
   TR_TRY(cudaGetLastError(), "train: tile ranges");
   return SNISR_OK;
 }
