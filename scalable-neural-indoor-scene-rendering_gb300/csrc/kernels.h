@@ -97,6 +97,7 @@ struct TrainTcArgs {
   const float4* dout;
   float* gvfeat;
   float* gmlp;
+  float* gstage;  // [NT][4][64 x 64 + 64] weight-gradient staging of the backward kernel
   int num_sms;
   int fwd_ctas_per_sm;
 };

@@ -510,6 +510,7 @@ struct TrainWS {
   int64_t nvox = 0;
   float4 *c = nullptr, *dout = nullptr;
   float *act = nullptr, *dlt = nullptr;
+  float* gstage = nullptr;     // [NT][4][64 x 64 + 64] staged weight gradients (TC backward)
   void* block = nullptr;
   size_t bytes = 0;
   int64_t last_n = -1;
@@ -529,7 +530,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
               al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al((NT + 2) * 4) + al(16) +
               al(rays * 128) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
-              al((size_t)nvox * 32);
+              al((size_t)nvox * 32) + al((size_t)NT * 4 * (64 * 64 + 64) * 4);
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, sz);
   if (e != cudaSuccess) return set_error(SNISR_OOM, std::string("train workspace: ") + cudaGetErrorString(e));
@@ -551,6 +552,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   T->wimg = (uint8_t*)take((size_t)img_stride * NT);
   T->stage = (TrainRec*)take((size_t)rays * kStage * sizeof(TrainRec));
   T->dcache = (float4*)take((size_t)nvox * 32);
+  T->gstage = (float*)take((size_t)NT * 4 * (64 * 64 + 64) * 4);
   T->nvox = nvox;
   T->img_stride = img_stride;
   T->block = p;
@@ -631,7 +633,7 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   cudaError_t e;
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, nullptr, nullptr, num_sms, ws.tune.train_fwd_ctas_per_sm};
+                  T->c, T->dout, nullptr, nullptr, nullptr, num_sms, ws.tune.train_fwd_ctas_per_sm};
     e = launch_train_tc(S, a, false, st);
     if (e == cudaErrorInvalidValue) return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
   } else if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
@@ -678,7 +680,7 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   if (T->last_form != form) return set_error(SNISR_INVALID_ARG, "train_backward: the forward call used another form");
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, gvfeat, gmlp, num_sms, ws.tune.train_fwd_ctas_per_sm};
+                  T->c, T->dout, gvfeat, gmlp, T->gstage, num_sms, ws.tune.train_fwd_ctas_per_sm};
     e = launch_train_tc(S, a, true, st);
   } else if (F == 32 && H == 64 && L == 3)
     e = train_plain_mlp_bwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->dout, T->act, T->dlt, gvfeat,

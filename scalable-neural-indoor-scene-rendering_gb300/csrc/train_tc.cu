@@ -451,6 +451,34 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
 // lanes 64..127 (output units that do not exist) and are never read.
 // ---------------------------------------------------------------------------
 constexpr int kBwdRun = 4;
+// weight-gradient staging per tile: per layer 64 rows x 64 columns, then 64
+// biases (16-byte aligned rows for vector reductions)
+constexpr int kDwStageLayer = 64 * 64 + 64, kDwStageTile = 4 * kDwStageLayer;
+
+// gmlp[t][P] += the staged weight gradients (one thread per parameter)
+__global__ void apply_dw_kernel(const float* __restrict__ gstage, int NT, int IN, int H, int L, int P,
+                                float* gmlp) {
+  const int64_t total = (int64_t)NT * P;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / P);
+    int j = (int)(idx % P);
+    for (int l = 0; l <= L; ++l) {
+      const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
+      const float* Gl = gstage + (size_t)t * kDwStageTile + (size_t)l * kDwStageLayer;
+      if (j < fi * fo) {
+        gmlp[idx] += Gl[(j / fi) * 64 + j % fi];
+        break;
+      }
+      j -= fi * fo;
+      if (j < fo) {
+        gmlp[idx] += Gl[4096 + j];
+        break;
+      }
+      j -= fo;
+    }
+  }
+}
 
 template <int F, int H, int L>
 __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float* __restrict__ vfeat,
@@ -459,7 +487,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
                                                         const int32_t* __restrict__ coff, int* work,
                                                         const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
                                                         int img_stride, const float4* __restrict__ dout, float* gvfeat,
-                                                        float* gmlp) {
+                                                        float* gstage) {
   constexpr int IN = F + 27;
   constexpr int kTiles = 5 + L;
   const ImageLayout lay(H, L);
@@ -516,21 +544,33 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
 
   // flush the weight/bias gradient accumulators of `tile` to global memory
   // (lanes = output units: threads 0..fo-1 of the first part)
+  // into the aligned staging rows (64 columns per output unit; the input
+  // columns past fi accumulate zeros), by vector reductions: part p adds
+  // columns [32 p, 32 p + 32) of rows 0..fo-1, part 0 the biases
+  (void)IN;
   auto flush = [&](int tile) {
-    float* G = gmlp + (size_t)tile * S.params_per_tile;
-    int64_t off = 0;
+    float* G = gstage + (size_t)tile * kDwStageTile;
     for (int l = 0; l <= L; ++l) {
-      const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
-      float v[64];
-      for (int cc = 0; cc < 64; cc += 16) tc::tmem_ld16(taddr + 64u + 64u * l + cc, v + cc);
-      float bv[4];
-      tc::tmem_ld4(taddr + 64u + 64u * (L + 1) + 16u * l, bv);
-      tc::tmem_wait_ld();
-      if (tid < fo) {
-        for (int i = 0; i < fi; ++i) atomicAdd(G + off + (int64_t)tid * fi + i, v[i]);
-        atomicAdd(G + off + (int64_t)fo * fi + tid, bv[0]);
+      const int fo = l == L ? 3 : H;
+      float* Gl = G + l * kDwStageLayer;
+#pragma unroll
+      for (int cc = 0; cc < 32; cc += 16) {
+        const int col = part * 32 + cc;
+        float v[16];
+        tc::tmem_ld16(taddr + 64u + 64u * l + col, v);
+        tc::tmem_wait_ld();
+        if (row < fo) {
+#pragma unroll
+          for (int q = 0; q < 16; q += 4)
+            red_add_v4(Gl + row * 64 + col + q, v[q], v[q + 1], v[q + 2], v[q + 3]);
+        }
       }
-      off += (int64_t)fi * fo + fo;
+      if (part == 0) {
+        float bv[4];
+        tc::tmem_ld4(taddr + 64u + 64u * (L + 1) + 16u * l, bv);
+        tc::tmem_wait_ld();
+        if (row < fo) atomicAdd(Gl + 4096 + row, bv[0]);
+      }
     }
   };
 
@@ -738,9 +778,15 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
       return cudaFuncSetAttribute(tr_mlp_bwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     });
     if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(a.gstage, 0, (size_t)S.num_tiles * kDwStageTile * sizeof(float), st);
+    if (e != cudaSuccess) return e;
     tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 256, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                          a.work, a.enc, a.wimg, a.img_stride, a.dout, a.gvfeat,
-                                                         a.gmlp);
+                                                         a.gstage);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int64_t np = (int64_t)S.num_tiles * S.params_per_tile;
+    apply_dw_kernel<<<(int)((np + 255) / 256 < 65536 ? (np + 255) / 256 : 65536), 256, 0, st>>>(
+        a.gstage, S.num_tiles, F + 27, H, L, S.params_per_tile, a.gmlp);
   }
   return cudaGetLastError();
 }
