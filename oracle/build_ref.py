@@ -1,12 +1,20 @@
-"""Recipe: compile the reference's header-only helpers for the host.
+"""Recipe: compile the reference's own code for the parity checks.
 
-Reads the reference tree in place (/root/reference, read-only) and writes only
-oracle/_ref/libref.so (git-ignored).  Test infrastructure; the reference's
+1. The reference's header-only helpers for the host: oracle/_ref/libref.so.
+2. The reference's CUDA kernel sources for sm_103a, device code only, one
+   cubin per source file (oracle/_ref/<name>.cubin), with the nvcc flags its
+   torch CUDAExtension builds pass (torch's COMMON_NVCC_FLAGS; no fast math).
+   The cubins carry no host code, so they travel to the GPU host as they are;
+   tests/refgpu.py loads them through the CUDA driver API.
+
+Reads the reference tree in place (/root/reference, read-only) and writes
+only under oracle/_ref/ (git-ignored).  Test infrastructure; the reference's
 own build system is not used.  Skipped (returns None) where the reference
-tree is absent, e.g. on the GPU machine.
+tree is absent, e.g. on the GPU host.
 """
 from __future__ import annotations
 
+import concurrent.futures
 import os
 import subprocess
 
@@ -15,10 +23,71 @@ REF = os.environ.get("SNISR_REFERENCE_TREE", "/root/reference")
 OUT = os.path.join(HERE, "_ref", "libref.so")
 
 
+# cubin name -> reference source file (path within the reference tree)
+CUBINS = {
+    "compute_rays": "rendering/src/compute_rays.cu",
+    "raytile_tracing": "rendering/src/raytile_tracing.cu",
+    "raydiffuse_render_octree_fp16": "rendering/src/raydiffuse_render_octree_fp16.cu",
+    "rayreflection_render": "rendering/src/rayreflection_render.cu",
+    "sampling": "rendering/src/sampling.cu",
+    "volume_rendering": "rendering/src/volume_rendering.cu",
+    "reorder": "rendering/src/reorder.cu",
+    "Sample_kernel": "training/src/Sample_kernel.cu",
+    "Helper_kernel": "training/src/Helper_kernel.cu",
+}
+# rayreflection_render.cu:5-6 include two ATen quantized CPU headers that it
+# does not use and that this torch no longer ships; empty stand-ins are found
+# first on the include path.
+_STUBS = ("ATen/native/quantized/cpu/embedding_packed_params.h", "ATen/native/quantized/cpu/fbgemm_utils.h")
+
+
+def cubin_path(name: str) -> str:
+    return os.path.join(HERE, "_ref", name + ".cubin")
+
+
+def _nvcc_cubin(name: str, src: str, incs: list, flags: list) -> str:
+    out = cubin_path(name)
+    cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-w"] + flags
+    for d in incs:
+        cmd += ["-I", d]
+    cmd += [src, "-o", out + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_cubins(force: bool = False):
+    """The reference's kernels as sm_103a cubins; None without the reference tree."""
+    if not os.path.isdir(os.path.join(REF, "rendering", "src")):
+        return None
+    from torch.utils.cpp_extension import COMMON_NVCC_FLAGS, include_paths
+    import sysconfig
+    stub = os.path.join(HERE, "_ref", "stub")
+    for h in _STUBS:
+        p = os.path.join(stub, h)
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        if not os.path.exists(p):
+            open(p, "w").close()
+    jobs = []
+    for name, rel in CUBINS.items():
+        src = os.path.join(REF, rel)
+        out = cubin_path(name)
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+            continue
+        incs = [stub, os.path.join(os.path.dirname(src), "include")] + list(include_paths()) + \
+            [sysconfig.get_paths()["include"]]
+        jobs.append((name, src, incs))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        for f in [ex.submit(_nvcc_cubin, n, s, i, list(COMMON_NVCC_FLAGS)) for n, s, i in jobs]:
+            f.result()
+    return {n: cubin_path(n) for n in CUBINS}
+
+
 def build(force: bool = False):
     inc = os.path.join(REF, "rendering", "src", "include")
     if not os.path.isdir(inc):
         return None
+    build_cubins(force)
     src = os.path.join(HERE, "ref_harness.cpp")
     if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= os.path.getmtime(src):
         return OUT

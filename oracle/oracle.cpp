@@ -9,6 +9,16 @@
 // specification of the visited-voxel sequence; shading (trilinear, MLP,
 // compositing) runs in float (mode 0) or double (mode 1, the FP64 oracle).
 //
+// The restatements of the reference's own CUDA ops (oracle_op_*, sample_bg,
+// train_tracing) also state the fused multiply-adds of the reference's nvcc
+// build, which contracts a product feeding an add into one fma (the left
+// product when both operands are products: a*b + c*d + e is
+// fma(a, b, c*d) + e).  fmac() below marks each of them; running the
+// reference's compiled kernels on the GPU showed them at these places.
+// The low-level helpers pinned against the reference headers compiled for
+// the host (ray_aabb, voxel traversal of the tile grid in the render path,
+// ray-triangle, FP32 trilinear) stay unfused, like that host build.
+//
 // Reference functions restated (paths inside the reference project):
 //   safe_divide / signf            rendering/src/include/cutil_math.h:856-876
 //   RayAABBIntersection            rendering/src/include/cuda_utils.h:506-598
@@ -35,6 +45,9 @@
 namespace {
 
 const float kInf = 100000000.0f;
+
+// One fused multiply-add, rounded once (a contraction of the reference's build).
+inline float fmac(float a, float b, float c) { return std::fma(a, b, c); }
 
 float f16_to_f32(uint16_t h) {
   uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
@@ -765,7 +778,7 @@ void oracle_op_compute_rays(const float* intr, const float* rot, int H, int W, f
   for (int64_t i = 0; i < (int64_t)H * W; ++i) {
     int py = (int)(i / W), px = (int)(i % W);
     float x = ((float)px - intr[0]) * intr[2], y = ((float)py - intr[1]) * intr[2];
-    for (int a = 0; a < 3; ++a) rays_d[3 * i + a] = (rot[3 * a] * x + rot[3 * a + 1] * y) + rot[3 * a + 2];
+    for (int a = 0; a < 3; ++a) rays_d[3 * i + a] = fmac(rot[3 * a], x, rot[3 * a + 1] * y) + rot[3 * a + 2];
   }
 }
 
@@ -783,7 +796,7 @@ void oracle_op_tracing_tiles(const float* rays_d, int64_t npix, const int32_t* i
       for (int a = 0; a < 3; ++a) { h[a] = ssize[a] / 2.0f; c[a] = smin[a] + h[a]; }
       Bound b = ray_aabb(origin, d, c, h);
       for (int a = 0; a < 3; ++a) {
-        p[a] = p[a] + b.lo * d[a];
+        p[a] = fmac(b.lo, d[a], p[a]);
         p[a] = std::min(std::max(p[a], 0.0f), ssize[a] - 0.000001f);
       }
     }
@@ -814,7 +827,7 @@ void oracle_op_tracing_tiles(const float* rays_d, int64_t npix, const int32_t* i
 static void uniform_v3(float* z, float* dist, float near_, float far_, int n) {
   float interval = (far_ - near_) / (float)n;
   for (int i = 0; i < n; ++i) {
-    z[i] = near_ + (float)i * interval;
+    z[i] = fmac((float)i, interval, near_);
     dist[i] = interval;
   }
 }
@@ -838,7 +851,7 @@ void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const 
     float loc[3], nb[3], tmax[3], tdel[3];
     int cur[3], st[3];
     for (int a = 0; a < 3; ++a) {
-      loc[a] = (o[a] + near_ * d[a]) - minc[a];
+      loc[a] = fmac(near_, d[a], o[a]) - minc[a];
       loc[a] = std::min(std::max(loc[a], 0.0f), tile - 0.000001f);
       cur[a] = std::min(std::max((int)(loc[a] * inv_vs), 0), N - 1);
       st[a] = d[a] >= 0 ? 1 : -1;
@@ -849,7 +862,7 @@ void oracle_op_sample_sparse(const float* ro, const float* rd, int64_t B, const 
     }
     auto vbound = [&]() {
       float vc[3];
-      for (int a = 0; a < 3; ++a) vc[a] = (minc[a] + (float)cur[a] * vs) + 0.5f * vs;
+      for (int a = 0; a < 3; ++a) vc[a] = fmac((float)cur[a], vs, minc[a]) + 0.5f * vs;
       const float h5 = 0.5f * vs;
       const float h3[3] = {h5, h5, h5};
       return ray_aabb(o, d, vc, h3);
@@ -916,10 +929,10 @@ void oracle_op_inverse_z(const float* rays_d, const float* origin, const float* 
   for (int64_t t = 0; t < npix * spr; ++t) {
     int64_t p = t / spr;
     int j = (int)(t % spr);
-    float z = 1.0f / ((float)(offset + j) * inv_bound[p] + inv_near[p]);
-    float zn = 1.0f / ((float)(offset + j + 1) * inv_bound[p] + inv_near[p]);
+    float z = 1.0f / fmac((float)(offset + j), inv_bound[p], inv_near[p]);
+    float zn = 1.0f / fmac((float)(offset + j + 1), inv_bound[p], inv_near[p]);
     steps[t] = std::max(zn - z, 0.0f);
-    for (int a = 0; a < 3; ++a) pts[3 * t + a] = origin[a] + z * rays_d[3 * p + a];
+    for (int a = 0; a < 3; ++a) pts[3 * t + a] = fmac(z, rays_d[3 * p + a], origin[a]);
   }
 }
 
@@ -932,7 +945,7 @@ void oracle_op_integrate(const float* rgba, const float* dz, int64_t npix, float
       const float* v = rgba + (i * 16 + s) * 4;
       float alpha = 1.0f - std::exp((-1.0f * v[3]) * dz[i * 16 + s]);
       float w = alpha * T;
-      for (int a = 0; a < 3; ++a) c[a] = c[a] + w * v[a];
+      for (int a = 0; a < 3; ++a) c[a] = fmac(w, v[a], c[a]);
       T = T * (1.0f - alpha);
     }
     trans[i] = T;
@@ -1190,7 +1203,20 @@ void oracle_op_assign_pixels(const int16_t* net, const int32_t* pixel_starts, co
 namespace {
 constexpr int kSpecIn = 63, kSpecH = 64, kSpecHidden = 5, kSpecOut = 28, kSpecParams = 22556;
 inline float h16(float v) { return round_f16(v); }
-inline float hfma(float a, float b, float c) { return round_f16((float)((double)a * (double)b + (double)c)); }
+// double -> FP16, round to nearest even (one rounding)
+inline float round_f16_d(double x) {
+  if (x == 0.0 || !std::isfinite(x)) return round_f16((float)x);
+  const double ax = std::fabs(x);
+  int e;
+  std::frexp(ax, &e);
+  const int lead = std::max(e - 1, -14);
+  const double q = std::ldexp(1.0, lead - 10);
+  double r = std::nearbyint(ax / q) * q;
+  if (r > 65504.0) r = INFINITY;
+  return (float)std::copysign(r, x);
+}
+// FP16 fused multiply-add, rounded once
+inline float hfma(float a, float b, float c) { return round_f16_d((double)a * (double)b + (double)c); }
 inline float hmul(float a, float b) { return round_f16((float)((double)a * (double)b)); }
 inline float hadd(float a, float b) { return round_f16((float)((double)a + (double)b)); }
 inline float hsub(float a, float b) { return round_f16((float)((double)a - (double)b)); }
@@ -1330,8 +1356,10 @@ namespace {
 // 1/(z + tile entry) and the tile's group; with soft_hit a pixel without a
 // first hit takes the last examined tile's group and 1/(its exit distance)
 // (:223-228).  Each FP16 operation rounds once
-// (round to nearest even); hexp is exp rounded to FP16.  FP32 position
-// arithmetic is written without fused multiply-adds.  Reads outside a node's
+// (round to nearest even); hexp is exp rounded to FP16.  The fused
+// multiply-adds of the compiled reference are stated: FP32 positions (entry
+// point, sample point, dilated corner), each linear interpolation
+// (fma(v1, 1 - x, v2 * x) in FP16) and the colour accumulation.  Reads outside a node's
 // 18^3 grid (not reached by in-block samples) are skipped.
 struct OctreeView {
   const int32_t* group_map;    // [NT]
@@ -1375,7 +1403,7 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
     float ro[3];
     for (int a = 0; a < 3; ++a) {
       const float corner = c[a] - hs;
-      ro[a] = (o[a] + b.lo * d[a]) - corner;
+      ro[a] = fmac(b.lo, d[a], o[a]) - corner;
       ro[a] = std::min(std::max(ro[a], 0.0f), V.tile_size - 0.00001f);
     }
     // block DDA (raydiffuse_render_octree_fp16.cu:39-131)
@@ -1400,13 +1428,13 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
         const uint8_t* flags = V.sample_flag + (int64_t)nidx * D3;
         const uint16_t* vox = V.data + 4 * V.vstart[nidx];
         float dc[3];
-        for (int a = 0; a < 3; ++a) dc[a] = (float)cb[a] * bs - V.voxel_size;
+        for (int a = 0; a < 3; ++a) dc[a] = fmac((float)cb[a], bs, -V.voxel_size);
         float z = near_;
         while (z < far_) {
           float pts[3], rel[3];
           int vl[3];
           for (int a = 0; a < 3; ++a) {
-            pts[a] = ro[a] + z * d[a];
+            pts[a] = fmac(z, d[a], ro[a]);
             rel[a] = (pts[a] - dc[a]) * inv_vs;
             vl[a] = (int)rel[a];
           }
@@ -1423,7 +1451,7 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
           float f[3];
           int x0[3];
           for (int a = 0; a < 3; ++a) {
-            f[a] = rel[a] - 0.5f;
+            f[a] = rel[a] - 0.5f;  // the product is shared with vl: not fused
             x0[a] = (int)f[a];
           }
           bool ok = true;
@@ -1438,9 +1466,9 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
               const int idx = nodes[xi * DD + yi * D + zi];
               for (int q = 0; q < 4; ++q) v[k][q] = f16_to_f32(vox[4 * (int64_t)idx + q]);
             }
-            auto lerp = [](float a, float bb, float x) {
-              return hadd(hmul(a, h16(1.0f - x)), hmul(bb, h16(x)));
-            };
+            // half_interpolate1D, v1 * (1 - x) + v2 * x: the compiled reference
+            // fuses the left product into the add (one FP16 rounding less)
+            auto lerp = [](float a, float bb, float x) { return hfma(a, h16(1.0f - x), hmul(bb, h16(x))); };
             float rgba[4];
             for (int q = 0; q < 4; ++q) {
               const float s0 = lerp(lerp(v[0][q], v[1][q], w[0]), lerp(v[2][q], v[3][q], w[0]), w[1]);
@@ -1451,7 +1479,7 @@ void octree_pixel(const OctreeView& V, const float o[3], const float d[3], const
             const float step_h = h16(interval);
             const float alpha = hsub(1.0f, hexp16(hmul(hmul(rgba[3], -1.0f), step_h)));
             const float wgt = hmul(alpha, T);
-            for (int a = 0; a < 3; ++a) col[a] = hadd(col[a], hmul(wgt, rgba[a]));
+            for (int a = 0; a < 3; ++a) col[a] = hfma(wgt, rgba[a], col[a]);  // color + weight * rgb, fused
             T = hmul(T, hsub(1.0f, alpha));
           }
           z = z + V.sample_step;
@@ -1505,7 +1533,9 @@ void oracle_op_rendering_diffuse_octree(const float* rays_d, const int32_t* visi
 //     the voxel centres given): block maximum, exp(-s) > th -> -1, 3^3 max
 //     filter of T_voxels <= T_th -> -1, then dilate_boundary.
 //   pack_occupancy: flags == 1 of the inner N^3 as 64-bit words.
-// Float operations round one at a time (no fused multiply-add); exp is
+// Float operations round one at a time except for the fused multiply-adds of
+// the compiled reference (fmac: sample positions, the cell coordinate and
+// the trilinear density sum of the statistic); exp is
 // std::exp in single precision.
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -1531,7 +1561,7 @@ void oracle_op_transparency_statistic(const float* ro, const float* rd, int64_t 
       float pts[3];
       int p[3];
       for (int a = 0; a < 3; ++a) {
-        pts[a] = o[a] + z * d[a];
+        pts[a] = fmac(z, d[a], o[a]);
         p[a] = (int)((pts[a] - dcorner[a]) * inv_vs);
       }
       if (p[0] < 0 || p[1] < 0 || p[2] < 0 || p[0] >= D || p[1] >= D || p[2] >= D ||
@@ -1543,7 +1573,7 @@ void oracle_op_transparency_statistic(const float* ro, const float* rd, int64_t 
       int x0[3];
       bool ok = true;
       for (int a = 0; a < 3; ++a) {
-        const float f = (pts[a] - tcorner[a]) * inv_vs + 0.5f;
+        const float f = fmac(pts[a] - tcorner[a], inv_vs, 0.5f);
         x0[a] = (int)f;
         x[a] = f - (float)x0[a];
         ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
@@ -1562,7 +1592,8 @@ void oracle_op_transparency_statistic(const float* ro, const float* rd, int64_t 
         const float t = T * w[k];
         float& slot = T_voxels[v000 + off[k]];
         if (t > slot) slot = t;
-        s = k == 0 ? sigma[v000] * w[0] : s + sigma[v000 + off[k]] * w[k];
+        if (k == 1) s = fmac(sigma[v000], w[0], sigma[v000 + off[1]] * w[1]);
+        else if (k > 1) s = fmac(sigma[v000 + off[k]], w[k], s);
       }
       const float alpha = 1.0f - std::exp((-1.0f * s) * step);
       T = T * (1.0f - alpha);
@@ -1703,7 +1734,7 @@ void oracle_train_tracing(const float* ro, const float* rd, int64_t n, const int
     for (int a = 0; a < 3; ++a) p[a] = o[a] - smin[a];
     if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
       const Bound b = ray_aabb(o, d, c, h);
-      for (int a = 0; a < 3; ++a) p[a] = p[a] + b.lo * d[a];
+      for (int a = 0; a < 3; ++a) p[a] = fmac(b.lo, d[a], p[a]);
     }
     for (int a = 0; a < 3; ++a) p[a] = std::max(0.0f, std::min(p[a], size[a] - 0.000001f));
     // voxel_traversal with the start cell clamped into the grid (p / tile can
@@ -1906,7 +1937,7 @@ void oracle_sample_bg(const float* ro, const float* rd, const float* bgz, int64_
       far_ = near_ + range;
     }
     const float interval = (far_ - near_) / (float)(ns - 1);
-    for (int k = 0; k < ns; ++k) z[i * ns + k] = near_ + (float)k * interval;
+    for (int k = 0; k < ns; ++k) z[i * ns + k] = fmac((float)k, interval, near_);
   }
 }
 

@@ -1,9 +1,18 @@
 // Device-side scene view and ray traversal shared by the GB300 kernels.
 //
 // Traversal arithmetic is written with explicit round-to-nearest intrinsics
-// (__fadd_rn, __fmul_rn, __fdiv_rn) so that no multiply-add is contracted:
-// the visited voxel sequence is then bit-identical to an IEEE single
-// precision evaluation of the same expressions on the host.
+// (__fadd_rn, __fmul_rn, __fdiv_rn) so that no multiply-add is contracted
+// behind our back: the visited voxel sequence is then bit-identical to an
+// IEEE single precision evaluation of the same expressions on the host.
+//
+// The drop-ins of the reference's own CUDA ops (ops.cu, prune.cu, octree.cu)
+// also reproduce the fused multiply-adds that the reference's nvcc build
+// forms (its default contraction: a product feeding an add becomes one fma,
+// the left product when both operands are products, e.g. a*b + c*d + e ->
+// fma(a, b, c*d) + e; a product that has a second use stays unfused).  They
+// write those with ffma() at exactly the places where the compiled reference
+// kernels have them, as measured by running those kernels bit-for-bit
+// against these drop-ins.
 #pragma once
 
 #include <cstdint>
@@ -27,6 +36,7 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 // reference safe_divide (rendering/src/include/cutil_math.h:867-869)
 __device__ __forceinline__ float safe_div(float a, float b) { return b != 0.0f ? __fdiv_rn(a, b) : SNISR_INF; }
 

@@ -8,10 +8,12 @@
 // transmittance; the first sample with transmittance below trans_th records
 // 1/(z + tile entry) and the tile's group; with soft_hit a pixel without a
 // first hit takes the last examined tile's group and 1/(its exit distance)
-// (:223-228).  Every FP16 and FP32 operation
-// rounds on its own (the _rn intrinsics keep the compiler from contracting a
-// multiply and an add into one fused operation; the reference's build may
-// fuse some of them, which changes results by FP16 ulps).  The camera origin is a
+// (:223-228).  Every FP16 and FP32 operation rounds on its own (the _rn
+// intrinsics keep the compiler from contracting a multiply and an add behind
+// our back) except where the reference's nvcc build fuses them, which is
+// written out: the FP32 entry point, sample point and dilated block corner,
+// every FP16 linear interpolation (fma(v1, 1 - x, v2 * x)) and the colour
+// accumulation (fma(weight, rgb, colour)).  The camera origin is a
 // kernel argument (the reference keeps it in a __constant__ symbol) and the
 // stream is the caller's.  Tile ids outside [0, num_tiles) and reads outside
 // a node's dilated grid are skipped.
@@ -29,10 +31,11 @@ namespace {
 
 constexpr int kOctBlocks = 4;
 
-// a * (1 - x) + b * x on both FP16 lanes (r, g) or (b, a): the same
-// per-lane operations and roundings as the scalar form, half the instructions
+// a * (1 - x) + b * x on both FP16 lanes (r, g) or (b, a), with the left
+// product fused into the add as in the compiled reference: the same per-lane
+// operations and roundings as the scalar form, half the instructions
 __device__ __forceinline__ __half2 hlerp2(__half2 a, __half2 b, __half2 one_minus_x, __half2 x) {
-  return __hadd2_rn(__hmul2_rn(a, one_minus_x), __hmul2_rn(b, x));
+  return __hfma2(a, one_minus_x, __hmul2_rn(b, x));
 }
 
 __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const int32_t* __restrict__ visited,
@@ -76,7 +79,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
       float tmax[3], tdel[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        ro[a] = fsub(fadd(o[a], fmul(b.x, d[a])), fsub(c[a], hs));
+        ro[a] = fsub(ffma(b.x, d[a], o[a]), fsub(c[a], hs));
         ro[a] = fminf(fmaxf(ro[a], 0.0f), fsub(tile_size, 0.00001f));
         cb[a] = (int)fmul(ro[a], inv_bs);
         st[a] = d[a] >= 0.0f ? 1 : -1;
@@ -97,14 +100,14 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
           const uint2* vox = data + vstart[nidx];
           float dc[3];
 #pragma unroll
-          for (int a = 0; a < 3; ++a) dc[a] = fsub(fmul((float)cb[a], bs), voxel_size);
+          for (int a = 0; a < 3; ++a) dc[a] = ffma((float)cb[a], bs, -voxel_size);
           float z = near_;
           while (z < far_) {
             float rel[3];
             int vl[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-              rel[a] = fmul(fsub(fadd(ro[a], fmul(z, d[a])), dc[a]), inv_vs);
+              rel[a] = fmul(fsub(ffma(z, d[a], ro[a]), dc[a]), inv_vs);
               vl[a] = (int)rel[a];
             }
             const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;
@@ -122,7 +125,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
             bool ok = true;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-              f[a] = fsub(rel[a], 0.5f);
+              f[a] = fsub(rel[a], 0.5f);  // the product is shared with vl: not fused
               x0[a] = (int)f[a];
               ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
             }
@@ -157,7 +160,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
                   __hsub_rn(one, hexp(__hmul_rn(__hmul_rn(rgba[3], __float2half(-1.0f)), __float2half(interval))));
               const __half wgt = __hmul_rn(alpha, T);
 #pragma unroll
-              for (int a = 0; a < 3; ++a) col[a] = __hadd_rn(col[a], __hmul_rn(wgt, rgba[a]));
+              for (int a = 0; a < 3; ++a) col[a] = __hfma(wgt, rgba[a], col[a]);
               T = __hmul_rn(T, __hsub_rn(one, alpha));
             }
             z = fadd(z, sample_step);

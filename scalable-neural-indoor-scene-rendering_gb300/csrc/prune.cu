@@ -20,8 +20,9 @@
 // cell at the reference's step of 0.1 voxel: a tenth of the atomics, same
 // result because a maximum does not depend on grouping).  All values are
 // transmittances times weights, never negative, so the atomic is a signed
-// integer max on their bit patterns.  Positions use non-contracting FP32
-// arithmetic; the density exponential is expf, as in the reference.
+// integer max on their bit patterns.  Positions and the trilinear density
+// use the fused multiply-adds of the compiled reference (ffma), the density
+// exponential is expf, as in the reference.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -70,7 +71,7 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
       int p[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        pts[a] = fadd(o[a], fmul(z, d[a]));
+        pts[a] = ffma(z, d[a], o[a]);
         p[a] = (int)fmul(fsub(pts[a], dcorner[a]), inv_vs);
       }
       if (p[0] < 0 || p[1] < 0 || p[2] < 0 || p[0] >= D || p[1] >= D || p[2] >= D ||
@@ -83,7 +84,7 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
       bool ok = true;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        f[a] = fadd(fmul(fsub(pts[a], tcorner[a]), inv_vs), 0.5f);
+        f[a] = ffma(fsub(pts[a], tcorner[a]), inv_vs, 0.5f);
         x0[a] = (int)f[a];
         x[a] = fsub(f[a], (float)x0[a]);
         ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
@@ -116,9 +117,10 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
 #pragma unroll
         for (int k = 0; k < 8; ++k) m[k] = fmaxf(m[k], fmul(T, w[k]));
       }
-      float s = fmul(__ldg(sigma + v000 + off[0]), w[0]);
+      // v0*w0 + v1*w1 + ... + v7*w7 compiles to fma(v0, w0, v1*w1), then fma(vk, wk, s)
+      float s = ffma(__ldg(sigma + v000 + off[0]), w[0], fmul(__ldg(sigma + v000 + off[1]), w[1]));
 #pragma unroll
-      for (int k = 1; k < 8; ++k) s = fadd(s, fmul(__ldg(sigma + v000 + off[k]), w[k]));
+      for (int k = 2; k < 8; ++k) s = ffma(__ldg(sigma + v000 + off[k]), w[k], s);
       const float alpha = fsub(1.0f, expf(fmul(fmul(-1.0f, s), step)));
       T = fmul(T, fsub(1.0f, alpha));
       if (T < 0.00000001f) break;

@@ -94,7 +94,7 @@ __global__ void train_tracing_kernel(const float* __restrict__ ro, const float* 
     if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
       const float2 b = slab(o, d, c, h);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) p[a] = fadd(p[a], fmul(b.x, d[a]));
+      for (int a = 0; a < 3; ++a) p[a] = ffma(b.x, d[a], p[a]);
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) p[a] = fmaxf(0.0f, fminf(p[a], fsub(size[a], 0.000001f)));
@@ -325,7 +325,7 @@ __global__ void sample_bg_kernel(const float* __restrict__ ro, const float* __re
       far_ = fadd(near_, range);
     }
     const float interval = fdiv(fsub(far_, near_), (float)(ns - 1));
-    for (int k = 0; k < ns; ++k) z[i * ns + k] = fadd(near_, fmul((float)k, interval));
+    for (int k = 0; k < ns; ++k) z[i * ns + k] = ffma((float)k, interval, near_);
   }
 }
 

@@ -1,0 +1,329 @@
+"""The drop-ins against the reference's own CUDA kernels on the GPU.
+
+The reference kernels run from the cubins that oracle/build_ref.py compiles
+from the reference's sources (tests/refgpu.py loads and launches them with
+the reference host wrappers' launch shapes and arguments).  Each test feeds
+the same device tensors to a reference kernel and to the libsnisr drop-in
+(and, where the oracle has the op, to the oracle) and compares.  Skipped
+where the cubins were not built (no reference tree when the extension was
+built)."""
+import numpy as np
+import pytest
+
+import oracle
+import snisr
+from snisr import octree, ops
+
+import refgpu
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not refgpu.available("compute_rays"), reason="reference cubins not built")]
+
+
+def _t(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _n(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy()
+
+
+def _ulps(a, b):
+    """Largest distance in units of the last place between two float32 arrays."""
+    ia = np.ascontiguousarray(a, np.float32).view(np.int32).astype(np.int64)
+    ib = np.ascontiguousarray(b, np.float32).view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7FFFFFFF), ia)
+    ib = np.where(ib < 0, -(ib & 0x7FFFFFFF), ib)
+    return int(np.abs(ia - ib).max()) if ia.size else 0
+
+
+def _report(name, got, ref):
+    same = float((got == ref).mean())
+    print(f"{name}: identical {same:.6f}, max-abs {float(np.abs(got.astype(np.float64) - ref).max()):.3g}, "
+          f"max-ulp {_ulps(got, ref) if got.dtype == np.float32 else '-'}")
+    return same
+
+
+def _cam_inputs(s, pose, W, H):
+    cam = s.camera(pose, W, H)
+    intr = np.array([cam.cx, cam.cy, cam.inv_focal], np.float32)
+    rot = np.array([[cam.c2w[4 * r + c] for c in range(3)] for r in range(3)], np.float32)
+    origin = np.array([cam.c2w[3], cam.c2w[7], cam.c2w[11]], np.float32)
+    return intr, rot, origin
+
+
+@pytest.fixture(scope="module")
+def scene16(cuda):
+    return snisr.SynthScene(snisr.CFG2.replace(res=64, with_mesh=False))
+
+
+def test_compute_rays(scene16):
+    import torch
+    H, W = 180, 320
+    intr, rot, _ = _cam_inputs(scene16, 0, W, H)
+    ref = torch.full((H, W, 3), -1.0, device="cuda")
+    got = torch.full((H, W, 3), -1.0, device="cuda")
+    refgpu.compute_rays(intr, rot, 256, ref)
+    ops.compute_rays(_t(intr), _t(rot), 256, got)
+    r, g = _n(ref), _n(got)
+    _report("compute_rays ours vs reference", g, r)
+    o = oracle.op_compute_rays(intr, rot, H, W).reshape(H, W, 3)
+    _report("compute_rays oracle vs reference", o, r)
+    assert np.array_equal(g, r) and np.array_equal(o, r)
+
+
+@pytest.mark.parametrize("inside", [True, False])
+def test_tracing_tiles(scene16, inside):
+    import torch
+    H, W, K = 144, 256, 30
+    intr, rot, origin = _cam_inputs(scene16, 1, W, H)
+    if not inside:
+        origin = np.array([-2.0, 5.5, 1.4], np.float32)
+    rays = torch.empty((H, W, 3), device="cuda")
+    refgpu.compute_rays(intr, rot, 256, rays)
+    d = scene16.desc
+    imap = np.asarray(scene16.arrays()["tile_index"], np.int32)
+    shape = np.array(list(d.grid), np.int32)
+    smin = np.zeros(3, np.float32)
+    ssize = shape.astype(np.float32) * np.float32(d.tile_size)
+    ref = torch.empty((H, W, K), dtype=torch.int32, device="cuda")
+    got = torch.empty((H, W, K), dtype=torch.int32, device="cuda")
+    refgpu.tracing_tiles(rays, _t(imap), origin, shape, smin, ssize, float(d.tile_size), 256, ref)
+    ops.tracing_tiles(rays, _t(imap), _t(origin), _t(shape), _t(smin), _t(ssize), float(d.tile_size), 256, got)
+    r, g = _n(ref), _n(got)
+    print(f"tracing_tiles ({'inside' if inside else 'outside'}): rays identical {float((g == r).all(-1).mean()):.6f}")
+    assert (r[..., 0] >= 0).mean() > 0.5
+    assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("soft", [False, True], ids=["hard", "soft"])
+def test_octree_diffuse(scene16, soft):
+    import torch
+    th = 0.0 if soft else 0.8
+    D = octree.from_synth(scene16, groups=4)
+    der = octree.derived(D)
+    T = octree.to_device(D)
+    H, W = 240, 320
+    intr, rot, origin = _cam_inputs(scene16, 1, W, H)
+    rays = torch.empty((H, W, 3), device="cuda")
+    refgpu.compute_rays(intr, rot, 256, rays)
+    vis = torch.empty((H, W, 30), dtype=torch.int32, device="cuda")
+    refgpu.tracing_tiles(rays, T["tile_IndexMap"], origin, D["tile_shape"], D["scene_min_corner"],
+                         der["scene_size"].astype(np.float32), der["tile_size"], 256, vis)
+    outs = {}
+    for who in ("ref", "ours"):
+        frame = torch.full((H, W, 3), -1.0, device="cuda")
+        inv = torch.full((H, W), 1e-8, device="cuda")
+        net = torch.full((H, W), -1, dtype=torch.int16, device="cuda")
+        args = (rays, vis)
+        common = (T["tile2group"], T["data_voxels"], T["block_IndexMap"], T["nodes_IndexMap"],
+                  T["nodes_sampleFlag"], T["voxels_start"], T["centers"], der["tile_size"], der["voxel_size"],
+                  der["sample_step"], der["block_num_voxel"], 256, th, 0.01, soft, frame, inv, net)
+        if who == "ref":
+            refgpu.rendering_diffuse_octree_fp16(*args, origin, *common)
+        else:
+            ops.rendering_diffuse_octree_fp16(*args, _t(origin), *common)
+        outs[who] = (_n(frame), _n(inv), _n(net))
+    (fr, ir, nr), (fg, ig, ng) = outs["ref"], outs["ours"]
+    _report(f"octree colour ({'soft' if soft else 'hard'})", fg, fr)
+    _report("octree inverse near", ig, ir)
+    print(f"octree network ids identical {float((ng == nr).mean()):.6f}, hit {float((nr >= 0).mean()):.3f}")
+    assert (nr >= 0).mean() > 0.3
+    assert np.array_equal(fg, fr) and np.array_equal(ig, ir) and np.array_equal(ng, nr)
+
+
+def test_inverse_z_sampling(cuda):
+    import torch
+    rng = np.random.default_rng(6)
+    H, W, spr = 60, 80, 16
+    rays_d = _t(rng.standard_normal((H, W, 3)).astype(np.float32))
+    inv_near_np = (1.0 / rng.uniform(0.3, 4.0, (H, W))).astype(np.float32)
+    inv_bound = _t(((1.0 / (1.0 / inv_near_np + np.float32(8.0)) - inv_near_np) / 63).astype(np.float32))
+    inv_near = _t(inv_near_np)
+    origin = np.array([0.3, -0.2, 1.1], np.float32)
+    for off in (0, 16, 48):
+        res = {}
+        for who in ("ref", "ours"):
+            pts = torch.full((H, W, spr, 3), -1.0, device="cuda")
+            steps = torch.zeros((H, W, spr), device="cuda")
+            if who == "ref":
+                refgpu.inverse_z_sampling(origin, rays_d, inv_near, inv_bound, 256, off, spr, pts, steps)
+            else:
+                ops.inverse_z_sampling(_t(origin), rays_d, inv_near, inv_bound, 256, off, spr, pts, steps)
+            res[who] = (_n(pts), _n(steps))
+        _report(f"inverse_z points (offset {off})", res["ours"][0], res["ref"][0])
+        _report(f"inverse_z steps (offset {off})", res["ours"][1], res["ref"][1])
+        assert np.array_equal(res["ours"][0], res["ref"][0]) and np.array_equal(res["ours"][1], res["ref"][1])
+
+
+def test_integrate_points(cuda):
+    rng = np.random.default_rng(7)
+    H, W = 40, 50
+    rgba = _t(rng.random((H, W, 16, 4)).astype(np.float32) * np.array([1, 1, 1, 5], np.float32))
+    dz = _t((rng.random((H, W, 16)) * 0.3).astype(np.float32))
+    trans = np.ones((H, W, 1), np.float32)
+    trans.reshape(-1)[::11] = 1e-4
+    frame = (rng.random((H, W, 3)) * 0.1).astype(np.float32)
+    tr, fr, tg, fg = _t(trans), _t(frame), _t(trans), _t(frame)
+    refgpu.integrate_points(rgba, dz, 512, 1e-3, tr, fr)
+    ops.integrate_points(rgba, dz, 512, 1e-3, tg, fg)
+    _report("integrate_points colour", _n(fg), _n(fr))
+    _report("integrate_points transmittance", _n(tg), _n(tr))
+    assert np.array_equal(_n(fg), _n(fr)) and np.array_equal(_n(tg), _n(tr))
+
+
+def test_assign_pixels(cuda):
+    import torch
+    rng = np.random.default_rng(2)
+    num_net = 37
+    counts = rng.integers(1, 300, num_net)
+    ps = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    bs = np.concatenate([[0], np.cumsum(np.ceil(counts / 64))]).astype(np.int32)
+    nets = rng.permutation(np.arange(num_net)).astype(np.int16)
+    nb = int(bs[-1])
+    out = {}
+    for who in ("ref", "ours"):
+        nn_ = torch.full((nb,), -5, dtype=torch.int16, device="cuda")
+        np_ = torch.full((nb,), -5, dtype=torch.int32, device="cuda")
+        (refgpu.assign_pixels if who == "ref" else ops.assign_pixels)(_t(nets), _t(ps), _t(bs), 64, nn_, np_)
+        out[who] = (_n(nn_), _n(np_))
+    assert np.array_equal(out["ours"][0], out["ref"][0]) and np.array_equal(out["ours"][1], out["ref"][1])
+
+
+def test_inference_mlp(cuda):
+    import torch
+    from snisr import spec_synth as sp
+    P = sp.problem(3)
+    npix, spr = P["npix"], P["spr"]
+    net_t = _t(P["net"])
+    keys = net_t.clone()
+    q = torch.arange(npix, dtype=torch.int32, device="cuda")
+    ps = torch.arange(npix, dtype=torch.int32, device="cuda")
+    num_net = ops.sort_by_key(keys, q, ps)
+    end = torch.full((1,), npix, dtype=torch.int32, device="cuda")
+    counts = torch.cat([ps[1:num_net], end]) - ps[:num_net]
+    ps2 = torch.cat([ps[:num_net], end])
+    bs = torch.cat([torch.zeros(1, dtype=torch.int32, device="cuda"), torch.cumsum(torch.ceil(counts / 64), 0).int()])
+    nb = int(bs[-1])
+    new_net = torch.empty(nb, dtype=torch.int16, device="cuda")
+    new_ps = torch.empty(nb, dtype=torch.int32, device="cuda")
+    ops.assign_pixels(keys[:num_net].contiguous(), ps2, bs, 64, new_net, new_ps)
+    new_ps = torch.cat([new_ps, end])
+    inv_near = P["inv_near"]
+    inv_bound = ((1.0 / (1.0 / inv_near + P["far"]) - inv_near) / 63).astype(np.float32)
+    pts, _ = oracle.op_inverse_z(P["rays_d"], P["origin"], inv_near, inv_bound, 0, spr)
+    samples = _t(pts.reshape(npix, spr, 3).astype(np.float32))
+    args = (new_net, _t(P["transparency"]), q, new_ps, _t(P["centers"]), samples, _t(P["rays_d"]), _t(P["params"]))
+    sent = -7.0
+    res = {}
+    for who in ("ref", "ours"):
+        out = _t(np.full((npix, spr, 4), sent, np.float32))
+        (refgpu.inference_mlp if who == "ref" else ops.inference_mlp)(
+            spr, nb, 64, float(P["inverse_far"]), float(P["trans_stop"]), *args, out)
+        res[who] = _n(out)
+    ops.check_errors()
+    r, g = res["ref"], res["ours"]
+    wrote = r[..., 0] != sent
+    assert np.array_equal(wrote, g[..., 0] != sent)
+    o16 = np.full((npix, spr, 4), sent, np.float32)
+    qo, nno, npo = q.cpu().numpy(), new_net.cpu().numpy(), new_ps.cpu().numpy()
+    oracle.op_inference_mlp(spr, nb, P["inverse_far"], P["trans_stop"], nno, P["transparency"], qo, npo,
+                            P["centers"], pts.reshape(npix, spr, 3).astype(np.float32), P["rays_d"],
+                            P["params"].view(np.uint16), o16, 0)
+    rr, gg, oo = r[wrote], g[wrote], o16[wrote]
+    rm_ours = float(np.sqrt(((gg[:, :3] - rr[:, :3]) ** 2).mean()))
+    rm_orc = float(np.sqrt(((oo[:, :3] - rr[:, :3]) ** 2).mean()))
+    print(f"inference_mlp: {int(wrote.sum())} samples; colour RMSE ours (tcgen05, FP32 accumulation) vs reference "
+          f"(scalar FP16) {rm_ours:.3g}, max-abs {float(np.abs(gg[:, :3] - rr[:, :3]).max()):.3g}; oracle FP16 "
+          f"restatement vs reference RMSE {rm_orc:.3g}, identical {float((oo == rr).all(-1).mean()):.4f}; density "
+          f"max-abs ours {float(np.abs(gg[:, 3] - rr[:, 3]).max()):.3g}")
+    assert rm_ours <= 1e-3
+
+
+def test_sample_sparse(cuda):
+    import torch
+    s = snisr.SynthScene(snisr.CFG1)
+    a = s.arrays()
+    N = s.desc.res
+    bits = np.unpackbits(a["occupancy"].view(np.uint8), bitorder="little")[: N ** 3]
+    flags = _t(bits.astype(np.int16).reshape(N, N, N))
+    rng = np.random.default_rng(5)
+    B, ns = 4096, 64
+    ro = _t(np.concatenate([rng.uniform(0.2, 1.8, (B // 2, 3)), rng.uniform(-1.0, 3.0, (B // 2, 3))]).astype(np.float32))
+    rdn = rng.standard_normal((B, 3)).astype(np.float32)
+    rdn /= np.linalg.norm(rdn, axis=1, keepdims=True)
+    rdn[::17, 1] = 0.0
+    rd = _t(rdn)
+    res = {}
+    for who in ("ref", "ours"):
+        z = torch.full((B, ns), -1.0, device="cuda")
+        dd = torch.full((B, ns), -1.0, device="cuda")
+        (refgpu.Sample_sparse if who == "ref" else ops.Sample_sparse)(ro, rd, flags, 1.0, 1.0, 1.0, 2.0, N, z, dd)
+        res[who] = (_n(z), _n(dd))
+    _report("Sample_sparse z", res["ours"][0], res["ref"][0])
+    _report("Sample_sparse dists", res["ours"][1], res["ref"][1])
+    assert (res["ref"][0][:, 0] != -1).sum() > 100
+    assert np.array_equal(res["ours"][0], res["ref"][0]) and np.array_equal(res["ours"][1], res["ref"][1])
+
+
+def test_sample_bg(cuda):
+    import torch
+    rng = np.random.default_rng(9)
+    n, ns = 4096, 16
+    center = np.array([1.5, 4.5, 1.5], np.float32)
+    ro = _t((center + rng.uniform(-6, 6, (n, 3))).astype(np.float32))
+    rd = _t(rng.standard_normal((n, 3)).astype(np.float32))
+    bgn = rng.uniform(0.0, 12.0, (n, 1)).astype(np.float32)
+    bgn[::7] = -1.0
+    bg = _t(bgn)
+    res = {}
+    for who in ("ref", "ours"):
+        z = torch.full((n, ns), -1.0, device="cuda")
+        (refgpu.Sample_bg if who == "ref" else ops.Sample_bg)(ro, rd, bg, _t(center), 3.0, 0.6, z)
+        res[who] = _n(z)
+    _report("Sample_bg", res["ours"], res["ref"])
+    assert np.array_equal(res["ours"], res["ref"])
+
+
+def test_dilate_boundary(cuda):
+    rng = np.random.default_rng(11)
+    for D, p in ((6, 0.05), (34, 0.05), (130, 0.01)):
+        f = rng.choice(np.array([-1, 0, 1], np.int16), size=(D, D, D), p=[0.9 - p, 0.1, p])
+        r, g = _t(f), _t(f)
+        refgpu.dilate_boundary(r, D)
+        ops.dilate_boundary(g, D)
+        assert np.array_equal(_n(g), _n(r))
+
+
+def test_transparency_statistic(cuda):
+    import torch
+    from snisr import prune
+    s = snisr.SynthScene(snisr.CFG2)
+    a = s.arrays()
+    t = 5
+    sig_d, _, flags = prune.grids_from_arrays(s.desc, a, t)
+    center = prune.tile_centers(s.desc, a)[t].astype(np.float32)
+    tile = float(s.desc.tile_size)
+    N = int(s.desc.res)
+    vs = tile / N
+    D = N + 2
+    ro, rd = [], []
+    for v in range(2):
+        cam = s.camera(v, 320, 180)
+        d = oracle.camera_dirs(cam)
+        o = oracle.camera_origins(cam, d.shape[0])
+        ro.append(o)
+        rd.append(d)
+    ro, rd = _t(np.concatenate(ro).astype(np.float32)), _t(np.concatenate(rd).astype(np.float32))
+    res = {}
+    for who in ("ref", "ours"):
+        T = torch.zeros((D, D, D), device="cuda")
+        (refgpu.transparency_statistic if who == "ref" else ops.transparency_statistic)(
+            ro, rd, D, _t(center), tile, vs, vs * 0.1, _t(sig_d), _t(flags), T)
+        res[who] = _n(T)
+    _report("transparency_statistic", res["ours"], res["ref"])
+    assert (res["ref"] > 0).sum() > 10000
+    assert np.array_equal(res["ours"], res["ref"])
