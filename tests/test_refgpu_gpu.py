@@ -327,3 +327,137 @@ def test_transparency_statistic(cuda):
     _report("transparency_statistic", res["ours"], res["ref"])
     assert (res["ref"] > 0).sum() > 10000
     assert np.array_equal(res["ours"], res["ref"])
+
+
+def test_reference_frame_timing(cuda):
+    """The reference renderer's frame (rendering/src/__init__.py:250-325 without
+    the CNN: compute_rays, tracing_tiles, the FP16 octree diffuse pass, then
+    the half-resolution specular pass in 4 steps of inverse_z_sampling +
+    inference_mlp + integrate_points, with batching by network) on the
+    1280x720 frame of a 16-tile scene of 64^3 tiles in renderData format,
+    once with the reference's own kernels at its launch shapes (num_thread
+    256; integrate_points 512) and once with the drop-ins.  sort_by_key is
+    the drop-in in both (the reference's is a thrust call, not a kernel of
+    its own).  Per-op CUDA-event times on the current stream, L2 flushed
+    before every frame; prints the table, checks the diffuse frames are
+    identical and the specular frames agree (the reference's MLP is scalar
+    FP16, the drop-in's FP32-accumulated on the tensor cores)."""
+    import torch
+    cfg = snisr.CFG2.replace(res=64, with_mesh=False)
+    synth = snisr.SynthScene(cfg)
+    data = octree.from_synth(synth, groups=synth.desc.num_tiles, seed=5)
+    T = octree.to_device(data)
+    der = octree.derived(data)
+    H, W, K = cfg.height, cfg.width, 30
+    DH, DW = H // 2, W // 2
+    far = der["far"]
+    flush = torch.empty(64 * 1024 * 1024, device="cuda")
+    names = ("compute_rays", "tracing_tiles", "octree_diffuse", "batching", "inverse_z_sampling", "inference_mlp",
+             "integrate_points")
+
+    def frame(impl, cam, ev):
+        import torch
+        intr_np = np.array([cam.cx, cam.cy, cam.inv_focal], np.float32)
+        rot_np = np.array([[cam.c2w[4 * r + c] for c in range(3)] for r in range(3)], np.float32)
+        org_np = np.array([cam.c2w[3], cam.c2w[7], cam.c2w[11]], np.float32)
+        intr, rot, origin = _t(intr_np), _t(rot_np), _t(org_np)
+        R = refgpu if impl == "ref" else ops
+        o_arg = org_np if impl == "ref" else origin
+        rays_d = torch.full((H, W, 3), -1.0, device="cuda")
+        visited = torch.full((H, W, K), -1, dtype=torch.int32, device="cuda")
+        diffuse = torch.full((H, W, 3), -1.0, device="cuda")
+        inv_near = torch.full((H, W), 1e-8, device="cuda")
+        net = torch.full((H, W), -1, dtype=torch.int16, device="cuda")
+        t = {n: 0.0 for n in names}
+        e = ev
+
+        def mark(i):
+            e[i].record()
+
+        mark(0)
+        if impl == "ref":
+            refgpu.compute_rays(intr_np, rot_np, 256, rays_d)
+        else:
+            ops.compute_rays(intr, rot, 256, rays_d)
+        mark(1)
+        if impl == "ref":
+            refgpu.tracing_tiles(rays_d, T["tile_IndexMap"], org_np, data["tile_shape"], data["scene_min_corner"],
+                                 der["scene_size"].astype(np.float32), der["tile_size"], 256, visited)
+        else:
+            ops.tracing_tiles(rays_d, T["tile_IndexMap"], origin, T["tile_shape"], T["scene_min_corner"],
+                              _t(der["scene_size"].astype(np.float32)), der["tile_size"], 256, visited)
+        mark(2)
+        R.rendering_diffuse_octree_fp16(rays_d, visited, o_arg, T["tile2group"], T["data_voxels"],
+                                        T["block_IndexMap"], T["nodes_IndexMap"], T["nodes_sampleFlag"],
+                                        T["voxels_start"], T["centers"], der["tile_size"], der["voxel_size"],
+                                        der["sample_step"], der["block_num_voxel"], 256, 0.8, 0.01, False, diffuse,
+                                        inv_near, net)
+        mark(3)
+        inv_s = inv_near[::2, ::2].contiguous()
+        net_s = net[::2, ::2].flatten().contiguous()
+        rays_s = rays_d[::2, ::2].contiguous()
+        npix = DH * DW
+        q = torch.arange(npix, dtype=torch.int32, device="cuda")
+        ps = torch.arange(npix, dtype=torch.int32, device="cuda")
+        num_net = ops.sort_by_key(net_s, q, ps)
+        end = torch.full((1,), npix, dtype=torch.int32, device="cuda")
+        counts = torch.cat([ps[1:num_net], end]) - ps[:num_net]
+        bs = torch.cat([torch.zeros(1, dtype=torch.int32, device="cuda"),
+                        torch.cumsum(torch.ceil(counts / 64), 0).int()])
+        nb = int(bs[-1])
+        new_net = torch.empty(nb, dtype=torch.int16, device="cuda")
+        new_ps = torch.empty(nb, dtype=torch.int32, device="cuda")
+        R.assign_pixels(net_s[:num_net].contiguous(), torch.cat([ps[:num_net], end]), bs, 256, new_net, new_ps)
+        new_ps = torch.cat([new_ps, end])
+        inv_bound = ((1.0 / (1.0 / inv_s + far) - inv_s) / 63).contiguous()
+        trans = torch.ones(DH, DW, 1, device="cuda")
+        spec = torch.zeros(DH, DW, 3, device="cuda")
+        mark(4)
+        torch.cuda.synchronize()
+        t["compute_rays"] += e[0].elapsed_time(e[1])
+        t["tracing_tiles"] += e[1].elapsed_time(e[2])
+        t["octree_diffuse"] += e[2].elapsed_time(e[3])
+        t["batching"] += e[3].elapsed_time(e[4])
+        for step in range(0, 64, 16):
+            res = torch.zeros(DH, DW, 16, 4, device="cuda")
+            pts = torch.full((DH, DW, 16, 3), -1.0, device="cuda")
+            isteps = torch.zeros(DH, DW, 16, device="cuda")
+            mark(5)
+            R.inverse_z_sampling(o_arg, rays_s, inv_s, inv_bound, 256, step, 16, pts, isteps)
+            mark(6)
+            R.inference_mlp(16, nb, 256, 1.0 / far, 0.01, new_net, trans, q, new_ps, T["group_centers"], pts, rays_s,
+                            T["net_params"], res)
+            mark(7)
+            R.integrate_points(res, isteps, 512, 0.01, trans, spec)
+            mark(8)
+            torch.cuda.synchronize()
+            t["inverse_z_sampling"] += e[5].elapsed_time(e[6])
+            t["inference_mlp"] += e[6].elapsed_time(e[7])
+            t["integrate_points"] += e[7].elapsed_time(e[8])
+        return t, diffuse, spec
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(9)]
+    cams = [synth.camera(p) for p in range(cfg.poses)]
+    acc = {impl: {n: 0.0 for n in names} for impl in ("ref", "ours")}
+    frames = 0
+    for i in range(2 + len(cams)):
+        outs = {}
+        for impl in ("ref", "ours"):
+            flush.zero_()
+            t, dif, spec = frame(impl, cams[i % len(cams)], ev)
+            outs[impl] = (_n(dif), _n(spec))
+            if i >= 2:
+                for n in names:
+                    acc[impl][n] += t[n]
+        if i >= 2:
+            frames += 1
+        assert np.array_equal(outs["ours"][0], outs["ref"][0])
+        e_spec = float(np.sqrt(((outs["ours"][1] - outs["ref"][1]) ** 2).mean()))
+        assert e_spec <= 1e-3, e_spec
+    ops.check_errors()
+    print(f"\nreference frame, 1280x720, 16 tiles of 64^3, {frames} poses, ms per frame (L2 flushed):")
+    print(f"{'op':22s} {'reference':>10s} {'drop-in':>10s} {'speed-up':>9s}")
+    for n in names + ("total",):
+        r = sum(acc["ref"].values()) if n == "total" else acc["ref"][n]
+        o = sum(acc["ours"].values()) if n == "total" else acc["ours"][n]
+        print(f"{n:22s} {r / frames:10.4f} {o / frames:10.4f} {r / max(o, 1e-9):8.2f}x")
