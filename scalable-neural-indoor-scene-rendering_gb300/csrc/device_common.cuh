@@ -89,6 +89,23 @@ __device__ __forceinline__ void tile_grid_walk(const float p[3], const float d[3
   }
 }
 
+// Visited-tile lists (K ints per pixel) are built per block in shared memory
+// and written out as the block's one contiguous range with coalesced stores
+// (a thread writing its own row alone makes every store a scattered 4-byte
+// write, 32 cache lines per warp instruction).  kTraceRowsThreads pixels per
+// block; lists longer than fit in 48 KB are written directly.
+constexpr int kTraceRowsThreads = 128;
+inline bool trace_rows_staged(int K) { return (size_t)kTraceRowsThreads * K * 4 <= 48 * 1024; }
+
+__device__ __forceinline__ void trace_rows_flush(const int32_t* rows, int32_t* visited, int64_t base, int64_t n,
+                                                 int K) {
+  __syncthreads();
+  const int64_t count = (n - base < (int64_t)blockDim.x ? n - base : (int64_t)blockDim.x) * K;
+  int32_t* dst = visited + base * K;
+  for (int64_t j = threadIdx.x; j < count; j += blockDim.x) dst[j] = rows[j];
+  __syncthreads();
+}
+
 __device__ __forceinline__ bool occupied(const SceneDev& S, int tile, int vid, uint32_t& rec) {
   const OccWord* w = S.occ + (size_t)tile * S.words_per_tile + (vid >> 6);
   uint4 raw = __ldg(reinterpret_cast<const uint4*>(w));

@@ -42,28 +42,35 @@ __global__ void op_compute_rays_kernel(const float* __restrict__ intr, const flo
 // rendering/src/include/cuda_utils.h:158-238).  A ray whose origin lies
 // outside the scene is moved to its entry point; as in the reference, a
 // missed scene box leaves t = -1 and the clamped point is traversed anyway.
+template <bool kStaged>
 __global__ void op_tracing_tiles_kernel(const float* __restrict__ rays_d, int64_t npix, const int32_t* __restrict__ imap,
                                         const float* __restrict__ origin, const int32_t* __restrict__ shape,
                                         const float* __restrict__ smin, const float* __restrict__ ssize, float tile,
                                         int K, int32_t* visited) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
-    int32_t* vis = visited + i * K;
-    for (int j = 0; j < K; ++j) vis[j] = -1;
-    float d[3] = {rays_d[3 * i], rays_d[3 * i + 1], rays_d[3 * i + 2]};
-    float o[3] = {origin[0], origin[1], origin[2]};
-    float p[3], size[3] = {ssize[0], ssize[1], ssize[2]};
-    for (int a = 0; a < 3; ++a) p[a] = fsub(o[a], smin[a]);
-    if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
-      float c[3], h[3];
-      for (int a = 0; a < 3; ++a) { h[a] = fdiv(size[a], 2.0f); c[a] = fadd(smin[a], h[a]); }
-      float2 b = slab(o, d, c, h);
-      for (int a = 0; a < 3; ++a) {
-        p[a] = ffma(b.x, d[a], p[a]);
-        p[a] = fminf(fmaxf(p[a], 0.0f), fsub(size[a], 0.000001f));
+  extern __shared__ int32_t rows[];  // kStaged: blockDim.x lists of K
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < npix; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int32_t* vis = kStaged ? rows + threadIdx.x * K : visited + i * K;
+    if (kStaged || i < npix)
+      for (int j = 0; j < K; ++j) vis[j] = -1;
+    if (i < npix) {
+      float d[3] = {rays_d[3 * i], rays_d[3 * i + 1], rays_d[3 * i + 2]};
+      float o[3] = {origin[0], origin[1], origin[2]};
+      float p[3], size[3] = {ssize[0], ssize[1], ssize[2]};
+      for (int a = 0; a < 3; ++a) p[a] = fsub(o[a], smin[a]);
+      if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
+        float c[3], h[3];
+        for (int a = 0; a < 3; ++a) { h[a] = fdiv(size[a], 2.0f); c[a] = fadd(smin[a], h[a]); }
+        float2 b = slab(o, d, c, h);
+        for (int a = 0; a < 3; ++a) {
+          p[a] = ffma(b.x, d[a], p[a]);
+          p[a] = fminf(fmaxf(p[a], 0.0f), fsub(size[a], 0.000001f));
+        }
       }
+      const int M[3] = {shape[0], shape[1], shape[2]};
+      tile_grid_walk(p, d, imap, M, tile, K, vis);
     }
-    const int M[3] = {shape[0], shape[1], shape[2]};
-    tile_grid_walk(p, d, imap, M, tile, K, vis);
+    if (kStaged) trace_rows_flush(rows, visited, base, npix, K);
   }
 }
 
@@ -262,8 +269,13 @@ snisr_status snisr_op_tracing_tiles(const float* rays_d, int64_t npix, const int
   if (npix == 0) return SNISR_OK;
   if (!rays_d || !imap || !origin || !shape || !smin || !ssize || !visited)
     return set_error(SNISR_INVALID_ARG, "tracing_tiles: null argument");
-  op_tracing_tiles_kernel<<<blocks_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(rays_d, npix, imap, origin, shape,
-                                                                                   smin, ssize, tile_size, K, visited);
+  if (trace_rows_staged(K))
+    op_tracing_tiles_kernel<true><<<blocks_for(npix, kTraceRowsThreads), kTraceRowsThreads,
+                                    (size_t)kTraceRowsThreads * K * 4, (cudaStream_t)stream>>>(
+        rays_d, npix, imap, origin, shape, smin, ssize, tile_size, K, visited);
+  else
+    op_tracing_tiles_kernel<false><<<blocks_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(
+        rays_d, npix, imap, origin, shape, smin, ssize, tile_size, K, visited);
   OP_CHECK("tracing_tiles");
   return SNISR_OK;
 }

@@ -69,9 +69,11 @@ __global__ void train_rays_kernel(const float* __restrict__ Km, const float* __r
   }
 }
 
+template <bool kStaged>
 __global__ void train_tracing_kernel(const float* __restrict__ ro, const float* __restrict__ rd, int64_t n,
                                      const int32_t* __restrict__ imap, int3 shape, float3 smin, float tile, int K,
                                      int32_t* visited) {
+  extern __shared__ int32_t rows[];  // kStaged: blockDim.x lists of K
   const int M[3] = {shape.x, shape.y, shape.z};
   const float sm[3] = {smin.x, smin.y, smin.z};
   float size[3], c[3], h[3];
@@ -81,24 +83,29 @@ __global__ void train_tracing_kernel(const float* __restrict__ ro, const float* 
     h[a] = fmul(size[a], 0.5f);
     c[a] = fadd(sm[a], h[a]);
   }
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int32_t* vis = visited + i * K;
-    for (int j = 0; j < K; ++j) vis[j] = -1;
-    const float o[3] = {ro[3 * i], ro[3 * i + 1], ro[3 * i + 2]};
-    const float d0[3] = {rd[3 * i], rd[3 * i + 1], rd[3 * i + 2]};
-    float d[3];
-    normalize3(d0, d);
-    float p[3];
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int32_t* vis = kStaged ? rows + threadIdx.x * K : visited + i * K;
+    if (kStaged || i < n)
+      for (int j = 0; j < K; ++j) vis[j] = -1;
+    if (i < n) {
+      const float o[3] = {ro[3 * i], ro[3 * i + 1], ro[3 * i + 2]};
+      const float d0[3] = {rd[3 * i], rd[3 * i + 1], rd[3 * i + 2]};
+      float d[3];
+      normalize3(d0, d);
+      float p[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) p[a] = fsub(o[a], sm[a]);
-    if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
-      const float2 b = slab(o, d, c, h);
+      for (int a = 0; a < 3; ++a) p[a] = fsub(o[a], sm[a]);
+      if (p[0] < 0 || p[0] >= size[0] || p[1] < 0 || p[1] >= size[1] || p[2] < 0 || p[2] >= size[2]) {
+        const float2 b = slab(o, d, c, h);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) p[a] = ffma(b.x, d[a], p[a]);
+        for (int a = 0; a < 3; ++a) p[a] = ffma(b.x, d[a], p[a]);
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) p[a] = fmaxf(0.0f, fminf(p[a], fsub(size[a], 0.000001f)));
+      tile_grid_walk(p, d, imap, M, tile, K, vis);
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) p[a] = fmaxf(0.0f, fminf(p[a], fsub(size[a], 0.000001f)));
-    tile_grid_walk(p, d, imap, M, tile, K, vis);
+    if (kStaged) trace_rows_flush(rows, visited, base, n, K);
   }
 }
 
@@ -451,9 +458,14 @@ snisr_status snisr_op_train_tracing_tiles(const float* rays_o, const float* rays
   if (n == 0) return SNISR_OK;
   if (!rays_o || !rays_d || !index_map || !visited)
     return set_error(SNISR_INVALID_ARG, "train_tracing_tiles: null argument");
-  train_tracing_kernel<<<grid_n(n, 128), 128, 0, (cudaStream_t)stream>>>(
-      rays_o, rays_d, n, index_map, make_int3(tile_shape[0], tile_shape[1], tile_shape[2]),
-      make_float3(scene_min_corner[0], scene_min_corner[1], scene_min_corner[2]), tile_size, K, visited);
+  const int3 shp = make_int3(tile_shape[0], tile_shape[1], tile_shape[2]);
+  const float3 smn = make_float3(scene_min_corner[0], scene_min_corner[1], scene_min_corner[2]);
+  if (trace_rows_staged(K))
+    train_tracing_kernel<true><<<grid_n(n, kTraceRowsThreads), kTraceRowsThreads, (size_t)kTraceRowsThreads * K * 4,
+                                 (cudaStream_t)stream>>>(rays_o, rays_d, n, index_map, shp, smn, tile_size, K, visited);
+  else
+    train_tracing_kernel<false><<<grid_n(n, 128), 128, 0, (cudaStream_t)stream>>>(rays_o, rays_d, n, index_map, shp,
+                                                                                  smn, tile_size, K, visited);
   PREP_CHECK("train_tracing_tiles");
   return SNISR_OK;
 }
