@@ -527,112 +527,120 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       rb = __ldg(src + 1);
     }
   };
-  if (tid == 0) chunk_slot[0] = atomicAdd(ctrl + CTRL_WORK, 1);
+  // Software pipeline: while chunk c runs its MMA chain, the threads gather
+  // chunk c + 1's A rows into registers, a share of the row groups during
+  // each layer's MMA, and write them into the A tile once chunk c's last
+  // MMA has read it.  Chunks are claimed two ahead (slots rotate by three),
+  // so the next chunk is known before its gather starts; thread tid holds
+  // row tid's record of the current and of the next chunk.
+  //
+  // Gather of one row group: RPI = 32/G rows per warp; lane (g = lane / RPI,
+  // row = lane % RPI) owns channel group g of one row.  The FP16 cache is
+  // corner-major ([voxel][corner][group] x 16 B), so for each corner the G
+  // lanes of a row read one contiguous G*16-byte slice: a load instruction
+  // touches RPI cache lines, not 32.  Each lane interpolates its 8 channels
+  // over the 8 corners in FP32; its row's view encoding chunks come along.
+  // A row holds chunks [0,G) features, [G,G+4) view encoding, the rest 0.
+  constexpr int RPI = 32 / G, NENC = 4 / G;
+  const int my_g = lane / RPI, my_row = lane % RPI;
+  uint4 hf[G], he[G][NENC];  // the next chunk's rows, held until the A tile is free
+  auto gather_group = [&](int it, const uint4& ra, const uint4& rb, uint4& f, uint4* e) {
+    const int src = it * RPI + my_row;
+    const uint32_t rec = __shfl_sync(kFull, ra.x, src);
+    const uint32_t ray = __shfl_sync(kFull, ra.y, src);
+    const float fx = __uint_as_float(__shfl_sync(kFull, rb.x, src));
+    const float fy = __uint_as_float(__shfl_sync(kFull, rb.y, src));
+    const float fz = __uint_as_float(__shfl_sync(kFull, rb.z, src));
+    f = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int j = 0; j < NENC; ++j) e[j] = make_uint4(0, 0, 0, 0);
+    if (rec != kInvalid) {
+      const uint4* fp = S.feat16 + (size_t)rec * 8 * G + my_g;
+      uint4 cv[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) cv[k] = __ldg(fp + k * G);
+#pragma unroll
+      for (int j = 0; j < NENC; ++j) e[j] = __ldg(enc + (size_t)ray * 4 + my_g + j * G);
+      float acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float wk = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
+        const __half2* hv = reinterpret_cast<const __half2*>(&cv[k]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float2 pp = __half22float2(hv[q]);
+          acc[2 * q] = fmaf(wk, pp.x, acc[2 * q]);
+          acc[2 * q + 1] = fmaf(wk, pp.y, acc[2 * q + 1]);
+        }
+      }
+      f.x = pack_h2(acc[0], acc[1]); f.y = pack_h2(acc[2], acc[3]);
+      f.z = pack_h2(acc[4], acc[5]); f.w = pack_h2(acc[6], acc[7]);
+    }
+  };
+  // the held rows into the A tile (8 consecutive rows per 8-lane phase: conflict-free)
+  auto write_rows = [&]() {
+#pragma unroll
+    for (int it = 0; it < G; ++it) {
+      const int r = warp * 32 + it * RPI + my_row;
+      *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, my_g)) = hf[it];
+#pragma unroll
+      for (int j = 0; j < NENC; ++j) *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, G + my_g + j * G)) = he[it][j];
+#pragma unroll
+      for (int ch = G + 4 + my_g; ch < 8; ch += G)
+        *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
+    }
+  };
+
+  if (tid == 0) {
+    chunk_slot[0] = atomicAdd(ctrl + CTRL_WORK, 1);
+    chunk_slot[1] = atomicAdd(ctrl + CTRL_WORK, 1);
+  }
   __syncthreads();
   ChunkRows cr = locate(chunk_slot[0]);
   uint4 my_ra, my_rb;
   load_row(cr, my_ra, my_rb);
+  bool w_pending = false;  // a weight image copy is in flight (block-uniform)
+  if (cr.c < total_chunks) {
+    // prologue: the first chunk's weights and rows
+    if (tid == 0) {
+      tc::mbar_arrive_expect_tx(wbar, (uint32_t)img_bytes);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cr.tile * img_stride, (uint32_t)img_bytes, wbar);
+    }
+    cur_tile = cr.tile;
+    w_pending = true;
+#pragma unroll
+    for (int it = 0; it < G; ++it) gather_group(it, my_ra, my_rb, hf[it], he[it]);
+    write_rows();
+    tc::fence_proxy_async();
+  }
   for (int iter = 0;; ++iter) {
     if (cr.c >= total_chunks) break;
-    int* next_slot = chunk_slot + ((iter + 1) & 1);
-    if (tid == 0) *next_slot = atomicAdd(ctrl + CTRL_WORK, 1);  // read after the gather's barrier
-    const int tile = cr.tile, row0 = cr.row0, cnt = cr.cnt;
-    (void)row0;
-    const bool new_w = tile != cur_tile;
-    if (new_w && tid == 0) {
-      tc::mbar_arrive_expect_tx(wbar, (uint32_t)img_bytes);
-      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)tile * img_stride, (uint32_t)img_bytes, wbar);
-    }
-    cur_tile = tile;
+    if (tid == 0) chunk_slot[(iter + 2) % 3] = atomicAdd(ctrl + CTRL_WORK, 1);  // read two iterations later
+    const ChunkRows nx = locate(chunk_slot[(iter + 1) % 3]);
+    const int cnt = cr.cnt;
     // this thread's output row (ray id, compositing weight)
     const uint32_t my_ray = my_ra.y;
     const float my_wt = __uint_as_float(my_ra.z);
-
-    // gather: per warp iteration RPI = 32/G rows; lane (g = lane / RPI,
-    // row = lane % RPI) owns channel group g of one row.  The FP16 cache is
-    // corner-major ([voxel][corner][group] x 16 B), so for each corner the G
-    // lanes of a row read one contiguous G*16-byte slice: a load instruction
-    // touches RPI cache lines, not 32.  Each lane interpolates its 8 channels
-    // over the 8 corners in FP32 and writes one 16-byte chunk of the
-    // swizzled A row (8 consecutive rows per 8-lane phase: conflict-free).
-    // A row holds chunks [0,G) features, [G,G+4) view encoding, the rest 0.
-    // Row records come from the lane holding the row (lane = row - warp*32).
-    {
-      constexpr int RPI = 32 / G;
-      const int my_g = lane / RPI, my_row = lane % RPI;
-#pragma unroll 1
-      for (int it = 0; it < G; it += 2) {
-        uint32_t rec[2], ray[2];
-        float fx[2], fy[2], fz[2];
-        uint4 cv[2][8];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int src_lane = (it + u) * RPI + my_row;
-          rec[u] = __shfl_sync(kFull, my_ra.x, src_lane);
-          ray[u] = __shfl_sync(kFull, my_ra.y, src_lane);
-          fx[u] = __uint_as_float(__shfl_sync(kFull, my_rb.x, src_lane));
-          fy[u] = __uint_as_float(__shfl_sync(kFull, my_rb.y, src_lane));
-          fz[u] = __uint_as_float(__shfl_sync(kFull, my_rb.z, src_lane));
-          if (rec[u] != kInvalid) {
-            const uint4* fp = S.feat16 + (size_t)rec[u] * 8 * G + my_g;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cv[u][k] = __ldg(fp + k * G);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int r = warp * 32 + (it + u) * RPI + my_row;
-          if (rec[u] != kInvalid) {
-            float acc[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              const float wk = ((k & 4) ? fx[u] : 1.0f - fx[u]) * ((k & 2) ? fy[u] : 1.0f - fy[u]) *
-                               ((k & 1) ? fz[u] : 1.0f - fz[u]);
-              const __half2* hv = reinterpret_cast<const __half2*>(&cv[u][k]);
-#pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                float2 pp = __half22float2(hv[q]);
-                acc[2 * q] = fmaf(wk, pp.x, acc[2 * q]);
-                acc[2 * q + 1] = fmaf(wk, pp.y, acc[2 * q + 1]);
-              }
-            }
-            uint4 o;
-            o.x = pack_h2(acc[0], acc[1]); o.y = pack_h2(acc[2], acc[3]);
-            o.z = pack_h2(acc[4], acc[5]); o.w = pack_h2(acc[6], acc[7]);
-            *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, my_g)) = o;
-#pragma unroll
-            for (int e = my_g; e < 4; e += G)
-              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, G + e)) = __ldg(enc + (size_t)ray[u] * 4 + e);
-#pragma unroll
-            for (int ch = G + 4 + my_g; ch < 8; ch += G)
-              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
-          } else {
-#pragma unroll
-            for (int ch = my_g; ch < 8; ch += G)
-              *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
-          }
-        }
-      }
-    }
-    tc::fence_proxy_async();
-    __syncthreads();
-    const ChunkRows nx = locate(*next_slot);
-    uint4 nra, nrb;
-    load_row(nx, nra, nrb);
-    if (new_w) {
+    if (w_pending) {
       // one thread polls the barrier; the others wait at bar.sync, which
       // keeps the shared-memory pipe free for the gathers of other CTAs
       bool ok = tid == 0 ? tc::mbar_wait(wbar, wphase) : true;
       wphase ^= 1u;
+      w_pending = false;
       if (__syncthreads_or(!ok)) { failed = true; break; }
+    } else {
+      __syncthreads();  // the A rows written above are visible to the MMA issuer
     }
 
     // L hidden Linear layers and the output Linear (N = 16, 3 used), all on
     // the tensor core; each layer's bias enters as one extra K = 16 step.
+    // During each layer's MMA the threads gather their share of the next
+    // chunk's row groups.
+    uint4 nra, nrb;
     float out3[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
+#pragma unroll
     for (int l = 0; l <= L; ++l) {
       if (tid == 0) {
         tc::fence_after_sync();
@@ -647,6 +655,9 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         tc::mma_f16(tmem, ones_desc, tc::sdesc_sw128(bias_tile + (last ? 0 : 32 * l)), id, 1);
         tc::mma_commit(mbar);
       }
+      if (l == 0) load_row(nx, nra, nrb);
+#pragma unroll
+      for (int it = l * G / (L + 1); it < (l + 1) * G / (L + 1); ++it) gather_group(it, nra, nrb, hf[it], he[it]);
       bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
       mphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -671,16 +682,29 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
           }
         }
         tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
       } else {
         float v[4];
         tc::tmem_ld4(taddr, v);
         tc::tmem_wait_ld();
         out3[0] = v[0]; out3[1] = v[1]; out3[2] = v[2];
       }
-      tc::fence_before_sync();
-      __syncthreads();
     }
     if (failed) break;
+    // chunk c's MMAs are done: the next tile's weights may replace these, and
+    // the A tile takes the next chunk's rows
+    if (nx.c < total_chunks && nx.tile != cur_tile) {
+      if (tid == 0) {
+        tc::mbar_arrive_expect_tx(wbar, (uint32_t)img_bytes);
+        tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)nx.tile * img_stride, (uint32_t)img_bytes, wbar);
+      }
+      cur_tile = nx.tile;
+      w_pending = true;
+    }
+    tc::fence_before_sync();  // output columns read before the next chunk's MMA (barrier at the loop top)
+    write_rows();  // chunk c's last MMA has completed: the A tile is free
+    tc::fence_proxy_async();
     if (tid < cnt) {
 #pragma unroll
       for (int c3 = 0; c3 < 3; ++c3) atomicAdd(rgb + 3 * (size_t)my_ray + c3, my_wt * sigmoidf_(out3[c3]));
