@@ -261,21 +261,43 @@ __global__ void __launch_bounds__(128, 3)
     }
     const float cx = centers[3 * g], cy = centers[3 * g + 1], cz = centers[3 * g + 2];
     const int64_t t0 = (int64_t)pstarts[b] * spr, t1 = (int64_t)pstarts[b + 1] * spr;
+    // The task of this thread's A row in the chunk starting at c: its pixel,
+    // whether it is live, the encoded position and the view direction.  The
+    // next chunk's tasks are fetched during the current chunk's first MMA
+    // (three dependent loads), so that only arithmetic is left between the
+    // chunks.
+    struct Task {
+      bool live;
+      int64_t ori;
+      float p[3], d[3];
+    };
+    auto fetch = [&](int64_t c) {
+      Task k;
+      const int64_t t = c + tid;
+      k.live = t < t1;
+      k.ori = 0;
+      if (k.live) {
+        const int64_t pix = qpix[t / spr];
+        k.live = transparency[pix] >= trans_stop;
+        k.ori = pix * spr + t % spr;
+        if (k.live) {
+          k.p[0] = (samples[3 * k.ori] - cx) * inv_far;
+          k.p[1] = (samples[3 * k.ori + 1] - cy) * inv_far;
+          k.p[2] = (samples[3 * k.ori + 2] - cz) * inv_far;
+          k.d[0] = rays_d[3 * pix];
+          k.d[1] = rays_d[3 * pix + 1];
+          k.d[2] = rays_d[3 * pix + 2];
+        }
+      }
+      return k;
+    };
+    Task cur = fetch(t0);
     for (int64_t c0 = t0; c0 < t1; c0 += 128) {
       // A row of this thread: position encoding of its task (zeros when skipped)
-      const int64_t t = c0 + tid;
-      bool live = t < t1;
-      int64_t pix = 0, ori = 0;
-      if (live) {
-        pix = qpix[t / spr];
-        live = transparency[pix] >= trans_stop;
-        ori = pix * spr + t % spr;
-      }
       {
         uint32_t h[32];
-        if (live) {
-          const float p[3] = {(samples[3 * ori] - cx) * inv_far, (samples[3 * ori + 1] - cy) * inv_far,
-                              (samples[3 * ori + 2] - cz) * inv_far};
+        if (cur.live) {
+          const float* p = cur.p;
           // sin/cos of 2^i p (i = 0..9): one accurate sincos per coordinate, then
           // double-angle steps (error ~2^9 x FP32 rounding at i = 9, below half
           // an FP16 ulp)
@@ -309,6 +331,8 @@ __global__ void __launch_bounds__(128, 3)
       }
       tc::fence_proxy_async();
       __syncthreads();
+      Task nxt;
+      nxt.live = false;
       float out[32];
       for (int l = 0; l <= kSpHidden; ++l) {
         if (tid == 0) {
@@ -320,6 +344,7 @@ __global__ void __launch_bounds__(128, 3)
             tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
           tc::mma_commit(mbar);
         }
+        if (l == 0 && c0 + 128 < t1) nxt = fetch(c0 + 128);
         const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
         mphase ^= 1u;
         if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -358,8 +383,8 @@ __global__ void __launch_bounds__(128, 3)
         __syncthreads();
       }
       if (failed) break;
-      if (live) {
-        const float dx = rays_d[3 * pix], dy = rays_d[3 * pix + 1], dz = rays_d[3 * pix + 2];
+      if (cur.live) {
+        const float dx = cur.d[0], dy = cur.d[1], dz = cur.d[2];
         const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
         const float X = dx * inv, Y = dy * inv, Z = dz * inv;
         const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f;
@@ -374,8 +399,9 @@ __global__ void __launch_bounds__(128, 3)
                C2[3] * X * Z * out[21 + i] + C2[4] * (xx - yy) * out[24 + i];
           rgb[i] = 1.0f / (1.0f + expf(-v));
         }
-        results[ori] = make_float4(rgb[0], rgb[1], rgb[2], fmaxf(out[kSpOut - 1], 0.f));
+        results[cur.ori] = make_float4(rgb[0], rgb[1], rgb[2], fmaxf(out[kSpOut - 1], 0.f));
       }
+      cur = nxt;
     }
     if (failed) break;
   }
