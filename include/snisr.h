@@ -525,6 +525,14 @@ snisr_status snisr_scene_frame_footprint(snisr_scene* scene, int64_t* out, void*
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev,
                             int32_t N, int32_t bf16, int32_t mode, void* stream);
 
+/* The bounded-wait error path of the tensor-core kernels: one wait on an
+ * mbarrier that nothing completes, given up after limit_ns (0 < limit_ns <=
+ * 10 s) of the GPU's global timer.  Returns SNISR_DEVICE_TIMEOUT when the wait
+ * ran out (the expected result), *waited_ns = the device time it waited.
+ * Every kernel wait of this library has the same bound (2 s).  Synchronises
+ * `stream`. */
+snisr_status snisr_diag_wait_timeout(int64_t limit_ns, int64_t* waited_ns, void* stream);
+
 const char* snisr_last_error_string(void);
 const char* snisr_version(void);
 int32_t snisr_abi_version(void);

@@ -887,6 +887,15 @@ snisr_status snisr_scene_autotune_train(snisr_scene* sc, const float* vfeat, con
   return snisr_scene_get_tuning(sc, out);
 }
 
+snisr_status snisr_diag_wait_timeout(int64_t limit_ns, int64_t* waited_ns, void* stream) {
+  if (limit_ns <= 0 || limit_ns > 10000000000ll || !waited_ns)
+    return set_error(SNISR_INVALID_ARG, "diag_wait_timeout: bad argument (limit in (0, 10 s])");
+  bool ran_out = false;
+  CUDA_TRY(launch_diag_wait(limit_ns, waited_ns, &ran_out, (cudaStream_t)stream), "diag_wait_timeout");
+  if (ran_out) return set_error(SNISR_DEVICE_TIMEOUT, "diag_wait_timeout: the wait ran out (expected)");
+  return SNISR_OK;
+}
+
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev, int32_t N, int32_t bf16,
                             int32_t mode, void* stream) {
   if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1) || mode < 0 || mode > 2 ||

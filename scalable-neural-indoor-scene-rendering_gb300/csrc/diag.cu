@@ -8,6 +8,10 @@
 //         64-row atom of A pointing at a zero tile.  Mode 1: leading byte
 //         offset = MN atom stride, stride byte offset = 8-row K group stride;
 //         mode 2: the two swapped.
+// diag_wait_kernel: a wait on an mbarrier that nothing completes, with a
+// given time limit: the bounded-wait error path of the tensor-core kernels
+// (the wait runs out, the kernel reports it and returns, the context stays
+// usable), exercised without a fault.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -71,7 +75,10 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   bool ok = tid == 0 ? tc::mbar_wait(tc::smem_addr(bar), 0) : true;
   tc::fence_after_sync();
   if (__syncthreads_or(!ok)) {
-    if (tid == 0) *status = 1;
+    if (tid == 0) {
+      *status = 1;
+      (void)tc::mbar_wait(tc::smem_addr(bar), 0);  // once more, bounded: the MMAs are done before TMEM is freed
+    }
   } else {
     const int nc = mode == 0 ? N : 64;
     float v[64];
@@ -86,7 +93,38 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   if (warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
+__global__ void diag_wait_kernel(uint64_t limit_ns, long long* out) {
+  __shared__ uint64_t bar;
+  const uint32_t b = tc::smem_addr(&bar);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(b, 1);  // one arrival expected; none comes
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = tc::global_ns();
+    const bool ok = tc::mbar_wait(b, 0, limit_ns);
+    out[0] = ok ? 0 : 1;
+    out[1] = (long long)(tc::global_ns() - t0);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_diag_wait(int64_t limit_ns, int64_t* waited_ns, bool* ran_out, cudaStream_t st) {
+  long long* out = nullptr;
+  cudaError_t e = cudaMallocAsync(&out, 2 * sizeof(long long), st);
+  if (e != cudaSuccess) return e;
+  diag_wait_kernel<<<1, 32, 0, st>>>((uint64_t)limit_ns, out);
+  e = cudaGetLastError();
+  long long h[2] = {-1, -1};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(out, st);
+  *ran_out = h[0] == 1;
+  *waited_ns = h[1];
+  return e;
+}
 
 cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
                             cudaStream_t st) {

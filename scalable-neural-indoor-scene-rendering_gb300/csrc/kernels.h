@@ -122,6 +122,7 @@ cudaError_t launch_inference_mlp(int spr, int num_block, float inv_far, float tr
                                  const float* rays_d, const uint16_t* params, float* results, int* work,
                                  uint32_t* err, int num_sms, cudaStream_t st);
 
+cudaError_t launch_diag_wait(int64_t limit_ns, int64_t* waited_ns, bool* ran_out, cudaStream_t st);
 cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int N, int bf16, int mode,
                             cudaStream_t st);
 

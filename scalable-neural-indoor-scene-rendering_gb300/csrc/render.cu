@@ -497,6 +497,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   int cur_tile = -1;
   uint32_t wphase = 0, mphase = 0;
   bool failed = false;
+  tc::Drain drain;
 
   // Chunks are claimed one ahead: while chunk c runs its MMA chain, thread 0
   // has already claimed the next chunk (slots alternate by iteration parity)
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       bool ok = tid == 0 ? tc::mbar_wait(wbar, wphase) : true;
       wphase ^= 1u;
       w_pending = false;
-      if (__syncthreads_or(!ok)) { failed = true; break; }
+      if (__syncthreads_or(!ok)) { failed = true; drain.set(wbar, wphase ^ 1u); break; }
     } else {
       __syncthreads();  // the A rows written above are visible to the MMA issuer
     }
@@ -660,7 +661,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       for (int it = l * G / (L + 1); it < (l + 1) * G / (L + 1); ++it) gather_group(it, nra, nrb, hf[it], he[it]);
       bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
       mphase ^= 1u;
-      if (__syncthreads_or(!ok)) { failed = true; break; }
+      if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
       if (l < L) {
@@ -713,7 +714,10 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     my_ra = nra;
     my_rb = nrb;
   }
-  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  if (failed && tid == 0) {
+    atomicOr(S.err, ERR_TIMEOUT);
+    drain.run();
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, H);

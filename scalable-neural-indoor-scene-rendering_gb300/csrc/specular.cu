@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(128, 3)
   uint32_t mphase = 0;
   int cur_net = -1;
   bool failed = false;
+  tc::Drain drain;
   for (;;) {
     __syncthreads();  // every thread has read the previous slot value
     if (tid == 0) *blk_slot = atomicAdd(work, 1);
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(128, 3)
         if (l == 0 && c0 + 128 < t1) nxt = fetch(c0 + 128);
         const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
         mphase ^= 1u;
-        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
         tc::fence_after_sync();
         if (l < kSpHidden) {
 #pragma unroll
@@ -405,7 +406,10 @@ __global__ void __launch_bounds__(128, 3)
     }
     if (failed) break;
   }
-  if (failed && tid == 0 && err) atomicOr(err, kErrTimeout);
+  if (failed && tid == 0) {
+    if (err) atomicOr(err, kErrTimeout);
+    drain.run();
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 64);

@@ -1,8 +1,9 @@
 // Inline-PTX wrappers for the sm_103a tensor-core path: tcgen05 MMA with
 // tensor-memory accumulators, bulk (TMA) copies and mbarrier waits.
 //
-// Every wait is bounded: after kSpinLimit polls it gives up and reports
-// failure so the caller can record an error and leave without hanging.
+// Every wait is bounded in time (kWaitLimitNs of the GPU's global timer):
+// after that it gives up and reports failure, so that the caller can record
+// an error, drain what it has in flight and leave without hanging.
 #pragma once
 
 #include <cstdint>
@@ -11,7 +12,13 @@
 namespace snisr {
 namespace tc {
 
-constexpr uint32_t kSpinLimit = 1u << 26;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -37,12 +44,34 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase with parity `phase` to complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, phase)) return true;
-  return false;
+// Bounded wait for the phase with parity `phase` to complete: polls, and
+// reads the global timer once per 64 polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint64_t limit_ns = kWaitLimitNs) {
+  if (mbar_try_wait(bar, phase)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, phase)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
 }
+
+// The barrier wait that ran out, kept so that the exit path can wait once
+// more (again bounded) for the copy or the MMAs still in flight before the
+// CTA frees its tensor memory and leaves: nothing of this CTA then writes
+// shared or tensor memory that a later CTA may own.
+struct Drain {
+  uint32_t bar = 0, phase = 0;
+  bool pending = false;
+  __device__ __forceinline__ void set(uint32_t b, uint32_t ph) {
+    bar = b;
+    phase = ph;
+    pending = true;
+  }
+  __device__ __forceinline__ void run() const {
+    if (pending) (void)mbar_wait(bar, phase);
+  }
+};
 
 // Bulk global->shared copy through the TMA engine, completion counted on `bar`.
 // dst, src 16-byte aligned, bytes a multiple of 16.

@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
   const int total = coff[NT];
   int cur_tile = -1;
   bool failed = false;
+  tc::Drain drain;
   for (;;) {
     if (tid == 0) *chunk_slot = atomicAdd(work, 1);
     __syncthreads();
@@ -400,7 +401,7 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
     if (new_w) {
       bool ok = tid == 0 ? tc::mbar_wait(B.wbar, B.wphase) : true;
       B.wphase ^= 1u;
-      if (__syncthreads_or(!ok)) { failed = true; break; }
+      if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
     }
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t ahi = tc::smem_addr(Ahi), alo = tc::smem_addr(Alo), w = tc::smem_addr(Wsm);
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
                           l == 0 ? 4 : H / 16);
         tc::mma_commit(B.mbar);
       }
-      if (!wait_mma(B, tid)) { failed = true; break; }
+      if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
       if (l < L) {
         epi_relu_split<H>(taddr, Ahi, Alo, tid);  // the output layer also takes split inputs
         tc::fence_proxy_async();
@@ -431,7 +432,10 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
     if (tid < cp.cnt)
       cout[cp.row0 + tid] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
   }
-  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  if (failed && tid == 0) {
+    atomicOr(S.err, ERR_TIMEOUT);
+    drain.run();
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 64);
@@ -539,6 +543,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   const int total = coff[NT];
   int cur_tile = -1;
   bool failed = false, have_acc = false;
+  tc::Drain drain;
   const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   int run_c = 0, run_left = 0;
 
@@ -625,7 +630,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     if (new_w) {
       bool ok = tid == 0 ? tc::mbar_wait(B.wbar, B.wphase) : true;
       B.wphase ^= 1u;
-      if (__syncthreads_or(!ok)) { failed = true; break; }
+      if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
     }
     const uint32_t w = tc::smem_addr(Wsm);
     // forward recomputation of the hidden activations H1..HL (split operands;
@@ -640,7 +645,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
                           l == 0 ? 4 : H / 16);
         tc::mma_commit(B.mbar);
       }
-      if (!wait_mma(B, tid)) { failed = true; break; }
+      if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
       epi_relu_split_part<H, 2>(taddr, Ht + l * 16384, l + 1 < L ? lo_out : nullptr, row, part);
       tc::fence_proxy_async();
       tc::fence_before_sync();
@@ -672,7 +677,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
           tc::mma_f16(tw, tc::sdesc_sw128(dlt + 32 * kk), tc::sdesc_sw128(wt + 32 * kk), idd, kk > 0);
         tc::mma_commit(B.mbar);
       }
-      if (!wait_mma(B, tid)) { failed = true; break; }
+      if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
       if (l > 0) {
         // delta of layer l-1's output = (delta W_l) * [act > 0], BF16 into D;
         // this thread's part: columns [part H/2, (part+1) H/2)
@@ -728,7 +733,10 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     tc::fence_after_sync();
     flush(cur_tile);
   }
-  if (failed && tid == 0) atomicOr(S.err, ERR_TIMEOUT);
+  if (failed && tid == 0) {
+    atomicOr(S.err, ERR_TIMEOUT);
+    drain.run();
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);

@@ -69,6 +69,10 @@ def test_invalid_arguments_are_reported_without_cuda():
     assert L.snisr_op_sample_sparse(None, None, 4, None, 0, 0, 0, 1.0, 8, 4, None, None, None) == _lib.INVALID_ARG
     assert L.snisr_op_tracing_tiles(None, 4, None, None, None, None, None, 1.0, 0, None, None) == _lib.INVALID_ARG
     assert L.snisr_diag_mma(None, None, None, 48, 0, 0, None) == _lib.INVALID_ARG
+    waited = C.c_int64()
+    assert L.snisr_diag_wait_timeout(0, C.byref(waited), None) == _lib.INVALID_ARG
+    assert L.snisr_diag_wait_timeout(11_000_000_000, C.byref(waited), None) == _lib.INVALID_ARG
+    assert L.snisr_diag_wait_timeout(1000, None, None) == _lib.INVALID_ARG
     t = _lib.Tuning(128, 16, 0, 128, 2)
     assert L.snisr_scene_set_tuning(None, C.byref(t)) == _lib.INVALID_ARG
     assert L.snisr_scene_get_tuning(None, C.byref(t)) == _lib.INVALID_ARG

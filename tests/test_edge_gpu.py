@@ -149,3 +149,27 @@ def test_sample_bg_all_background_missing(cuda):
     z = ops.sampling_background(_t(ro), _t(rd), _t(bg), _t(np.zeros(3, np.float32)), 3.0, ns, 0.5)
     torch.cuda.synchronize()
     assert (z.cpu().numpy() == -1).all()
+
+
+def test_bounded_wait_reports_timeout_and_context_stays_usable(cuda):
+    """A kernel wait on an mbarrier that nothing completes gives up after its
+    time limit and reports it (no fault, no hang); the context is usable
+    afterwards: a render right after it matches the oracle."""
+    import ctypes as C
+    import torch
+    from snisr import _lib
+    waited = C.c_int64()
+    assert snisr.lib().snisr_diag_wait_timeout(20_000_000, C.byref(waited), None) == _lib.DEVICE_TIMEOUT
+    assert 20_000_000 <= waited.value < 1_000_000_000, waited.value
+    s = snisr.SynthScene(snisr.CFG1)
+    sc = snisr.Scene(s.desc)
+    cam = s.camera(0, 64, 48)
+    rgb, depth, opac = sc.render(cam, snisr.FORM_PLAIN_FP32)
+    torch.cuda.synchronize()
+    sc.check()
+    d = oracle.camera_dirs(cam)
+    o = oracle.camera_origins(cam, d.shape[0])
+    osc = oracle.OracleScene(s.desc)
+    _, _, oop, _ = osc.render(o, d, None, 0)
+    assert np.abs(opac.cpu().numpy() - oop).max() <= 1e-5
+    sc.close()
