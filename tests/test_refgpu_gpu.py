@@ -17,7 +17,10 @@ from snisr import octree, ops
 import refgpu
 
 pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(not refgpu.available("compute_rays"), reason="reference cubins not built")]
+              pytest.mark.skipif(not refgpu.available("compute_rays", "raytile_tracing", "raydiffuse_render_octree_fp16",
+                                                      "rayreflection_render", "sampling", "volume_rendering",
+                                                      "reorder", "Sample_kernel", "Helper_kernel"),
+                                 reason="reference cubins not built")]
 
 
 def _t(a):
