@@ -464,3 +464,91 @@ def test_reference_frame_timing(cuda):
         r = sum(acc["ref"].values()) if n == "total" else acc["ref"][n]
         o = sum(acc["ours"].values()) if n == "total" else acc["ours"][n]
         print(f"{n:22s} {r / frames:10.4f} {o / frames:10.4f} {r / max(o, 1e-9):8.2f}x")
+
+
+def test_reference_training_ops_timing(cuda):
+    """CUDA_EXT's ops on the reference's own kernels (training/src, launch
+    shapes of its host wrappers: 512 threads) against the drop-ins, CUDA
+    events on the current stream, L2 flushed before every call; prints the
+    table and checks the outputs are identical."""
+    import torch
+    from snisr import prune
+    flush = torch.empty(64 * 1024 * 1024, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn, reps=5):
+        ms = []
+        for _ in range(reps + 1):
+            flush.zero_()
+            ev[0].record()
+            fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms.append(ev[0].elapsed_time(ev[1]))
+        return float(np.median(ms[1:]))
+
+    rows = []
+    # Sample_sparse: 65,536 rays through a 64^3 tile, 64 samples per ray
+    s1 = snisr.SynthScene(snisr.CFG1)
+    N = s1.desc.res
+    bits = np.unpackbits(s1.arrays()["occupancy"].view(np.uint8), bitorder="little")[: N ** 3]
+    flags = _t(bits.astype(np.int16).reshape(N, N, N))
+    rng = np.random.default_rng(5)
+    B, ns = 65536, 64
+    ro = _t(rng.uniform(0.2, 1.8, (B, 3)).astype(np.float32))
+    rdn = rng.standard_normal((B, 3)).astype(np.float32)
+    rd = _t(rdn / np.linalg.norm(rdn, axis=1, keepdims=True))
+    out = {}
+    for who, fn in (("ref", refgpu.Sample_sparse), ("ours", ops.Sample_sparse)):
+        z = torch.full((B, ns), -1.0, device="cuda")
+        dd = torch.full((B, ns), -1.0, device="cuda")
+        t = timed(lambda: fn(ro, rd, flags, 1.0, 1.0, 1.0, 2.0, N, z, dd))
+        out[who] = (t, _n(z), _n(dd))
+    assert np.array_equal(out["ours"][1], out["ref"][1]) and np.array_equal(out["ours"][2], out["ref"][2])
+    rows.append(("Sample_sparse (65,536 rays, 64^3 tile)", out["ref"][0], out["ours"][0]))
+    # Sample_bg: 65,536 rays, 16 samples
+    center = np.array([1.5, 4.5, 1.5], np.float32)
+    rob = _t((center + rng.uniform(-6, 6, (B, 3))).astype(np.float32))
+    rdb = _t(rng.standard_normal((B, 3)).astype(np.float32))
+    bg = _t(rng.uniform(0.0, 12.0, (B, 1)).astype(np.float32))
+    for who, fn in (("ref", refgpu.Sample_bg), ("ours", ops.Sample_bg)):
+        z = torch.full((B, 16), -1.0, device="cuda")
+        t = timed(lambda: fn(rob, rdb, bg, _t(center), 3.0, 0.6, z))
+        out[who] = (t, _n(z))
+    assert np.array_equal(out["ours"][1], out["ref"][1])
+    rows.append(("Sample_bg (65,536 rays, 16 samples)", out["ref"][0], out["ours"][0]))
+    # transparency_statistic: the camera rays of 4 640x360 views crossing one 128^3 tile, step 0.1 voxel
+    s = snisr.SynthScene(snisr.CFG2)
+    a = s.arrays()
+    sig_d, _, fl = prune.grids_from_arrays(s.desc, a, 5)
+    c5 = prune.tile_centers(s.desc, a)[5].astype(np.float32)
+    tile = float(s.desc.tile_size)
+    N2 = int(s.desc.res)
+    vs = tile / N2
+    D = N2 + 2
+    ros, rds = [], []
+    for v in range(4):
+        cam = s.camera(v, 640, 360)
+        d = oracle.camera_dirs(cam)
+        ros.append(oracle.camera_origins(cam, d.shape[0]))
+        rds.append(d)
+    rot, rdt = _t(np.concatenate(ros).astype(np.float32)), _t(np.concatenate(rds).astype(np.float32))
+    sg, flt, cen = _t(sig_d), _t(fl), _t(c5)
+    for who, fn in (("ref", refgpu.transparency_statistic), ("ours", ops.transparency_statistic)):
+        T = torch.zeros((D, D, D), device="cuda")
+        t = timed(lambda: (T.zero_(), fn(rot, rdt, D, cen, tile, vs, vs * 0.1, sg, flt, T)))
+        out[who] = (t, _n(T))
+    assert np.array_equal(out["ours"][1], out["ref"][1])
+    rows.append((f"transparency_statistic ({rot.shape[0]:,} rays, 128^3 tile)", out["ref"][0], out["ours"][0]))
+    # dilate_boundary on a 130^3 grid
+    f = _t(np.random.default_rng(11).choice(np.array([-1, 0, 1], np.int16), size=(130,) * 3, p=[0.89, 0.1, 0.01]))
+    for who, fn in (("ref", refgpu.dilate_boundary), ("ours", ops.dilate_boundary)):
+        g = f.clone()
+        t = timed(lambda: (g.copy_(f), fn(g, 130)))
+        out[who] = (t, _n(g))
+    assert np.array_equal(out["ours"][1], out["ref"][1])
+    rows.append(("dilate_boundary (130^3)", out["ref"][0], out["ours"][0]))
+    print("\nCUDA_EXT ops, ms per call (L2 flushed):")
+    print(f"{'op':48s} {'reference':>10s} {'drop-in':>10s} {'speed-up':>9s}")
+    for name, r, o in rows:
+        print(f"{name:48s} {r:10.4f} {o:10.4f} {r / max(o, 1e-9):8.2f}x")
