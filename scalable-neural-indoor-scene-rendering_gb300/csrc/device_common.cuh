@@ -60,6 +60,24 @@ __device__ __forceinline__ float2 slab(const float o[3], const float d[3], const
   return make_float2(lo, hi);
 }
 
+// The same slab test with the reciprocals of the direction computed once per
+// ray (safe_div(1, d[a]), as slab() computes them on every call).
+__device__ __forceinline__ float2 slab_inv(const float o[3], const float inv[3], const float c[3], float h) {
+  float lo = 0.0f, hi = 100000.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float l = fmul(fsub(fsub(c[a], h), o[a]), inv[a]);
+    float u = fmul(fsub(fadd(c[a], h), o[a]), inv[a]);
+    if (u < l) { float t = l; l = u; u = t; }
+    if (u < lo) return make_float2(-1.0f, -1.0f);
+    if (l > hi) return make_float2(-1.0f, -1.0f);
+    lo = (l > lo) ? l : lo;
+    hi = (u < hi) ? u : hi;
+    if (lo > hi) return make_float2(-1.0f, -1.0f);
+  }
+  return make_float2(lo, hi);
+}
+
 // voxel_traversal (rendering/src/include/cuda_utils.h:158-238) over the tile
 // grid: p is the start in scene-local coordinates, the visited sparse ids
 // (dense cells mapping to -1 are skipped) go to vis[0..K).

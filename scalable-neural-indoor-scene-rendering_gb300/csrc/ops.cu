@@ -105,6 +105,8 @@ __global__ void op_sample_sparse_kernel(const float* __restrict__ ro, const floa
     float d[3] = {rd[3 * i], rd[3 * i + 1], rd[3 * i + 2]};
     float2 nf = slab_scalar(o, d, center, half);
     if (nf.x == -1.0f && nf.y == -1.0f) continue;
+    // every per-voxel slab test of the ray divides by the same direction
+    const float inv_d[3] = {safe_div(1.0f, d[0]), safe_div(1.0f, d[1]), safe_div(1.0f, d[2])};
     float near = nf.x, far = nf.y;
     float total = 0.0f;
     float loc[3], nb[3], tmax[3], tdel[3];
@@ -122,7 +124,7 @@ __global__ void op_sample_sparse_kernel(const float* __restrict__ ro, const floa
     auto voxel_bound = [&](const int* c) {
       float vc[3];
       for (int a = 0; a < 3; ++a) vc[a] = fadd(ffma((float)c[a], vs, minc[a]), fmul(0.5f, vs));
-      return slab_scalar(o, d, vc, fmul(0.5f, vs));
+      return slab_inv(o, inv_d, vc, fmul(0.5f, vs));
     };
     auto step = [&]() {
       int a = (tmax[0] < tmax[1]) ? ((tmax[0] < tmax[2]) ? 0 : 2) : ((tmax[1] < tmax[2]) ? 1 : 2);
