@@ -58,8 +58,26 @@ __global__ void raygen_kernel(SceneDev S, CamDev cam, const float* __restrict__ 
     ray_o[i] = make_float4(o[0], o[1], o[2], 0.0f);
     ray_d[i] = make_float4(d[0], d[1], d[2], ts);
     if (want_enc) {
-      float e[27];
-      dir_encoding(d, 4, e);
+      // the FP16 view encoding of the tensor-core form: [d, sin(2^i d),
+      // cos(2^i d)] for i < 4 from one sincosf per axis and double-angle steps
+      // (a few FP32 ulps at 2^3, far below the encoding's FP16 rounding)
+      float e[27], sn[3], cs[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        e[a] = d[a];
+        sincosf(d[a], &sn[a], &cs[a]);
+      }
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          e[3 + 6 * f + a] = sn[a];
+          e[6 + 6 * f + a] = cs[a];
+          const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
+          sn[a] = s2;
+          cs[a] = c2;
+        }
+      }
       __align__(16) __half h[32];
       for (int k = 0; k < 32; ++k) h[k] = __float2half_rn(k < 27 ? e[k] : 0.0f);
       const uint4* src = reinterpret_cast<const uint4*>(h);
