@@ -173,3 +173,41 @@ def test_bounded_wait_reports_timeout_and_context_stays_usable(cuda):
     _, _, oop, _ = osc.render(o, d, None, 0)
     assert np.abs(opac.cpu().numpy() - oop).max() <= 1e-5
     sc.close()
+
+
+@pytest.mark.parametrize("case", ["all_miss", "one_ray", "mixed"])
+def test_render_tc_frames_without_or_with_few_samples(cuda, case):
+    """The tensor-core render on frames that give the MLP no chunk at all
+    (every ray misses the scene), one ray, and a ragged mix of misses and
+    hits: colour, depth and opacity against the oracle, and an error word
+    that stays clear."""
+    import torch
+    s = snisr.SynthScene(snisr.CFG1)
+    sc = snisr.Scene(s.desc)
+    osc = oracle.OracleScene(s.desc)
+    cam = s.camera(0)
+    d_all = oracle.camera_dirs(cam)
+    o_all = oracle.camera_origins(cam, d_all.shape[0])
+    rng = np.random.default_rng(4)
+    away_o = np.tile(np.array([[-10.0, -10.0, -10.0]], np.float32), (300, 1))
+    away_d = np.tile(np.array([[-1.0, 0.0, 0.0]], np.float32), (300, 1))
+    if case == "all_miss":
+        o, d = away_o, away_d
+    elif case == "one_ray":
+        k = d_all.shape[0] // 2 + cam.width // 2  # the centre pixel
+        o, d = o_all[k:k + 1], d_all[k:k + 1]
+    else:
+        pick = rng.choice(d_all.shape[0], 333, replace=False)
+        o = np.concatenate([o_all[pick], away_o[:77]])
+        d = np.concatenate([d_all[pick], away_d[:77]])
+    o, d = np.ascontiguousarray(o, np.float32), np.ascontiguousarray(d, np.float32)
+    rgb, depth, opac = sc.render_rays(_t(o), _t(d), snisr.FORM_TC)
+    torch.cuda.synchronize()
+    sc.check()
+    orgb, odep, oop, _ = osc.render(o, d, None, 1)
+    assert np.abs(opac.cpu().numpy() - oop).max() <= 1e-5
+    assert float(np.sqrt(((rgb.cpu().numpy() - orgb) ** 2).mean())) <= 1e-3
+    assert np.abs(rgb.cpu().numpy() - orgb).max() <= 1e-2
+    if case == "all_miss":
+        assert (opac.cpu().numpy() == 0).all() and (rgb.cpu().numpy() == 0).all()
+    sc.close()
