@@ -469,7 +469,10 @@ __global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* 
 // Every Linear, the output one included (N = 16, 3 used), is FP16 x FP16 ->
 // FP32 on tcgen05; biases enter as one extra K = 16 step (A = 1/16
 // everywhere, B slice = 16 copies of the bias).  The epilogue applies ReLU
-// (hidden) or sigmoid + compositing weight (output).
+// (hidden) or sigmoid + compositing weight (output).  Persistent CTAs (four
+// per SM) pull chunks from a device work queue and run a software pipeline:
+// the next chunk's A rows are gathered into registers during the current
+// chunk's MMA chain.
 template <int F, int H, int L>
 __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const SampleRec* __restrict__ sorted, int* ctrl,
                                                      int NT, const uint4* __restrict__ enc,
@@ -517,10 +520,9 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   bool failed = false;
   tc::Drain drain;
 
-  // Chunks are claimed one ahead: while chunk c runs its MMA chain, thread 0
-  // has already claimed the next chunk (slots alternate by iteration parity)
-  // and every thread loads its own row's record of that chunk (32 rows per
-  // warp: thread tid holds row tid), so the next gather starts from registers.
+  // A chunk: its tile and its rows [row0, row0 + cnt) of the tile-sorted
+  // sample records (locate: binary search of the per-tile chunk offsets).
+  // load_row: thread tid's row record of a chunk (32 rows per warp).
   struct ChunkRows {
     int c, tile, row0, cnt;
   };
