@@ -202,24 +202,46 @@ __global__ void op_inverse_z_kernel(const float* __restrict__ rays_d, const floa
 
 // integrate_points_kernel (rendering/src/volume_rendering.cu:5-58), 16 samples
 // per call, transmittance carried across calls; the reference's exponential
-// is the __expf intrinsic.
-__global__ void op_integrate_kernel(const float4* __restrict__ rgba, const float* __restrict__ dz, int64_t npix,
-                                    float early, float* frame, float* trans) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
-    float T = trans[i];
-    if (T < early) continue;
-    float c[3] = {0.f, 0.f, 0.f};
-    for (int s = 0; s < 16; ++s) {
-      float4 v = rgba[i * 16 + s];
-      float alpha = fsub(1.0f, __expf(fmul(fmul(-1.0f, v.w), dz[i * 16 + s])));
-      float w = fmul(alpha, T);
-      c[0] = ffma(w, v.x, c[0]);
-      c[1] = ffma(w, v.y, c[1]);
-      c[2] = ffma(w, v.z, c[2]);
-      T = fmul(T, fsub(1.0f, alpha));
+// is the __expf intrinsic.  A block stages its pixels' samples in shared
+// memory with coalesced loads (one thread per pixel reading its own 256-byte
+// row makes every load instruction touch 32 scattered sectors), rows padded
+// to 17 entries so that the per-pixel reads are free of bank conflicts; each
+// pixel is then composited in the reference's order.
+constexpr int kIntPix = 128;  // pixels (and threads) per block
+__global__ void __launch_bounds__(kIntPix) op_integrate_kernel(const float4* __restrict__ rgba,
+                                                              const float* __restrict__ dz, int64_t npix,
+                                                              float early, float* frame, float* trans) {
+  __shared__ float4 s_rgba[kIntPix * 17];
+  __shared__ float s_dz[kIntPix * 17];
+  for (int64_t base = (int64_t)blockIdx.x * kIntPix; base < npix; base += (int64_t)gridDim.x * kIntPix) {
+    const int cnt = (int)(npix - base < kIntPix ? npix - base : kIntPix);
+    for (int j = threadIdx.x; j < cnt * 16; j += kIntPix) {
+      const int p = j >> 4, q = j & 15;
+      s_rgba[p * 17 + q] = rgba[base * 16 + j];
+      s_dz[p * 17 + q] = dz[base * 16 + j];
     }
-    trans[i] = T;
-    for (int a = 0; a < 3; ++a) frame[3 * i + a] = fadd(frame[3 * i + a], c[a]);
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const int64_t i = base + threadIdx.x;
+      float T = trans[i];
+      if (!(T < early)) {  // the reference skips a pixel when T < early
+        const float4* v4 = s_rgba + threadIdx.x * 17;
+        const float* d1 = s_dz + threadIdx.x * 17;
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int q = 0; q < 16; ++q) {
+          const float4 v = v4[q];
+          float alpha = fsub(1.0f, __expf(fmul(fmul(-1.0f, v.w), d1[q])));
+          float w = fmul(alpha, T);
+          c[0] = ffma(w, v.x, c[0]);
+          c[1] = ffma(w, v.y, c[1]);
+          c[2] = ffma(w, v.z, c[2]);
+          T = fmul(T, fsub(1.0f, alpha));
+        }
+        trans[i] = T;
+        for (int a = 0; a < 3; ++a) frame[3 * i + a] = fadd(frame[3 * i + a], c[a]);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -313,7 +335,7 @@ snisr_status snisr_op_integrate_points(const float* rgba, const float* dz, int64
   if (npix < 0) return set_error(SNISR_INVALID_ARG, "integrate_points: bad size");
   if (npix == 0) return SNISR_OK;
   if (!rgba || !dz || !frame || !trans) return set_error(SNISR_INVALID_ARG, "integrate_points: null argument");
-  op_integrate_kernel<<<blocks_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(
+  op_integrate_kernel<<<blocks_for(npix, kIntPix), kIntPix, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float4*>(rgba), dz, npix, early, frame, trans);
   OP_CHECK("integrate_points");
   return SNISR_OK;
