@@ -295,3 +295,40 @@ def test_assign_pixels_known_answer():
     oracle.op_assign_pixels(net, pixel_starts, block_starts, new_net, new_ps)
     assert new_net.tolist() == [7, 7, 7, 2]
     assert new_ps.tolist() == [0, 44, 87, 130]
+
+
+def _fma32(a, b, c):
+    """Correctly rounded binary32 a*b + c: the product is exact in binary64,
+    the sum's rounding error is recovered exactly (two-sum) and the binary64
+    sum is rounded to odd before the final rounding to binary32, which makes
+    that final rounding correct."""
+    a, b, c = (np.asarray(x, np.float32).astype(np.float64) for x in (a, b, c))
+    p = a * b
+    s = p + c
+    bb = s - p
+    e = (p - (s - bb)) + (c - bb)
+    odd = (s.view(np.int64) & 1) == 1
+    s = np.where((e != 0) & ~odd, np.nextafter(s, np.where(e > 0, np.inf, -np.inf)), s)
+    return s.astype(np.float32)
+
+
+def test_compute_rays_states_the_fused_operation():
+    """The oracle's compute_rays is fma(c0, x, c1 * y) + c2 per component
+    with one rounding in the fma (the form the reference's nvcc build
+    compiles get_direction to), on random cameras: checked against an
+    independent binary64 model of the same expression."""
+    rng = np.random.default_rng(12)
+    for _ in range(4):
+        H, W = 24, 40
+        intr = np.array([rng.uniform(10, 30), rng.uniform(5, 20), rng.uniform(1e-3, 5e-2)], np.float32)
+        rot = rng.standard_normal((3, 3)).astype(np.float32)
+        got = oracle.op_compute_rays(intr, rot, H, W).reshape(H, W, 3)
+        py, px = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+        x = ((px.astype(np.float32) - intr[0]) * intr[2]).astype(np.float32)
+        y = ((py.astype(np.float32) - intr[1]) * intr[2]).astype(np.float32)
+        want = np.stack([(_fma32(rot[a, 0], x, (rot[a, 1] * y).astype(np.float32)) + rot[a, 2]).astype(np.float32)
+                         for a in range(3)], -1)
+        assert np.array_equal(got, want)
+        unfused = np.stack([(((rot[a, 0] * x).astype(np.float32) + (rot[a, 1] * y).astype(np.float32))
+                             .astype(np.float32) + rot[a, 2]).astype(np.float32) for a in range(3)], -1)
+        assert not np.array_equal(got, unfused)  # the test can tell the two forms apart
