@@ -7,9 +7,12 @@ reference file:line each function follows.
 Parity pinning: the reference has no tests or golden vectors for this path.
 The restatement is pinned (a) against the reference's own header functions
 compiled for the host from the reference tree by oracle/build_ref.py (only
-where the reference tree is present), and (b) against golden vectors made by
+where the reference tree is present), (b) against golden vectors made by
 running the reference's Python code (training/scripts/utils.py volume_rendering,
-tile.py query_voxel, networks.py PE/MLP) with tests/golden/make_golden.py.
+tile.py query_voxel, networks.py PE/MLP) with tests/golden/make_golden.py, and
+(c) against golden vectors written on the GPU by the reference's own CUDA
+kernels, compiled from its sources into cubins by oracle/build_ref.py
+(tests/golden/make_refgpu_golden.py, tests/test_oracle_refgpu_golden.py).
 """
 from __future__ import annotations
 
