@@ -169,7 +169,9 @@ snisr_status snisr_render_host_wait(snisr_scene* scene);
  * of their own, and real-time frame loops that must not block on the
  * allocator.  Ray staging uses a 2 MiB file-scope __device__ array that every
  * GPU loading the library holds until exit; the first call on a device looks
- * up its address, so make that call before any stream capture.  All calls
+ * up its address, so make that call before any stream capture.  The address
+ * is tied to the device's CUDA context: after a cudaDeviceReset the next call
+ * looks it up again (make that call before any capture as well).  All calls
  * share the array: calls that overlap on the GPU (other streams, other
  * threads) race and must be serialised by the caller.  Results equal
  * snisr_render_rays(..., SNISR_FORM_PLAIN_FP32, ...); n > 32768 is rejected

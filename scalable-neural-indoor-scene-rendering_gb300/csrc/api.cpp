@@ -223,7 +223,12 @@ snisr_status validate_desc(const snisr_scene_desc* d) {
   if (d->num_voxels >= (int64_t)0xFFFFFFF0) return set_error(SNISR_UNSUPPORTED, "scene_create: more than 2^32-16 voxels");
   if (d->num_triangles < 0 || (d->num_triangles > 0 && (!d->mesh_vertices || !d->mesh_faces)))
     return set_error(SNISR_INVALID_ARG, "scene_create: mesh data missing");
-  if (!(d->step_vox > 0.0f) || !(d->early_stop >= 0.0f)) return set_error(SNISR_INVALID_ARG, "scene_create: bad marching parameters");
+  if (!(d->step_vox > 0.0f) || !(d->early_stop >= 0.0f)) return set_error(SNISR_INVALID_ARG, "scene_create: bad marching parameters (step_vox > 0, early_stop >= 0)");
+  // A march position inside a tile stays below 2 tile sizes, whose float
+  // spacing is tile_size * 2^-22; steps of at least voxel / 1024 (>= tile_size
+  // * 2^-20 for res <= 1024) always advance it.
+  if (!(d->step_vox >= kMinStepVox) || !(d->step_vox <= 64.0f))
+    return set_error(SNISR_INVALID_ARG, "scene_create: step_vox must lie in [1/1024, 64] voxels");
   if (d->max_pixels < 0 || d->max_samples_per_ray < 0) return set_error(SNISR_INVALID_ARG, "scene_create: negative workspace bound");
   return SNISR_OK;
 }
@@ -510,6 +515,10 @@ snisr_status snisr_scene_check(snisr_scene* sc, void* stream) {
   uint32_t e = sc->err_host[0];
   CUDA_TRY(cudaMemsetAsync(sc->S.err, 0, 4, st), "scene_check");
   CUDA_TRY(cudaStreamSynchronize(st), "scene_check");
+  if (e & ERR_DRAIN)
+    return set_error(SNISR_DEVICE_TIMEOUT,
+                     "a bounded device wait ran out and the tensor-core work in flight did not finish: the CUDA "
+                     "context is unusable (destroy the scene and exit the process)");
   if (e & ERR_TIMEOUT) return set_error(SNISR_DEVICE_TIMEOUT, "a bounded device wait ran out");
   if (e & ERR_OVERFLOW) return set_error(SNISR_OVERFLOW, "sample workspace or traversal stack overflowed; raise max_samples_per_ray");
   if (e) return set_error(SNISR_CUDA_ERROR, "device error word set");
@@ -578,17 +587,40 @@ snisr_status snisr_render_host_async(snisr_scene* sc, const snisr_camera* cam, i
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t cap = sc->ws.max_rays;
   if (!sc->async_bufs) {
+    // Build the copy stream, the events and the staging into locals and
+    // publish them together, so that a failure part-way leaves the scene as
+    // it was (the next call sets everything up again).
+    cudaStream_t cs = nullptr;
+    cudaEvent_t rd[2] = {}, cd[2] = {};
     void* p = nullptr;
-    CUDA_TRY(cudaMalloc(&p, (size_t)cap * 5 * 4 * 2), "render_host_async: output staging");
-    sc->async_bufs = static_cast<float*>(p);
+    auto undo = [&]() {
+      for (int k = 0; k < 2; ++k) {
+        if (rd[k]) cudaEventDestroy(rd[k]);
+        if (cd[k]) cudaEventDestroy(cd[k]);
+      }
+      if (cs) cudaStreamDestroy(cs);
+      if (p) cudaFree(p);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&rd[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cd[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(cd[k], cs);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&p, (size_t)cap * 5 * 4 * 2);
+    if (e != cudaSuccess) {
+      undo();
+      return set_error(e == cudaErrorMemoryAllocation ? SNISR_OOM : SNISR_CUDA_ERROR,
+                       std::string("render_host_async: set-up: ") + cudaGetErrorString(e));
+    }
+    sc->copy_stream = cs;
+    for (int k = 0; k < 2; ++k) {
+      sc->render_done[k] = rd[k];
+      sc->copy_done[k] = cd[k];
+    }
     sc->allocs.push_back(p);
     sc->info.device_bytes += cap * 40;
-    CUDA_TRY(cudaStreamCreateWithFlags(&sc->copy_stream, cudaStreamNonBlocking), "render_host_async: copy stream");
-    for (int k = 0; k < 2; ++k) {
-      CUDA_TRY(cudaEventCreateWithFlags(&sc->render_done[k], cudaEventDisableTiming), "render_host_async: events");
-      CUDA_TRY(cudaEventCreateWithFlags(&sc->copy_done[k], cudaEventDisableTiming), "render_host_async: events");
-      CUDA_TRY(cudaEventRecord(sc->copy_done[k], sc->copy_stream), "render_host_async: events");
-    }
+    sc->async_bufs = static_cast<float*>(p);
   }
   const int k = sc->async_slot;
   sc->async_slot ^= 1;

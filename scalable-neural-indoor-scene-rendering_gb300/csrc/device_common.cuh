@@ -40,6 +40,16 @@ __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf
 // reference safe_divide (rendering/src/include/cutil_math.h:867-869)
 __device__ __forceinline__ float safe_div(float a, float b) { return b != 0.0f ? __fdiv_rn(a, b) : SNISR_INF; }
 
+// One step of a fixed-step march.  When the step is too small to change z
+// (below half the float spacing at z) the march would repeat the same sample
+// forever; the step then returns +inf, which ends every `while (z < far)`
+// loop.  For any step that does advance z the result is z + step, so outputs
+// are unchanged.
+__device__ __forceinline__ float march_next(float z, float step) {
+  const float zn = __fadd_rn(z, step);
+  return zn > z ? zn : SNISR_INF;
+}
+
 // Slab test with the reference's conventions (RayAABBIntersection,
 // rendering/src/include/cuda_utils.h:506-598): t_low starts at 0, t_high at
 // 1e5, a miss returns (-1, -1).
@@ -353,7 +363,7 @@ __device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Samp
       }
       s.interval = fminf(S.step_len, fsub(R.far_, R.z));
       s.t = fadd(R.t_in, R.z);
-      R.z = fadd(R.z, S.step_len);
+      R.z = march_next(R.z, S.step_len);
       return true;
     }
     if (!R.next_voxel(S)) return false;

@@ -74,10 +74,12 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   }
   bool ok = tid == 0 ? tc::mbar_wait(tc::smem_addr(bar), 0) : true;
   tc::fence_after_sync();
+  bool drained = true;
   if (__syncthreads_or(!ok)) {
     if (tid == 0) {
-      *status = 1;
-      (void)tc::mbar_wait(tc::smem_addr(bar), 0);  // once more, bounded: the MMAs are done before TMEM is freed
+      // once more, bounded: the MMAs must be done before TMEM is freed
+      drained = tc::mbar_wait(tc::smem_addr(bar), 0);
+      *status = drained ? 1 : 2;
     }
   } else {
     const int nc = mode == 0 ? N : 64;
@@ -89,8 +91,8 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
     if (tid == 0) *status = 0;
   }
   tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  // tensor memory stays allocated when the MMAs did not drain (status 2)
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
 __global__ void diag_wait_kernel(uint64_t limit_ns, long long* out) {

@@ -12,7 +12,12 @@
 // array's name is only a host-side stand-in, so its device address is
 // looked up with cudaGetSymbolAddress once per device (with that device
 // current) and cached; the first call on a device performs this set-up, so
-// make that first call before any stream capture on that device.
+// make that first call before any stream capture on that device.  The cache
+// remembers the id of the CUDA context the address belongs to: after a
+// cudaDeviceReset (a new context, the array loaded again, possibly at another
+// address) the next call sees a different id and looks the address up again,
+// so that first call after a reset also belongs before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,17 +39,48 @@ __device__ __align__(256) float4 g_noalloc_rays[2 * kNoAllocMaxRays];
 
 std::mutex g_symbol_mutex;
 float4* g_symbol_ptr[kMaxDevices] = {};
+unsigned long long g_symbol_ctx[kMaxDevices] = {};  // id of the context the cached address belongs to
 
-// Device address of g_noalloc_rays on the current device (set-up on first use).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId, through
+// the runtime's driver entry points, so the library needs no link to the
+// driver library); 0 when there is none or it cannot be read.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of g_noalloc_rays on the current device: looked up on the
+// first use and again whenever the device's context has changed.
 snisr_status noalloc_scratch(int device, float4** out) {
   if (device < 0 || device >= kMaxDevices) return set_error(SNISR_UNSUPPORTED, "render_rays_noalloc: device ordinal too large");
   std::lock_guard<std::mutex> lock(g_symbol_mutex);
-  if (!g_symbol_ptr[device]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_symbol_ptr[device] || ctx == 0 || ctx != g_symbol_ctx[device]) {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_rays);
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_rays);  // also brings up the device's context
     if (e != cudaSuccess || !p)
       return set_error(SNISR_CUDA_ERROR, std::string("render_rays_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_symbol_ptr[device] = static_cast<float4*>(p);
+    g_symbol_ctx[device] = current_context_id();
   }
   *out = g_symbol_ptr[device];
   return SNISR_OK;

@@ -112,7 +112,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
             }
             const bool inside = vl[0] >= 0 && vl[1] >= 0 && vl[2] >= 0 && vl[0] < D && vl[1] < D && vl[2] < D;
             if (!inside || !fl[vl[0] * DD + vl[1] * D + vl[2]]) {
-              z = fadd(z, sample_step);
+              z = march_next(z, sample_step);
               continue;
             }
             if (!first_hit && __hlt(T, trans_th)) {
@@ -163,7 +163,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
               for (int a = 0; a < 3; ++a) col[a] = __hfma(wgt, rgba[a], col[a]);
               T = __hmul_rn(T, __hsub_rn(one, alpha));
             }
-            z = fadd(z, sample_step);
+            z = march_next(z, sample_step);
           }
         }
         int a = 2;
@@ -200,6 +200,8 @@ extern "C" snisr_status snisr_op_rendering_diffuse_octree(
   if (npix < 0 || K <= 0 || num_tiles <= 0 || dilated_voxels <= 1 || !(tile_size > 0) || !(voxel_size > 0) ||
       !(sample_step > 0))
     return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: bad size");
+  if (!(sample_step >= voxel_size * kMinStepVox))
+    return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: sample_step below voxel_size / 1024");
   if (npix == 0) return SNISR_OK;
   if (!rays_d || !visited || !origin || !group_map || !data_voxels || !block_map || !node_map ||
       !sample_flags || !voxels_start || !centers || !frame || !inverse_near || !net_idx)

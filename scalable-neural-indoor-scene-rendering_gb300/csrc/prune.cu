@@ -76,7 +76,7 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
       }
       if (p[0] < 0 || p[1] < 0 || p[2] < 0 || p[0] >= D || p[1] >= D || p[2] >= D ||
           __ldg(nodes + p[0] * DD + p[1] * D + p[2]) != 1) {
-        z = fadd(z, step);
+        z = march_next(z, step);
         continue;
       }
       float f[3], x[3];
@@ -90,7 +90,7 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
         ok = ok && x0[a] >= 0 && x0[a] + 1 < D;
       }
       if (!ok) {  // flagged border cell: the reference asserts here; the sample is skipped
-        z = fadd(z, step);
+        z = march_next(z, step);
         continue;
       }
       const float ux = fsub(1.0f, x[0]), uy = fsub(1.0f, x[1]), uz = fsub(1.0f, x[2]);
@@ -124,7 +124,7 @@ __global__ void transparency_stat_kernel(const float* __restrict__ ro, const flo
       const float alpha = fsub(1.0f, expf(fmul(fmul(-1.0f, s), step)));
       T = fmul(T, fsub(1.0f, alpha));
       if (T < 0.00000001f) break;
-      z = fadd(z, step);
+      z = march_next(z, step);
     }
     if (cell >= 0) {
       const int off[8] = {0, 1, D, D + 1, DD, DD + 1, DD + D, DD + D + 1};
@@ -237,6 +237,8 @@ snisr_status snisr_op_transparency_statistic(const float* rays_start, const floa
                                              const int16_t* nodes, float* T_voxels, void* stream) {
   if (n < 0 || num_voxel < 2 || num_voxel > 1024 || !(tile_size > 0) || !(voxel_size > 0) || !(sample_step > 0))
     return set_error(SNISR_INVALID_ARG, "transparency_statistic: bad size (2 <= num_voxel <= 1024)");
+  if (!(sample_step >= voxel_size * kMinStepVox))
+    return set_error(SNISR_INVALID_ARG, "transparency_statistic: sample_step below voxel_size / 1024");
   if (n == 0) return SNISR_OK;
   if (!rays_start || !rays_dir || !tile_center || !voxels || !nodes || !T_voxels)
     return set_error(SNISR_INVALID_ARG, "transparency_statistic: null argument");

@@ -734,13 +734,15 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     my_ra = nra;
     my_rb = nrb;
   }
+  bool drained = true;
   if (failed && tid == 0) {
     atomicOr(S.err, ERR_TIMEOUT);
-    drain.run();
+    drained = drain.run();
+    if (!drained) atomicOr(S.err, ERR_DRAIN);
   }
   tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, H);
+  // tensor memory stays allocated when in-flight work did not drain
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, H);
 }
 
 inline int grid_for(int64_t n, int threads, int cap_blocks) {

@@ -46,7 +46,9 @@ struct SceneDev {
   uint32_t* err;                 // device error word
 };
 
-enum : uint32_t { ERR_OVERFLOW = 1u, ERR_TIMEOUT = 2u, ERR_TMEM = 4u };
+// ERR_DRAIN: after a wait ran out, the in-flight copy or MMAs did not finish
+// either; the CTA kept its tensor memory and the context is unusable.
+enum : uint32_t { ERR_OVERFLOW = 1u, ERR_TIMEOUT = 2u, ERR_TMEM = 4u, ERR_DRAIN = 8u };
 
 // One compacted sample of the batched form (32 bytes).
 struct __align__(16) SampleRec {

@@ -10,6 +10,12 @@
 namespace snisr {
 
 snisr_status set_error(snisr_status st, const std::string& msg);
+
+// Smallest fixed march step accepted by the entry points, in voxels.  Every
+// march position is a tile-local distance below two tile sizes, and a step of
+// voxel / 1024 is at least tile_size * 2^-20 for res <= 1024: four float
+// spacings at the largest position, so each step advances the march.
+constexpr float kMinStepVox = 1.0f / 1024.0f;
 float f16_bits_to_f32(uint16_t h);
 uint16_t f32_to_f16(float f);
 

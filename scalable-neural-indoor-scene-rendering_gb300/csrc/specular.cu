@@ -149,6 +149,7 @@ __global__ void assign_pixels_kernel(const int16_t* __restrict__ net, const int3
 // ---------------------------------------------------------------------------
 constexpr int kSpIn = 63, kSpH = 64, kSpHidden = 5, kSpOut = 28, kSpParams = 22556;
 constexpr uint32_t kErrTimeout = 2u;
+constexpr uint32_t kErrDrain = 8u;  // in-flight MMAs did not finish after a timeout: context unusable
 
 // reference parameter offsets: per layer bias[fo] then W[fi][fo]
 __host__ __device__ constexpr int sp_layer_off(int l) {
@@ -406,13 +407,15 @@ __global__ void __launch_bounds__(128, 3)
     }
     if (failed) break;
   }
+  bool drained = true;
   if (failed && tid == 0) {
     if (err) atomicOr(err, kErrTimeout);
-    drain.run();
+    drained = drain.run();
+    if (!drained && err) atomicOr(err, kErrDrain);
   }
   tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  // tensor memory stays allocated when in-flight work did not drain
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
 }  // namespace

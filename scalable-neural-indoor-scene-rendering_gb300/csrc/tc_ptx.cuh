@@ -59,7 +59,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint64_t
 // The barrier wait that ran out, kept so that the exit path can wait once
 // more (again bounded) for the copy or the MMAs still in flight before the
 // CTA frees its tensor memory and leaves: nothing of this CTA then writes
-// shared or tensor memory that a later CTA may own.
+// shared or tensor memory that a later CTA may own.  run() returns false when
+// that second wait also ran out: the work is still in flight, so the CTA must
+// not free its tensor memory (a later CTA could be given columns that the
+// MMAs still write).  The kernel then sets ERR_DRAIN and leaves the columns
+// allocated; the host reports the CUDA context as unusable.
 struct Drain {
   uint32_t bar = 0, phase = 0;
   bool pending = false;
@@ -68,9 +72,7 @@ struct Drain {
     phase = ph;
     pending = true;
   }
-  __device__ __forceinline__ void run() const {
-    if (pending) (void)mbar_wait(bar, phase);
-  }
+  __device__ __forceinline__ bool run() const { return !pending || mbar_wait(bar, phase); }
 };
 
 // Bulk global->shared copy through the TMA engine, completion counted on `bar`.

@@ -432,13 +432,15 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
     if (tid < cp.cnt)
       cout[cp.row0 + tid] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
   }
+  bool drained = true;
   if (failed && tid == 0) {
     atomicOr(S.err, ERR_TIMEOUT);
-    drain.run();
+    drained = drain.run();
+    if (!drained) atomicOr(S.err, ERR_DRAIN);
   }
   tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  // tensor memory stays allocated when in-flight work did not drain
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
 // ---------------------------------------------------------------------------
@@ -733,13 +735,15 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     tc::fence_after_sync();
     flush(cur_tile);
   }
+  bool drained = true;
   if (failed && tid == 0) {
     atomicOr(S.err, ERR_TIMEOUT);
-    drain.run();
+    drained = drain.run();
+    if (!drained) atomicOr(S.err, ERR_DRAIN);
   }
   tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  // tensor memory stays allocated when in-flight work did not drain
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 }  // namespace

@@ -63,6 +63,13 @@ def test_invalid_arguments_are_reported_without_cuda():
     bad = _lib.SceneDesc.from_buffer_copy(s.desc)
     bad.dir_freqs = 6
     assert L.snisr_scene_create(C.byref(bad), 0, C.byref(h)) == _lib.UNSUPPORTED
+    # a march step too small to advance the tile-local position is rejected
+    # (the march would otherwise repeat one sample forever)
+    for step in (1e-9, 1.0 / 2048, float("nan"), 100.0):
+        bad = _lib.SceneDesc.from_buffer_copy(s.desc)
+        bad.step_vox = step
+        assert L.snisr_scene_create(C.byref(bad), 0, C.byref(h)) == _lib.INVALID_ARG
+        assert b"step_vox" in L.snisr_last_error_string()
     # entry points reject null scenes and bad sizes before any CUDA call
     assert L.snisr_render(None, None, 0, None, None, None, None) == _lib.INVALID_ARG
     assert L.snisr_scene_check(None, None) == _lib.INVALID_ARG
@@ -149,6 +156,10 @@ def test_op_argument_validation_without_cuda():
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 6.4)) == BAD  # null buffers
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 0, 6.4)) == BAD
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 0.0)) == BAD
+    tiny = lambda step: (fake, fake, 10, 30) + (fake,) * 8 + (1, 6.4, 0.1, step, 18, 0.8, 0.01, 0, fake, fake, fake,
+                                                              None)
+    assert L.snisr_op_rendering_diffuse_octree(*tiny(1e-9)) == BAD  # step < voxel / 1024 would never advance z
+    assert b"sample_step" in L.snisr_last_error_string()
     # pruning
     assert L.snisr_op_transparency_statistic(None, None, 0, 18, None, 1.0, 0.0625, 0.006, None, None, None,
                                              None) == OK
@@ -156,6 +167,9 @@ def test_op_argument_validation_without_cuda():
                                              None) == BAD
     assert L.snisr_op_transparency_statistic(fake, fake, 5, 2000, fake, 1.0, 0.0625, 0.006, fake, fake, fake,
                                              None) == BAD
+    assert L.snisr_op_transparency_statistic(fake, fake, 5, 18, fake, 1.0, 0.0625, 1e-9, fake, fake, fake,
+                                             None) == BAD
+    assert b"sample_step" in L.snisr_last_error_string()
     assert L.snisr_op_dilate_boundary(None, 18, None) == BAD
     assert L.snisr_op_dilate_boundary(fake, 0, None) == BAD
     assert L.snisr_op_prune_flags(fake, fake, None, 18, 4, 0.5, 0.0, fake, None) == BAD  # 18 % 4 != 0

@@ -43,6 +43,17 @@ def test_noalloc_matches_allocating_entry_point(cuda):
         for a, b in zip(out, ref):
             assert float((a - b).abs().max()) <= TOL
         assert float(ref[2].max()) > 0.1  # the rays hit something
+    # the property the entry point exists for: once set up, calls allocate
+    # no device memory (the device's free bytes do not move over many calls)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(8):
+        _lib.check(L.snisr_render_rays_noalloc(sc.handle, od.data_ptr(), dd.data_ptr(), n, out[0].data_ptr(),
+                                               out[1].data_ptr(), out[2].data_ptr(), stream))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    for a, b in zip(out, ref):
+        assert float((a - b).abs().max()) <= TOL
     # sizes beyond the static scratch are rejected with a clear error
     st = L.snisr_render_rays_noalloc(sc.handle, od.data_ptr(), dd.data_ptr(), 32769, out[0].data_ptr(),
                                      out[1].data_ptr(), out[2].data_ptr(), stream)
