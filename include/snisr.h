@@ -222,23 +222,29 @@ snisr_status snisr_render_rays(snisr_scene* scene, const float* origins_dev,
  * BF16 operands (hi + lo, ~16 significant bits), backward products with
  * BF16 operands.  Sample records are kept in
  * a per-scene training workspace (grown on the first call of a larger batch,
- * n * max_samples_per_ray records) for the backward call. */
+ * n * max_samples_per_ray records) for the backward call.  *generation_out
+ * (may be NULL) receives a non-zero id of this forward's records; the next
+ * forward on the scene replaces them and takes a new id. */
 snisr_status snisr_train_forward(snisr_scene* scene, const float* vfeat_dev,
                                  const float* vdens_dev, const float* mlp_dev,
                                  const float* origins_dev, const float* dirs_dev,
                                  const int32_t* ray_tile_dev, int64_t n, int32_t form,
-                                 float* rgb_dev, void* stream);
-/* Hand-written adjoint of the preceding snisr_train_forward call on the same
- * scene and rays: per-ray reverse compositing with suffix sums, per-sample
- * recomputation of features and MLP activations.  grad_rgb_dev [n*3] =
- * dL/drgb; rgb_dev (the forward output) may be NULL.  Gradients are
+                                 float* rgb_dev, uint64_t* generation_out, void* stream);
+/* Hand-written adjoint of a snisr_train_forward call on the same scene and
+ * rays: per-ray reverse compositing with suffix sums, per-sample
+ * recomputation of features and MLP activations.  `generation` is the id
+ * that forward returned; if another forward ran on the scene since, its
+ * records are gone and the call returns SNISR_INVALID_ARG (instead of
+ * back-propagating through the other forward's samples).  grad_rgb_dev
+ * [n*3] = dL/drgb; rgb_dev (the forward output) may be NULL.  Gradients are
  * ACCUMULATED (+=) into gvfeat_dev [NV][F] (16-byte aligned), gvdens_dev [NV],
  * gmlp_dev [NT][P]. */
 snisr_status snisr_train_backward(snisr_scene* scene, const float* vfeat_dev,
                                   const float* vdens_dev, const float* mlp_dev,
                                   const float* origins_dev, const float* dirs_dev,
                                   const int32_t* ray_tile_dev, int64_t n, int32_t form,
-                                  const float* rgb_dev, const float* grad_rgb_dev,
+                                  uint64_t generation, const float* rgb_dev,
+                                  const float* grad_rgb_dev,
                                   float* gvfeat_dev, float* gvdens_dev, float* gmlp_dev,
                                   void* stream);
 
@@ -534,6 +540,13 @@ snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float*
  * Every kernel wait of this library has the same bound (2 s).  Synchronises
  * `stream`. */
 snisr_status snisr_diag_wait_timeout(int64_t limit_ns, int64_t* waited_ns, void* stream);
+
+/* The render march's own single-precision functions, elementwise on device
+ * arrays (no counterpart in the reference; a check of the transmittance
+ * arithmetic): fn 0 e^x for x <= 0, fn 1 log(1 + y) for y in [0, 1], fn 2
+ * softplus.  The host restatement gives the same bits. */
+snisr_status snisr_diag_march_math(int32_t fn, const float* x_dev, int64_t n, float* out_dev,
+                                   void* stream);
 
 const char* snisr_last_error_string(void);
 const char* snisr_version(void);

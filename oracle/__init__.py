@@ -56,7 +56,9 @@ def lib() -> C.CDLL:
             "oracle_scene_create": (P, [P]),
             "oracle_scene_destroy": (None, [P]),
             "oracle_camera_dirs": (None, [P, P]),
+            "oracle_march_math": (None, [C.c_int, P, C.c_int64, P]),
             "oracle_proxy": (None, [P, P, P, C.c_int64, P, P, P, C.c_int]),
+            "oracle_proxy_bvh": (None, [P, P, P, C.c_int64, P, P, P, C.c_int]),
             "oracle_trace": (None, [P, P, P, P, C.c_int64, C.c_int, P, P, C.c_int]),
             "oracle_render": (None, [P, P, P, P, C.c_int64, C.c_int, P, P, P, P, C.c_int]),
             "oracle_op_compute_rays": (None, [P, P, C.c_int, C.c_int, P]),
@@ -143,6 +145,16 @@ class OracleScene:
         th = np.zeros(n, np.float32)
         tri = np.zeros(n, np.int32)
         lib().oracle_proxy(self._h, _p(o), _p(d), n, _p(ts), _p(th), _p(tri), nthreads or threads())
+        return ts, th, tri
+
+    def proxy_bvh(self, o: np.ndarray, d: np.ndarray, nthreads: int | None = None):
+        """proxy() through the oracle's own hierarchy (built on first use): the
+        same results, in time fit for timing the host path on a full mesh."""
+        n = o.shape[0]
+        ts = np.zeros(n, np.float32)
+        th = np.zeros(n, np.float32)
+        tri = np.zeros(n, np.int32)
+        lib().oracle_proxy_bvh(self._h, _p(o), _p(d), n, _p(ts), _p(th), _p(tri), nthreads or threads())
         return ts, th, tri
 
     def double_hits(self, ro, rd, visited, nthreads: int | None = None):
@@ -232,6 +244,18 @@ class OracleScene:
 def camera_dirs(cam) -> np.ndarray:
     out = np.zeros((cam.height * cam.width, 3), np.float32)
     lib().oracle_camera_dirs(C.byref(cam), _p(out))
+    return out
+
+
+MATH_EXP, MATH_LOG1P, MATH_SOFTPLUS = 0, 1, 2
+
+
+def march_math(fn: int, x: np.ndarray) -> np.ndarray:
+    """The render march's single-precision e^x (x <= 0), log1p (y in [0, 1])
+    or softplus, elementwise on float32 input."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.empty_like(x)
+    lib().oracle_march_math(fn, _p(x), x.size, _p(out))
     return out
 
 

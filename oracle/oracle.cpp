@@ -38,6 +38,7 @@
 #include <cstdint>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "snisr.h"
@@ -121,6 +122,14 @@ inline int dda_axis(const float m[3]) {
   return (m[1] < m[2]) ? 1 : 2;
 }
 
+// Node of the oracle's own bounding-volume hierarchy over the proxy mesh
+// (only to time the host path on the full mesh; the nearest hit it returns is
+// the brute-force one).  Leaf: count > 0 triangles from `first` in `tri`.
+struct HostBvhNode {
+  float lo[3], hi[3];
+  int32_t first, count;  // inner node: children first, first + 1 (count 0)
+};
+
 struct Scene {
   const snisr_scene_desc* d;
   int N, NT, F, H, L, in, P;
@@ -129,6 +138,8 @@ struct Scene {
   std::vector<float> centers;      // [NT][3]
   std::vector<uint32_t> base;      // [NT*words] first global voxel of a word
   std::vector<float> vfeat, vdens; // vertex data as float
+  std::vector<HostBvhNode> bvh;    // built on first use by oracle_proxy_bvh
+  std::vector<int32_t> bvh_tri;
 };
 
 bool occupied(const Scene& s, int tile, int vid, uint32_t& rec) {
@@ -218,6 +229,45 @@ void march(const Scene& s, const float o[3], const float d[3], float t_start, Vi
 
 template <class T>
 T softplus(T x) { return std::max(x, T(0)) + std::log1p(std::exp(-std::fabs(x))); }
+
+// The render march's own single-precision exponential and log1p, as the
+// kernels define them (the transmittance they produce is specified bit for
+// bit, so these are the same operations in the same order; every float
+// operation here is one IEEE single-precision rounding: -ffp-contract=off,
+// std::fma is the fused multiply-add).
+//
+// e^x for x <= 0: Cody-Waite reduction x = k ln2 + r (ln2 = 16-bit head +
+// tail), degree-7 Taylor polynomial of e^r by Horner's rule, scaling by 2^k.
+// 0 below -80; NaN propagates.
+float exp_nonpos(float x) {
+  if (!(x >= -80.0f)) return x != x ? x : 0.0f;
+  const float k = std::nearbyint(x * 1.44269504088896341f);
+  float r = std::fma(-k, 0.693145751953125f, x);
+  r = std::fma(-k, 1.42860682030941723212e-6f, r);
+  const float c[8] = {1.98412698412698413e-4f, 1.38888888888888889e-3f, 8.33333333333333333e-3f,
+                      4.16666666666666667e-2f, 1.66666666666666667e-1f, 0.5f, 1.0f, 1.0f};
+  float p = c[0];
+  for (int i = 1; i < 8; ++i) p = std::fma(p, r, c[i]);
+  const uint32_t bits = (uint32_t)((int)k + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &bits, 4);
+  return p * scale;
+}
+
+// log(1 + y), y in [0, 1]: 2 atanh(y / (2 + y)) by its odd series to s^19.
+float log1p_unit(float y) {
+  const float s = y / (2.0f + y);
+  const float s2 = s * s;
+  const float c[10] = {5.26315789473684211e-2f, 5.88235294117647059e-2f, 6.66666666666666667e-2f,
+                       7.69230769230769231e-2f, 9.09090909090909091e-2f, 1.11111111111111111e-1f,
+                       1.42857142857142857e-1f, 2.0e-1f, 3.33333333333333333e-1f, 1.0f};
+  float q = c[0];
+  for (int i = 1; i < 10; ++i) q = std::fma(q, s2, c[i]);
+  const float t = s * q;
+  return t + t;
+}
+
+float softplus_march(float x) { return std::max(x, 0.0f) + log1p_unit(exp_nonpos(-std::fabs(x))); }
 template <class T>
 T sigmoid(T x) { return T(1) / (T(1) + std::exp(-x)); }
 
@@ -323,8 +373,14 @@ void render_ray(const Scene& s, const float o[3], const float d[3], float t_star
       const int32_t* cn = s.d->voxel_corners + (int64_t)rec * 8;
       T logit = 0;
       for (int k = 0; k < 8; ++k) logit += w[k] * (T)s.vdens[(size_t)cn[k]];
-      T sigma = softplus<T>(logit);
-      T alpha = T(1) - std::exp(-sigma * (T)(g.interval * s.inv_voxel));
+      T sigma, alpha;
+      if constexpr (std::is_same<T, float>::value) {  // the kernels' transmittance, bit for bit
+        sigma = softplus_march(logit);
+        alpha = 1.0f - exp_nonpos(-sigma * (g.interval * s.inv_voxel));
+      } else {
+        sigma = softplus<T>(logit);
+        alpha = T(1) - std::exp(-sigma * (T)(g.interval * s.inv_voxel));
+      }
       T wt = Tr * alpha;
       for (int c = 0; c < s.F; ++c) {
         T acc = 0;
@@ -419,6 +475,123 @@ float nearest_hit(const snisr_scene_desc* D, const float o[3], const float d[3],
   return bid >= 0 ? best : -1.0f;
 }
 
+// Median-split hierarchy over triangle centroids, at most 4 triangles per
+// leaf; node boxes are padded by 1e-4 of the mesh extent (plus 1e-5) so that
+// a hit whose rounded t lies a little outside its triangle's exact box is
+// still reached.
+void build_host_bvh(Scene& s) {
+  const snisr_scene_desc* D = s.d;
+  const int64_t nt = D->num_triangles;
+  s.bvh_tri.resize((size_t)nt);
+  std::vector<float> cen((size_t)nt * 3), tlo((size_t)nt * 3), thi((size_t)nt * 3);
+  float mlo[3] = {3e38f, 3e38f, 3e38f}, mhi[3] = {-3e38f, -3e38f, -3e38f};
+  for (int64_t t = 0; t < nt; ++t) {
+    s.bvh_tri[(size_t)t] = (int32_t)t;
+    for (int a = 0; a < 3; ++a) {
+      float lo = 3e38f, hi = -3e38f;
+      for (int k = 0; k < 3; ++k) {
+        const float v = D->mesh_vertices[3 * (int64_t)D->mesh_faces[3 * t + k] + a];
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+      tlo[(size_t)t * 3 + a] = lo;
+      thi[(size_t)t * 3 + a] = hi;
+      cen[(size_t)t * 3 + a] = 0.5f * (lo + hi);
+      mlo[a] = std::min(mlo[a], lo);
+      mhi[a] = std::max(mhi[a], hi);
+    }
+  }
+  float pad = 1e-5f;
+  for (int a = 0; a < 3; ++a) pad = std::max(pad, 1e-4f * (mhi[a] - mlo[a]) + 1e-5f);
+  struct Job { int32_t node, begin, end; };
+  s.bvh.clear();
+  s.bvh.push_back(HostBvhNode{});
+  std::vector<Job> jobs{{0, 0, (int32_t)nt}};
+  while (!jobs.empty()) {
+    const Job j = jobs.back();
+    jobs.pop_back();
+    HostBvhNode nd{};
+    float clo[3] = {3e38f, 3e38f, 3e38f}, chi[3] = {-3e38f, -3e38f, -3e38f};
+    for (int a = 0; a < 3; ++a) { nd.lo[a] = 3e38f; nd.hi[a] = -3e38f; }
+    for (int32_t i = j.begin; i < j.end; ++i) {
+      const int32_t t = s.bvh_tri[(size_t)i];
+      for (int a = 0; a < 3; ++a) {
+        nd.lo[a] = std::min(nd.lo[a], tlo[(size_t)t * 3 + a]);
+        nd.hi[a] = std::max(nd.hi[a], thi[(size_t)t * 3 + a]);
+        clo[a] = std::min(clo[a], cen[(size_t)t * 3 + a]);
+        chi[a] = std::max(chi[a], cen[(size_t)t * 3 + a]);
+      }
+    }
+    for (int a = 0; a < 3; ++a) { nd.lo[a] -= pad; nd.hi[a] += pad; }
+    if (j.end - j.begin <= 4) {
+      nd.first = j.begin;
+      nd.count = j.end - j.begin;
+      s.bvh[(size_t)j.node] = nd;
+      continue;
+    }
+    int axis = 0;
+    for (int a = 1; a < 3; ++a)
+      if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+    const int32_t mid = (j.begin + j.end) / 2;
+    std::nth_element(s.bvh_tri.begin() + j.begin, s.bvh_tri.begin() + mid, s.bvh_tri.begin() + j.end,
+                     [&](int32_t x, int32_t y) {
+                       const float cx = cen[(size_t)x * 3 + axis], cy = cen[(size_t)y * 3 + axis];
+                       return cx < cy || (cx == cy && x < y);
+                     });
+    nd.first = (int32_t)s.bvh.size();
+    nd.count = 0;
+    s.bvh[(size_t)j.node] = nd;
+    s.bvh.push_back(HostBvhNode{});
+    s.bvh.push_back(HostBvhNode{});
+    jobs.push_back({nd.first, j.begin, mid});
+    jobs.push_back({nd.first + 1, mid, j.end});
+  }
+}
+
+// Nearest hit through the hierarchy: the same triangle tests and the same
+// rule as nearest_hit (smallest t, ties to the lower triangle id); boxes
+// entered beyond the best t so far are skipped.
+float nearest_hit_bvh(const Scene& s, const float o[3], const float d[3], int& tri) {
+  const snisr_scene_desc* D = s.d;
+  float inv[3];
+  for (int a = 0; a < 3; ++a) inv[a] = d[a] != 0.0f ? 1.0f / d[a] : (std::signbit(d[a]) ? -kInf : kInf);
+  float best = 3.0e38f;
+  int bid = -1;
+  int32_t stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const HostBvhNode& nd = s.bvh[(size_t)stack[--sp]];
+    float t0 = 0.0f, t1 = best;
+    bool miss = false;
+    for (int a = 0; a < 3 && !miss; ++a) {
+      float ta = (nd.lo[a] - o[a]) * inv[a], tb = (nd.hi[a] - o[a]) * inv[a];
+      if (ta != ta) ta = -kInf;  // 0 * inf: the ray runs inside the slab's plane
+      if (tb != tb) tb = kInf;
+      if (ta > tb) std::swap(ta, tb);
+      t0 = std::max(t0, ta);
+      t1 = std::min(t1, tb);
+      miss = t0 > t1;
+    }
+    if (miss) continue;
+    if (nd.count > 0) {
+      for (int32_t i = nd.first; i < nd.first + nd.count; ++i) {
+        const int64_t t = s.bvh_tri[(size_t)i];
+        const float* A = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t];
+        const float* B = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 1];
+        const float* C = D->mesh_vertices + 3 * (int64_t)D->mesh_faces[3 * t + 2];
+        float th;
+        if (tri_hit(o, d, A, B, C, th) && (th < best || (th == best && t < bid))) { best = th; bid = (int)t; }
+      }
+    } else if (sp + 2 <= 128) {
+      stack[sp++] = nd.first;
+      stack[sp++] = nd.first + 1;
+    }
+  }
+  tri = bid;
+  return bid >= 0 ? best : -1.0f;
+}
+
 template <class F>
 void parallel_for(int64_t n, int threads, F&& fn) {
   if (threads <= 1 || n < 64) {
@@ -493,6 +666,14 @@ oracle_scene* oracle_scene_create(const snisr_scene_desc* d) {
 void oracle_scene_destroy(oracle_scene* s) { delete reinterpret_cast<Scene*>(s); }
 
 // Normalised camera directions, same operation order as the GPU ray setup.
+// The march's single-precision functions on an array (fn 0: e^x for x <= 0,
+// 1: log(1 + y) for y in [0, 1], 2: softplus), for checks of the kernels'
+// transmittance arithmetic.
+void oracle_march_math(int fn, const float* x, int64_t n, float* out) {
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = fn == 0 ? exp_nonpos(x[i]) : fn == 1 ? log1p_unit(x[i]) : softplus_march(x[i]);
+}
+
 void oracle_camera_dirs(const snisr_camera* cam, float* dirs) {
   for (int64_t i = 0; i < (int64_t)cam->width * cam->height; ++i) {
     int py = (int)(i / cam->width), px = (int)(i % cam->width);
@@ -512,6 +693,21 @@ void oracle_proxy(const oracle_scene* os, const float* o, const float* d, int64_
   parallel_for(n, threads, [&](int64_t i) {
     int id = -1;
     float th = s.d->num_triangles > 0 ? nearest_hit(s.d, o + 3 * i, d + 3 * i, id) : -1.0f;
+    if (t_hit) t_hit[i] = th;
+    if (tri) tri[i] = id;
+    if (t_start) t_start[i] = th >= 0.0f ? std::max(th - s.start_off, 0.0f) : 0.0f;
+  });
+}
+
+// oracle_proxy through the host hierarchy (same results; used to time the
+// host path with the same work per ray as the GPU's BVH walk).
+void oracle_proxy_bvh(oracle_scene* os, const float* o, const float* d, int64_t n, float* t_start, float* t_hit,
+                      int32_t* tri, int threads) {
+  Scene& s = *reinterpret_cast<Scene*>(os);
+  if (s.d->num_triangles > 0 && s.bvh.empty()) build_host_bvh(s);
+  parallel_for(n, threads, [&](int64_t i) {
+    int id = -1;
+    float th = s.d->num_triangles > 0 ? nearest_hit_bvh(s, o + 3 * i, d + 3 * i, id) : -1.0f;
     if (t_hit) t_hit[i] = th;
     if (tri) tri[i] = id;
     if (t_start) t_start[i] = th >= 0.0f ? std::max(th - s.start_off, 0.0f) : 0.0f;
@@ -649,9 +845,12 @@ struct TrainParams {
   // emul = 1: operand emulation of the tensor-core training form.  Forward
   // products (and the backward's recomputation) use split BF16 operands,
   // v = hi + lo with hi = bf16(v), lo = bf16(v - hi): MLP inputs, weights,
-  // biases and post-ReLU activations (rf).  Backward products use single
-  // BF16 operands (rb): the output-logit gradient, each hidden delta, W^T in
-  // the data gradient and the activation in the weight gradient.
+  // biases and post-ReLU activations (rf).  A product of two split operands
+  // is taken as three BF16 products, hi*hi + hi*lo + lo*hi: the lo*lo term
+  // is dropped, as the kernels issue three MMAs per K step (product3).
+  // Backward products use single BF16 operands (rb): the output-logit
+  // gradient, each hidden delta, W^T in the data gradient and the activation
+  // in the weight gradient.
   int emul = 0;
   double rf(double v) const {
     if (emul == 0) return v;
@@ -659,6 +858,13 @@ struct TrainParams {
     return (double)hi + (double)round_bf16((float)v - hi);
   }
   double rb(double v) const { return emul == 0 ? v : (double)round_bf16((float)v); }
+  // w * x for the forward products (exact when emul == 0)
+  double product3(double w, double x) const {
+    if (emul == 0) return w * x;
+    const float wh = round_bf16((float)w), xh = round_bf16((float)x);
+    const double wl = (double)round_bf16((float)w - wh), xl = (double)round_bf16((float)x - xh);
+    return (double)wh * (double)xh + (double)wh * xl + wl * (double)xh;
+  }
 };
 
 // Forward of one segment; returns the samples (with activations) and colour.
@@ -700,7 +906,7 @@ void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const flo
         std::vector<double> nx((size_t)fo);
         for (int oo = 0; oo < fo; ++oo) {
           double acc = p.rf(W[off + (int64_t)fi * fo + oo]);
-          for (int i = 0; i < fi; ++i) acc += p.rf(W[off + (int64_t)oo * fi + i]) * cur[(size_t)i];
+          for (int i = 0; i < fi; ++i) acc += p.product3(W[off + (int64_t)oo * fi + i], cur[(size_t)i]);
           nx[(size_t)oo] = l < s.L ? p.rf(std::max(acc, 0.0)) : acc;
         }
         off += (int64_t)fi * fo + fo;

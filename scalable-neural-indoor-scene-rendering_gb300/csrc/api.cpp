@@ -890,10 +890,12 @@ snisr_status snisr_scene_autotune_train(snisr_scene* sc, const float* vfeat, con
   CUDA_TRY(cudaEventCreate(&e0), "autotune_train: event");
   CUDA_TRY(cudaEventCreate(&e1), "autotune_train: event");
   auto step = [&]() -> snisr_status {
-    snisr_status s = snisr_train_forward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, rgb, stream);
+    uint64_t gen = 0;
+    snisr_status s =
+        snisr_train_forward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, rgb, &gen, stream);
     if (s != SNISR_OK) return s;
-    return snisr_train_backward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, rgb, grad, gF, gG,
-                                gW, stream);
+    return snisr_train_backward(sc, vfeat, vdens, mlp, origins, dirs, ray_tile, n, SNISR_FORM_TC, gen, rgb, grad, gF,
+                                gG, gW, stream);
   };
   auto eval = [&](float* ms) -> snisr_status {
     snisr_status s = step();

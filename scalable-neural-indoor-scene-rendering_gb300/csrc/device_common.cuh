@@ -381,13 +381,75 @@ __device__ __forceinline__ void trilinear_weights(const float f[3], float w[8]) 
 __device__ __forceinline__ float softplusf(float x) { return fmaxf(x, 0.0f) + log1pf(expf(-fabsf(x))); }
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
-// Density of a sample: softplus of the trilinear density logit, per voxel length.
+// Transmittance arithmetic of the render march.  Its exponential and log1p
+// are this library's own single-precision functions, evaluated with explicit
+// round-to-nearest operations and fused multiply-adds only where written, so
+// that the host restatement (the same operations in the same order) gives
+// the same bits: transmittance, and with it the early-stop decision, is then
+// identical on both sides.
+//
+// e^x for x <= 0: Cody-Waite reduction x = k ln2 + r with ln2 split into a
+// 16-bit head and a tail, |r| <= ln2/2; the degree-7 Taylor polynomial of e^r
+// (truncation error below 2^-26 on that interval) by Horner's rule in fused
+// multiply-adds; scaling by 2^k through the exponent field.  Below -80 the
+// result is 0 (e^-80 < 2^-115); NaN propagates.  Error below 1 ulp.
+__device__ __forceinline__ float exp_nonpos(float x) {
+  if (!(x >= -80.0f)) return x != x ? x : 0.0f;
+  const float k = rintf(__fmul_rn(x, 1.44269504088896341f));
+  float r = __fmaf_rn(-k, 0.693145751953125f, x);   // ln2 head (exact product)
+  r = __fmaf_rn(-k, 1.42860682030941723212e-6f, r);  // ln2 tail
+  float p = 1.98412698412698413e-4f;                 // 1/7!
+  p = __fmaf_rn(p, r, 1.38888888888888889e-3f);      // 1/6!
+  p = __fmaf_rn(p, r, 8.33333333333333333e-3f);      // 1/5!
+  p = __fmaf_rn(p, r, 4.16666666666666667e-2f);      // 1/4!
+  p = __fmaf_rn(p, r, 1.66666666666666667e-1f);      // 1/3!
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  return __fmul_rn(p, __int_as_float(((int)k + 127) << 23));  // k in [-116, 0]: an exact power of two
+}
+
+// log(1 + y) for y in [0, 1]: 2 atanh(s) with s = y / (2 + y) in [0, 1/3],
+// atanh(s) = s (1 + s^2/3 + s^4/5 + ... + s^18/19) (next term below 2^-35).
+// Error below 3 ulp (the roundings of 2 + y, the quotient and the product).
+__device__ __forceinline__ float log1p_unit(float y) {
+  const float s = __fdiv_rn(y, __fadd_rn(2.0f, y));
+  const float s2 = __fmul_rn(s, s);
+  float q = 5.26315789473684211e-2f;             // 1/19
+  q = __fmaf_rn(q, s2, 5.88235294117647059e-2f);  // 1/17
+  q = __fmaf_rn(q, s2, 6.66666666666666667e-2f);  // 1/15
+  q = __fmaf_rn(q, s2, 7.69230769230769231e-2f);  // 1/13
+  q = __fmaf_rn(q, s2, 9.09090909090909091e-2f);  // 1/11
+  q = __fmaf_rn(q, s2, 1.11111111111111111e-1f);  // 1/9
+  q = __fmaf_rn(q, s2, 1.42857142857142857e-1f);  // 1/7
+  q = __fmaf_rn(q, s2, 2.0e-1f);                  // 1/5
+  q = __fmaf_rn(q, s2, 3.33333333333333333e-1f);  // 1/3
+  q = __fmaf_rn(q, s2, 1.0f);
+  const float t = __fmul_rn(s, q);
+  return __fadd_rn(t, t);
+}
+
+// softplus(x) = max(x, 0) + log(1 + e^-|x|)
+__device__ __forceinline__ float softplus_march(float x) {
+  return __fadd_rn(fmaxf(x, 0.0f), log1p_unit(exp_nonpos(-fabsf(x))));
+}
+
+// Opacity of a sample: 1 - e^(-sigma * interval / voxel).
+__device__ __forceinline__ float alpha_march(float sigma, float dv) {
+  return __fsub_rn(1.0f, exp_nonpos(__fmul_rn(-sigma, dv)));
+}
+
+// Density of a sample: softplus of the trilinear density logit, per voxel
+// length; the logit summed corner by corner in order, unfused.
 __device__ __forceinline__ float sample_sigma(const SceneDev& S, const Sample& s, float w[8]) {
   trilinear_weights(s.f, w);
   const float4* dp = reinterpret_cast<const float4*>(S.dens + (size_t)s.rec * 8);
   float4 a = __ldg(dp), b = __ldg(dp + 1);
-  float g = w[0] * a.x + w[1] * a.y + w[2] * a.z + w[3] * a.w + w[4] * b.x + w[5] * b.y + w[6] * b.z + w[7] * b.w;
-  return softplusf(g);
+  const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  float g = __fmul_rn(w[0], v[0]);
+#pragma unroll
+  for (int k = 1; k < 8; ++k) g = __fadd_rn(g, __fmul_rn(w[k], v[k]));
+  return softplus_march(g);
 }
 
 // View-direction encoding: [d, sin(2^0 d), cos(2^0 d), ..., sin(2^{L-1} d), cos(2^{L-1} d)]

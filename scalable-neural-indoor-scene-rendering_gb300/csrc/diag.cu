@@ -12,9 +12,17 @@
 // given time limit: the bounded-wait error path of the tensor-core kernels
 // (the wait runs out, the kernel reports it and returns, the context stays
 // usable), exercised without a fault.
+// march_math_kernel: the render march's single-precision e^x, log1p and
+// softplus on an array, so that tests can compare their bits with the host
+// restatement.
 #include <cuda_runtime.h>
 
+#include <string>
+
+#include "device_common.cuh"
 #include "kernels.h"
+#include "snisr.h"
+#include "snisr_internal.h"
 #include "tc_ptx.cuh"
 
 namespace snisr {
@@ -111,6 +119,13 @@ __global__ void diag_wait_kernel(uint64_t limit_ns, long long* out) {
   }
 }
 
+__global__ void march_math_kernel(int fn, const float* __restrict__ x, int64_t n, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = x[i];
+    out[i] = fn == 0 ? exp_nonpos(v) : fn == 1 ? log1p_unit(v) : softplus_march(v);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_diag_wait(int64_t limit_ns, int64_t* waited_ns, bool* ran_out, cudaStream_t st) {
@@ -148,3 +163,17 @@ cudaError_t launch_diag_mma(const uint16_t* A, const uint16_t* B, float* D, int 
 }
 
 }  // namespace snisr
+
+extern "C" snisr_status snisr_diag_march_math(int32_t fn, const float* x_dev, int64_t n, float* out_dev,
+                                              void* stream) {
+  using namespace snisr;
+  if (fn < 0 || fn > 2 || n < 0 || (n > 0 && (!x_dev || !out_dev)))
+    return set_error(SNISR_INVALID_ARG, "diag_march_math: bad argument (fn 0..2, device arrays of n floats)");
+  if (n == 0) return SNISR_OK;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 65536) blocks = 65536;
+  march_math_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(fn, x_dev, n, out_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(SNISR_CUDA_ERROR, std::string("diag_march_math: ") + cudaGetErrorString(e));
+  return SNISR_OK;
+}

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const flo
       while (next_sample(S, R, s)) {
         float w[8];
         float sig = sample_sigma(S, s, w);
-        float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
+        float alpha = alpha_march(sig, fmul(s.interval, S.inv_voxel));
         float wt = T * alpha;
         const float4* fp = S.feat32 + (size_t)s.rec * (F / 4) * 8;
 #pragma unroll
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const flo
         float out[3];
         mlp_plain<KIN, H, L>(S.mlp_plain + (size_t)s.tile * S.plain_stride, x, out);
         for (int c = 0; c < 3; ++c) C[c] += wt * sigmoidf_(out[c]);
-        D += wt * s.t;
+        D = fadd(D, fmul(wt, s.t));
         T *= (1.0f - alpha);
         if (T < S.early_stop) break;
       }
@@ -289,9 +289,9 @@ __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S
         }
         float w[8];
         const float sig = sample_sigma(S, s, w);
-        const float alpha = 1.0f - expf(-sig * fmul(s.interval, S.inv_voxel));
+        const float alpha = alpha_march(sig, fmul(s.interval, S.inv_voxel));
         const float wt = T * alpha;
-        D += wt * s.t;
+        D = fadd(D, fmul(wt, s.t));
         T *= (1.0f - alpha);
         vrec = s.rec;
         vtile = (uint32_t)s.tile;

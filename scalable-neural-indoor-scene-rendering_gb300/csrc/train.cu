@@ -408,13 +408,16 @@ __global__ void __launch_bounds__(128) tr_mlp_bwd_plain(SceneDev S, const float*
 
 // Weight gradients: for tile t, layer l: dW[o][i] += sum_s delta_l[s][o] h_{l-1}[s][i],
 // db[o] += sum_s delta_l[s][o].  Block = (sample block of kDwBlock, layer, tile);
-// 256 threads each own outputs (o, i) strided over fo x (fi + 1).
+// 256 threads each own outputs (o, i) strided over fo x (fi + 1): kPerThread
+// of them, enough for the largest layer (H x (max(IN, H) + 1) outputs).
 constexpr int kDwBlock = 512;
 
 template <int F, int H, int L>
 __global__ void __launch_bounds__(256) tr_dw_kernel(const float* __restrict__ act, const float* __restrict__ dlt,
                                                     const int32_t* __restrict__ tstart, int P, float* gmlp) {
   constexpr int IN = F + 27;
+  constexpr int kMaxOut = H * ((IN > H ? IN : H) + 1);
+  constexpr int kPerThread = (kMaxOut + 255) / 256;
   const int tile = blockIdx.z, l = blockIdx.y;
   const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
   const int a_off = 64 * l;  // input of Linear l: x (l = 0) or h_l
@@ -424,9 +427,10 @@ __global__ void __launch_bounds__(256) tr_dw_kernel(const float* __restrict__ ac
   float* G = gmlp + (size_t)tile * P + poff;
   __shared__ float sh_a[32][65], sh_d[32][65];
   const int nout = fo * (fi + 1);
-  float acc[16];
+  static_assert(kPerThread * 256 >= kMaxOut, "every output of the largest layer has a thread");
+  float acc[kPerThread];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) acc[k] = 0.f;
+  for (int k = 0; k < kPerThread; ++k) acc[k] = 0.f;
   const int64_t t0 = tstart[tile], t1 = tstart[tile + 1];
   for (int64_t s0 = t0 + (int64_t)blockIdx.x * kDwBlock; s0 < t1; s0 += (int64_t)gridDim.x * kDwBlock) {
     const int64_t s1 = min(s0 + kDwBlock, t1);
@@ -439,7 +443,7 @@ __global__ void __launch_bounds__(256) tr_dw_kernel(const float* __restrict__ ac
       }
       __syncthreads();
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
+      for (int k = 0; k < kPerThread; ++k) {
         const int idx = threadIdx.x + 256 * k;
         if (idx < nout) {
           const int o = idx / (fi + 1), i = idx % (fi + 1);
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(256) tr_dw_kernel(const float* __restrict__ ac
     }
   }
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
+  for (int k = 0; k < kPerThread; ++k) {
     const int idx = threadIdx.x + 256 * k;
     if (idx < nout && acc[k] != 0.f) {
       const int o = idx / (fi + 1), i = idx % (fi + 1);
@@ -515,6 +519,10 @@ struct TrainWS {
   size_t bytes = 0;
   int64_t last_n = -1;
   int last_form = -1;
+  // Generation of the forward whose records the workspace holds (0: none).
+  // Every forward takes a new one from the counter; a backward must name the
+  // generation its forward returned.
+  uint64_t last_gen = 0, gen_counter = 0;
 };
 
 snisr_status scene_views(snisr_scene* scene, SceneDev* S, Workspace* ws, int* device);
@@ -588,6 +596,10 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
   snisr_status s = scene_views(sc, &S, &ws, &device);
   if (s != SNISR_OK) return s;
   if ((s = scene_train_ws(sc, &T, &num_sms, &msr, &nvox)) != SNISR_OK) return s;
+  if (march) {  // a forward overwrites the records: the previous generation is gone from here on
+    T->last_gen = 0;
+    T->last_n = -1;
+  }
   if ((s = train_ws_reserve(T, n, msr, S.num_tiles, nvox)) != SNISR_OK) return s;
   if (!march) return SNISR_OK;
   tr_dens_cache_kernel<<<gridn(nvox, 256), 256, 0, st>>>(S.corners, vdens, nvox, T->dcache);
@@ -615,7 +627,8 @@ snisr_status train_common(snisr_scene* sc, const float* vdens, const float* orig
 
 extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat, const float* vdens, const float* mlp,
                                             const float* orig, const float* dirs, const int32_t* ray_tile, int64_t n,
-                                            int32_t form, float* rgb, void* stream) {
+                                            int32_t form, float* rgb, uint64_t* generation, void* stream) {
+  if (generation) *generation = 0;
   if (!sc) return set_error(SNISR_INVALID_ARG, "train_forward: scene is null");
   if (n < 0) return set_error(SNISR_INVALID_ARG, "train_forward: negative ray count");
   if (n == 0) return SNISR_OK;
@@ -644,13 +657,16 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   TR_TRY(cudaGetLastError(), "train_forward: composite");
   T->last_n = n;
   T->last_form = form;
+  T->last_gen = ++T->gen_counter;
+  if (generation) *generation = T->last_gen;
   return SNISR_OK;
 }
 
 extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat, const float* vdens, const float* mlp,
                                              const float* orig, const float* dirs, const int32_t* ray_tile, int64_t n,
-                                             int32_t form, const float* rgb, const float* grad_rgb, float* gvfeat,
-                                             float* gvdens, float* gmlp, void* stream) {
+                                             int32_t form, uint64_t generation, const float* rgb,
+                                             const float* grad_rgb, float* gvfeat, float* gvdens, float* gmlp,
+                                             void* stream) {
   (void)rgb;
   (void)vdens;
   (void)orig;
@@ -670,6 +686,11 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   Workspace ws;
   snisr_status s = train_common(sc, vdens, orig, dirs, ray_tile, n, S, T, num_sms, st, false, ws);
   if (s != SNISR_OK) return s;
+  if (generation == 0 || generation != T->last_gen)
+    return set_error(SNISR_INVALID_ARG,
+                     "train_backward: generation " + std::to_string(generation) +
+                         " is not the latest train_forward on this scene (latest: " + std::to_string(T->last_gen) +
+                         "); another forward ran in between and replaced its sample records");
   if (T->last_n != n) return set_error(SNISR_INVALID_ARG, "train_backward: must follow train_forward on the same rays");
   tr_composite_bwd<<<gridn(n, 128), 128, 0, st>>>(S, T->recs, T->c, T->cnt, T->off, n, T->cap, grad_rgb, T->dout,
                                                   gvdens);

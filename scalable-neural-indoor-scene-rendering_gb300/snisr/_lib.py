@@ -121,8 +121,8 @@ _SIGNATURES = {
     "snisr_trace_voxels": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P]),
     "snisr_render_rays": (C.c_int, [P, P, P, C.c_int64, C.c_int32, P, P, P, P]),
     "snisr_render_rays_noalloc": (C.c_int, [P, P, P, C.c_int64, P, P, P, P]),
-    "snisr_train_forward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, P]),
-    "snisr_train_backward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, P, P, P, P, P]),
+    "snisr_train_forward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, P, P, P]),
+    "snisr_train_backward": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, C.c_int32, C.c_uint64, P, P, P, P, P, P]),
     "snisr_op_compute_rays": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P]),
     "snisr_op_tracing_tiles": (C.c_int, [P, C.c_int64, P, P, P, P, P, C.c_float, C.c_int32, P, P]),
     "snisr_op_sample_sparse": (C.c_int, [P, P, C.c_int64, P, C.c_float, C.c_float, C.c_float, C.c_float,
@@ -159,6 +159,7 @@ _SIGNATURES = {
     "snisr_synth_camera": (C.c_int, [P, C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.POINTER(Camera)]),
     "snisr_diag_mma": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, P]),
     "snisr_diag_wait_timeout": (C.c_int, [C.c_int64, C.POINTER(C.c_int64), P]),
+    "snisr_diag_march_math": (C.c_int, [C.c_int32, P, C.c_int64, P, P]),
     "snisr_scene_set_profiling": (C.c_int, [P, C.c_int32]),
     "snisr_scene_stage_times": (C.c_int, [P, P, C.c_int32, P]),
     "snisr_scene_frame_stats": (C.c_int, [P, P, P]),

@@ -71,18 +71,22 @@ class Config:
 #    MLP 43 -> 32 -> 32 -> 3, 256x256, no proxy mesh.
 CFG1 = Config("cfg1_small", 0, (1, 1, 1), 2.0, 64, 16, _lib.F32, 32, 2, 3, 0.2, 0.6, False, 0.0,
               256, 256, 60.0, 8, False, 1001)
+# Box sides are drawn U(box_min, box_max); the ranges below give the stated
+# occupied fractions of the full-resolution scenes (voxels within one voxel of
+# a surface): cfg2 5.1 %, cfg3 4.0 %, cfg4 5.0 %, cfg5 4.2 %.
+#
 # 2: full frame, 4x4x1 tiles of 128^3 over 3 m, FP16 32-dim features, per-tile
 #    FP16 MLP 59 -> 64x3 -> 3, ~200k-triangle proxy mesh, 1280x720.
-CFG2 = Config("cfg2_frame", 1, (4, 4, 1), 3.0, 128, 32, _lib.F16, 64, 3, 40, 0.3, 1.2, True, 0.075,
+CFG2 = Config("cfg2_frame", 1, (4, 4, 1), 3.0, 128, 32, _lib.F16, 64, 3, 40, 0.5, 1.65, True, 0.085,
               1280, 720, 60.0, 8, True, 1002)
 # 3: training, one 256^3 tile over 4 m, FP32 32-dim master features.
-CFG3 = Config("cfg3_train", 1, (1, 1, 1), 4.0, 256, 32, _lib.F32, 64, 3, 12, 0.3, 1.0, False, 0.0,
+CFG3 = Config("cfg3_train", 1, (1, 1, 1), 4.0, 256, 32, _lib.F32, 64, 3, 12, 0.4, 1.4, False, 0.0,
               640, 480, 60.0, 8, False, 1003)
 # 4: batched multi-tile training, 32 tiles of 128^3.
-CFG4 = Config("cfg4_batched", 1, (4, 4, 2), 3.0, 128, 32, _lib.F32, 64, 3, 60, 0.3, 1.2, False, 0.0,
+CFG4 = Config("cfg4_batched", 1, (4, 4, 2), 3.0, 128, 32, _lib.F32, 64, 3, 120, 0.5, 1.6, False, 0.0,
               640, 480, 60.0, 8, False, 1004)
 # 5: large scene, 8x8x2 tiles of 128^3 over 24x24x6 m, multi-room, ~1M-tri mesh.
-CFG5 = Config("cfg5_large", 2, (8, 8, 2), 3.0, 128, 32, _lib.F16, 64, 3, 300, 0.3, 1.2, True, 0.085,
+CFG5 = Config("cfg5_large", 2, (8, 8, 2), 3.0, 128, 32, _lib.F16, 64, 3, 300, 0.4, 1.5, True, 0.093,
               1920, 1080, 75.0, 16, True, 1005)
 
 ALL = {c.name: c for c in (CFG1, CFG2, CFG3, CFG4, CFG5)}

@@ -8,6 +8,8 @@ on trilinear per-corner features and the backward is libsnisr's adjoint.
 """
 from __future__ import annotations
 
+import ctypes
+
 from . import _lib
 
 
@@ -29,8 +31,11 @@ class TileFieldFunction:
 
     vfeat [NV, F], vdens [NV], mlp [NT, P] (FP32, requires_grad as needed);
     origins/dirs [n, 3] (normalised dirs); ray_tile [n] int32, grouped by tile.
-    The backward must run before the next forward on the same scene (the
-    forward's sample records live in the scene's training workspace)."""
+    The forward's sample records live in the scene's training workspace until
+    the next forward on the same scene replaces them; each forward's id
+    (generation) is kept in the autograd context, and a backward whose
+    forward was replaced raises SnisrError instead of back-propagating
+    through another forward's samples."""
 
     _fn = None
 
@@ -52,12 +57,14 @@ def _make_function():
                 _check(t, nm)
             n = origins.shape[0]
             rgb = torch.empty(n, 3, device=origins.device)
+            gen = ctypes.c_uint64(0)
             _lib.check(_lib.lib().snisr_train_forward(scene.handle, vfeat.data_ptr(), vdens.data_ptr(), mlp.data_ptr(),
                                                       origins.data_ptr(), dirs.data_ptr(), ray_tile.data_ptr(), n,
-                                                      int(form), rgb.data_ptr(), _stream()))
+                                                      int(form), rgb.data_ptr(), ctypes.byref(gen), _stream()))
             ctx.save_for_backward(vfeat, vdens, mlp, origins, dirs, ray_tile)
             ctx.scene = scene
             ctx.form = int(form)
+            ctx.generation = gen.value
             return rgb
 
         @staticmethod
@@ -70,7 +77,8 @@ def _make_function():
             n = origins.shape[0]
             _lib.check(_lib.lib().snisr_train_backward(ctx.scene.handle, vfeat.data_ptr(), vdens.data_ptr(),
                                                        mlp.data_ptr(), origins.data_ptr(), dirs.data_ptr(),
-                                                       ray_tile.data_ptr(), n, ctx.form, 0, g.data_ptr(),
+                                                       ray_tile.data_ptr(), n, ctx.form, ctx.generation, 0,
+                                                       g.data_ptr(),
                                                        gF.data_ptr(), gG.data_ptr(), gW.data_ptr(), _stream()))
             return gF, gG, gW, None, None, None, None, None
 

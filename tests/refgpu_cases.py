@@ -15,7 +15,9 @@ OUTSIDE_ORIGIN = np.array([-2.0, 5.5, 1.4], np.float32)
 
 @functools.lru_cache(maxsize=None)
 def _scene16():
-    return snisr.SynthScene(snisr.CFG2.replace(res=64, with_mesh=False))
+    # the scene the golden vectors were written on: 16 tiles of 64^3, 40 boxes
+    # with sides U(0.3, 1.2) m (fixed here, independent of the benchmark config)
+    return snisr.SynthScene(snisr.CFG2.replace(res=64, with_mesh=False, box_min=0.3, box_max=1.2))
 
 
 @functools.lru_cache(maxsize=None)

@@ -211,3 +211,19 @@ def test_render_tc_frames_without_or_with_few_samples(cuda, case):
     if case == "all_miss":
         assert (opac.cpu().numpy() == 0).all() and (rgb.cpu().numpy() == 0).all()
     sc.close()
+
+
+def test_march_math_bits_match_the_oracle(cuda):
+    """The kernels' e^x, log1p and softplus give the host restatement's bits,
+    so transmittance and the early-stop decision agree exactly."""
+    import torch
+    from test_oracle import _march_math_inputs
+    L = snisr.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    for fn, v in zip((oracle.MATH_EXP, oracle.MATH_LOG1P, oracle.MATH_SOFTPLUS), _march_math_inputs()):
+        xd = torch.from_numpy(v).cuda()
+        out = torch.empty_like(xd)
+        snisr._lib.check(L.snisr_diag_march_math(fn, xd.data_ptr(), v.size, out.data_ptr(), stream))
+        got = out.cpu().numpy()
+        ref = oracle.march_math(fn, v)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), fn

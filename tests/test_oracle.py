@@ -332,3 +332,48 @@ def test_compute_rays_states_the_fused_operation():
         unfused = np.stack([(((rot[a, 0] * x).astype(np.float32) + (rot[a, 1] * y).astype(np.float32))
                              .astype(np.float32) + rot[a, 2]).astype(np.float32) for a in range(3)], -1)
         assert not np.array_equal(got, unfused)  # the test can tell the two forms apart
+
+
+def _march_math_inputs():
+    x = -np.linspace(0, 80, 2000001).astype(np.float32)
+    y = np.concatenate([np.linspace(0, 1, 2000001).astype(np.float32),
+                        (10.0 ** np.linspace(-40, 0, 100000)).astype(np.float32)])
+    z = np.linspace(-30, 30, 1000001).astype(np.float32)
+    return x, y, z
+
+
+def test_march_math_accuracy():
+    """The render march's own e^x, log1p and softplus (single precision, the
+    same operations on the host and the device) against float64: e^x below
+    1 ulp on [-80, 0], log1p below 3 ulp on [0, 1], softplus relative error
+    below 5e-7 on [-30, 30]."""
+    x, y, z = _march_math_inputs()
+    e = oracle.march_math(oracle.MATH_EXP, x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    assert (np.abs(e - ref) / np.spacing(ref.astype(np.float32)).astype(np.float64)).max() < 1.0
+    l1 = oracle.march_math(oracle.MATH_LOG1P, y).astype(np.float64)
+    ref = np.log1p(y.astype(np.float64))
+    ulp = np.spacing(np.maximum(ref, 1e-45).astype(np.float32)).astype(np.float64)
+    assert (np.abs(l1 - ref) / ulp).max() < 3.0
+    sp = oracle.march_math(oracle.MATH_SOFTPLUS, z).astype(np.float64)
+    ref = np.logaddexp(0.0, z.astype(np.float64))
+    assert (np.abs(sp - ref) / ref).max() < 5e-7
+    assert oracle.march_math(oracle.MATH_EXP, np.array([-100.0, 0.0, np.nan], np.float32))[:2].tolist() == [0.0, 1.0]
+
+
+def test_host_bvh_proxy_equals_brute_force():
+    """The oracle's hierarchy (used to time the host path) returns the brute-
+    force nearest hit: same t and triangle id, on rays of two poses of the
+    1280x720 scene's ~205k-triangle proxy mesh."""
+    s = snisr.SynthScene(snisr.CFG2.replace(res=32))
+    osc = oracle.OracleScene(s.desc)
+    rng = np.random.default_rng(4)
+    for pose in (0, 5):
+        cam = s.camera(pose, 320, 180)
+        d = oracle.camera_dirs(cam)
+        d = np.ascontiguousarray(d[np.sort(rng.choice(d.shape[0], 1500, replace=False))])
+        o = oracle.camera_origins(cam, d.shape[0])
+        ts, th, tri = osc.proxy(o, d)
+        ts2, th2, tri2 = osc.proxy_bvh(o, d)
+        assert np.array_equal(tri, tri2) and np.array_equal(th, th2) and np.array_equal(ts, ts2)
+        assert (tri >= 0).mean() > 0.95

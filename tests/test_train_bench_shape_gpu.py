@@ -1,0 +1,248 @@
+"""Tensor-core training at the benchmarked shape: 32-dim features and the
+59 -> 64 -> 64 -> 64 -> 3 MLP of the single-tile training step (256^3 tile
+over 4 m, reduced here to 64^3 so the FP64 oracle finishes in seconds) and of
+the 32-tile batched step (128^3 tiles, reduced to 64^3).  This is the
+tr_mlp_fwd_tc / tr_mlp_bwd_tc instantiation whose speed the training
+benchmark reports.
+
+Checked against, per parameter group (features, density logits, MLP):
+* the exact FP64 oracle adjoint: relative error <= 1e-2 for the tensor-core
+  form (split BF16 forward operands, BF16 backward operands), <= 1e-3 for the
+  plain FP32 form; forward colour RMSE <= 1e-3 (TC), max-abs <= 1e-5 (plain);
+* the oracle's emulation of the tensor-core operand rounding: colours
+  max-abs <= 1e-4, gradients relative <= 2e-3 (the kernels are exact up to
+  FP32 summation order);
+* autograd of the reference-style graph (grid_sample lookup, Linear/ReLU MLP,
+  cumprod compositing; tests/reference_graph.py), float64 on the CPU;
+* FP64 central differences (h = 1e-4) on 64 parameters with non-negligible
+  gradient, for both forms.
+
+Relative error = ||g - g_ref|| / ||g_ref||.  Two density settings: the
+scene's own logits ~N(2, 1) (opaque surfaces: the first samples of a segment
+carry nearly all the weight) and logits shifted by -3 (a thin medium: every
+sample of the segment until it leaves the tile carries weight, so all of
+their MLP evaluations and ReLU masks enter the gradients).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import snisr
+from snisr import batch
+from snisr.train import tile_field
+
+pytestmark = pytest.mark.gpu
+
+RAYS = 16384  # from two 640x480 views
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def tile(cuda):
+    import torch
+    cfg = snisr.CFG3.replace(res=64)
+    s = snisr.SynthScene(cfg)
+    d_ = s.desc
+    assert (d_.feat_dim, d_.mlp_hidden, d_.mlp_layers) == (32, 64, 3)
+    sc = snisr.Scene(s.desc)
+    a = s.arrays()
+    rng = np.random.default_rng(33)
+    W = a["mlp_params"].copy()
+    W += rng.normal(0, 0.05, W.shape).astype(np.float32)  # non-zero biases, off the Xavier init
+    ds, os_ = [], []
+    for pose in (0, 5):
+        cam = s.camera(pose)
+        d = oracle.camera_dirs(cam)
+        idx = np.sort(rng.choice(d.shape[0], RAYS // 2, replace=False))
+        ds.append(np.ascontiguousarray(d[idx]))
+        os_.append(oracle.camera_origins(cam, RAYS // 2))
+    d = np.ascontiguousarray(np.concatenate(ds))
+    o = np.ascontiguousarray(np.concatenate(os_))
+    rt = np.zeros(RAYS, np.int32)
+    g = rng.standard_normal((RAYS, 3))
+    T = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    yield dict(s=s, sc=sc, osc=oracle.OracleScene(s.desc), vf=a["vertex_feat"].astype(np.float32).copy(),
+               vd=a["vertex_density"].astype(np.float32).copy(), W=W, o=o, d=d, rt=rt, g=g, T=T, cache={})
+    sc.close()
+
+
+def _density(P, kind):
+    return P["vd"] if kind == "synthetic" else (P["vd"] - 3.0).astype(np.float32)
+
+
+def _gpu(P, vd, form):
+    import torch
+    T = P["T"]
+    vf_t, vd_t, W_t = (T(x).requires_grad_(True) for x in (P["vf"], vd, P["W"]))
+    rgb = tile_field(vf_t, vd_t, W_t, P["sc"], T(P["o"]), T(P["d"]), T(P["rt"]), form)
+    (rgb * torch.from_numpy(P["g"]).float().cuda()).sum().backward()
+    P["sc"].check()
+    return rgb.detach().cpu().numpy(), vf_t.grad.cpu().numpy(), vd_t.grad.cpu().numpy(), W_t.grad.cpu().numpy()
+
+
+def _oracle(P, dens, vd, emulate):
+    key = (dens, emulate)
+    if key not in P["cache"]:
+        rgb, cnt = P["osc"].train_forward(P["vf"], vd, P["W"], P["o"], P["d"], P["rt"], emulate=emulate)
+        grads = P["osc"].train_backward(P["vf"], vd, P["W"], P["o"], P["d"], P["rt"], P["g"], emulate=emulate)
+        P["cache"][key] = (rgb, cnt) + tuple(grads)
+    return P["cache"][key]
+
+
+@pytest.mark.parametrize("dens", ["synthetic", "thin"])
+@pytest.mark.parametrize("form", [snisr.FORM_PLAIN_FP32, snisr.FORM_TC])
+def test_bench_shape_against_fp64_oracle(tile, form, dens):
+    P = tile
+    vd = _density(P, dens)
+    rgb, gF, gG, gW = _gpu(P, vd, form)
+    ref = _oracle(P, dens, vd, None)
+    cnt = ref[1]
+    assert cnt.sum() > 40000  # hundreds of 128-sample chunks
+    errs = (_rel(gF, ref[2]), _rel(gG, ref[3]), _rel(gW, ref[4]))
+    rmse = float(np.sqrt(((rgb - ref[0]) ** 2).mean()))
+    print(f"form {form} density {dens}: samples {int(cnt.sum())}, colour RMSE {rmse:.2e}, max-abs "
+          f"{np.abs(rgb - ref[0]).max():.2e}; gradient relative errors vs FP64 (features, density, mlp) = "
+          f"({errs[0]:.2e}, {errs[1]:.2e}, {errs[2]:.2e})")
+    if form == snisr.FORM_PLAIN_FP32:
+        assert np.abs(rgb - ref[0]).max() <= 1e-5
+        assert max(errs) <= 1e-3
+    else:
+        assert rmse <= 1e-3
+        assert max(errs) <= 1e-2
+        emu = _oracle(P, dens, vd, "tc")
+        eerr = (_rel(gF, emu[2]), _rel(gG, emu[3]), _rel(gW, emu[4]))
+        print(f"   against the tensor-core emulation: colour max-abs {np.abs(rgb - emu[0]).max():.2e}, gradients "
+              f"({eerr[0]:.2e}, {eerr[1]:.2e}, {eerr[2]:.2e})")
+        assert np.abs(rgb - emu[0]).max() <= 1e-4
+        assert max(eerr) <= 2e-3
+    P["cache"][(form, dens)] = (gF, gG, gW)
+
+
+@pytest.mark.parametrize("form,tol", [(snisr.FORM_PLAIN_FP32, 1e-3), (snisr.FORM_TC, 1e-2)])
+def test_bench_shape_against_reference_graph(tile, form, tol):
+    """Autograd of the reference-style graph (float64, CPU) on a 4096-ray
+    subset: the gradients the reference's own training would compute."""
+    import torch
+    import reference_graph as rg
+    P = tile
+    sub = slice(0, 4096)
+    o, d, rt = (np.ascontiguousarray(P[k][sub]) for k in ("o", "d", "rt"))
+    g = P["g"][sub]
+    samples = P["osc"].train_samples(P["vf"], P["vd"], P["W"], o, d, rt)
+    grid = rg.corner_index_grid(P["s"].desc, P["s"].arrays(), 0)
+    tv = [torch.tensor(x.astype(np.float64).reshape(-1) if x is P["W"] else x.astype(np.float64), requires_grad=True)
+          for x in (P["vf"], P["vd"], P["W"])]
+    rgb_ref = rg.render(tv[0], tv[1], tv[2], P["s"].desc, grid, samples, d)
+    (rgb_ref * torch.from_numpy(g)).sum().backward()
+    T = P["T"]
+    vf_t, vd_t, W_t = (T(x).requires_grad_(True) for x in (P["vf"], P["vd"], P["W"]))
+    rgb = tile_field(vf_t, vd_t, W_t, P["sc"], T(o), T(d), T(rt), form)
+    (rgb * torch.from_numpy(g).float().cuda()).sum().backward()
+    P["sc"].check()
+    errs = (_rel(vf_t.grad.cpu().numpy(), tv[0].grad.numpy()), _rel(vd_t.grad.cpu().numpy(), tv[1].grad.numpy()),
+            _rel(W_t.grad.cpu().numpy(), tv[2].grad.numpy().reshape(P["W"].shape)))
+    print(f"form {form}: gradient relative errors vs the reference-style autograd graph = "
+          f"({errs[0]:.2e}, {errs[1]:.2e}, {errs[2]:.2e})")
+    assert max(errs) <= tol
+
+
+@pytest.mark.parametrize("form", [snisr.FORM_PLAIN_FP32, snisr.FORM_TC])
+def test_bench_shape_against_finite_differences(tile, form):
+    """FP64 central differences (h = 1e-4) of the oracle's FP64 forward on a
+    4096-ray subset, at 64 parameters (22 features, 20 density logits, 22 MLP
+    weights) whose gradient is at least 1e-3 of the group's largest."""
+    import torch
+    P = tile
+    sub = slice(0, 4096)
+    o, d, rt = (np.ascontiguousarray(P[k][sub]) for k in ("o", "d", "rt"))
+    g = P["g"][sub]
+    T = P["T"]
+    leaves = [T(x).requires_grad_(True) for x in (P["vf"], P["vd"], P["W"])]
+    rgb = tile_field(*leaves, P["sc"], T(o), T(d), T(rt), form)
+    (rgb * torch.from_numpy(g).float().cuda()).sum().backward()
+    grads = {k: x.grad.cpu().numpy() for k, x in zip(("vf", "vd", "W"), leaves)}
+    osc = P["osc"]
+
+    def loss(vf, vd, W):
+        r, _ = osc.train_forward(vf, vd, W, o, d, rt)
+        return float((r * g).sum())
+
+    rng = np.random.default_rng(17)
+    picks = []
+    for name, grad in grads.items():
+        flat = np.abs(grad.reshape(-1))
+        cand = np.nonzero(flat > 1e-3 * flat.max())[0]
+        for i in rng.choice(cand, 20 if name == "vd" else 22, replace=False):
+            picks.append((name, int(i)))
+    errs = []
+    h = 1e-4
+    for name, i in picks:
+        args = {"vf": P["vf"], "vd": P["vd"], "W": P["W"]}
+        p = args[name].copy()
+        flat = p.reshape(-1)
+        orig = float(flat[i])
+        flat[i] = np.float32(orig + h)
+        lp = loss(**{**args, name: p})
+        flat[i] = np.float32(orig - h)
+        lm = loss(**{**args, name: p})
+        fd = (lp - lm) / (float(np.float32(orig + h)) - float(np.float32(orig - h)))
+        errs.append(abs(grads[name].reshape(-1)[i] - fd) / max(abs(fd), 1e-6))
+    errs = np.array(errs)
+    print(f"form {form}: per-parameter relative error vs FP64 central differences: median {np.median(errs):.2e}, "
+          f"90th percentile {np.quantile(errs, 0.9):.2e}")
+    # a few parameters sit on ReLU kinks or the early-stop cut at this step
+    if form == snisr.FORM_PLAIN_FP32:
+        assert np.median(errs) <= 1e-3
+        assert (errs <= 1e-2).mean() >= 0.9
+    else:
+        assert np.median(errs) <= 1e-2
+        assert (errs <= 5e-2).mean() >= 0.9
+
+
+@pytest.fixture(scope="module")
+def batched(cuda):
+    import torch
+    cfg = snisr.CFG4.replace(res=64)
+    s = snisr.SynthScene(cfg)
+    sc = snisr.Scene(s.desc)
+    o, d, t, counts = batch.tile_batch(s, views=4, lo=256, hi=4096, seed=7)
+    a = s.arrays()
+    rng = np.random.default_rng(2)
+    W = a["mlp_params"].copy()
+    W += rng.normal(0, 0.05, W.shape).astype(np.float32)
+    g = rng.standard_normal((o.shape[0], 3))
+    yield dict(s=s, sc=sc, o=o, d=d, t=t, counts=counts, vf=a["vertex_feat"].astype(np.float32).copy(),
+               vd=a["vertex_density"].astype(np.float32).copy(), W=W, g=g)
+    sc.close()
+
+
+def test_batched_tensor_core_step_against_fp64_oracle(batched):
+    """The 32-tile batched step (one forward/backward over all tiles' segments,
+    per-tile MLPs 59 -> 64x3 -> 3) in the tensor-core form against the FP64
+    oracle adjoint and its tensor-core emulation."""
+    import torch
+    P = batched
+    assert P["s"].desc.num_tiles == 32 and (P["counts"] > 0).sum() >= 10
+    T = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    leaves = [T(x).requires_grad_(True) for x in (P["vf"], P["vd"], P["W"])]
+    rgb = tile_field(*leaves, P["sc"], P["o"], P["d"], P["t"], snisr.FORM_TC)
+    (rgb * torch.from_numpy(P["g"]).float().cuda()).sum().backward()
+    P["sc"].check()
+    osc = oracle.OracleScene(P["s"].desc)
+    o, d, t = (x.cpu().numpy() for x in (P["o"], P["d"], P["t"]))
+    ref, cnt = osc.train_forward(P["vf"], P["vd"], P["W"], o, d, t)
+    gref = osc.train_backward(P["vf"], P["vd"], P["W"], o, d, t, P["g"])
+    emu = osc.train_backward(P["vf"], P["vd"], P["W"], o, d, t, P["g"], emulate="tc")
+    got = [x.grad.cpu().numpy() for x in leaves]
+    errs = [_rel(a, b) for a, b in zip(got, gref)]
+    eerr = [_rel(a, b) for a, b in zip(got, emu)]
+    rmse = float(np.sqrt(((rgb.detach().cpu().numpy() - ref) ** 2).mean()))
+    print(f"batched TC: {o.shape[0]} segments, {int(cnt.sum())} samples, colour RMSE {rmse:.2e}; gradient relative "
+          f"errors vs FP64 {['%.2e' % e for e in errs]}, vs the TC emulation {['%.2e' % e for e in eerr]}")
+    assert cnt.sum() > 20000
+    assert rmse <= 1e-3
+    assert max(errs) <= 1e-2
+    assert max(eerr) <= 2e-3

@@ -153,3 +153,27 @@ def test_train_long_segments_match_oracle(setup, form):
     assert _rel(vf.grad.cpu().numpy(), gF) <= tol
     assert _rel(vd.grad.cpu().numpy(), gG) <= tol
     assert _rel(W.grad.cpu().numpy(), gW) <= tol
+
+
+def test_backward_of_a_replaced_forward_is_rejected(setup):
+    """Two forwards of equal batch size on one scene, then the first one's
+    backward: the records of the first were replaced by the second, so the
+    backward must fail with a clear error; the second's backward still gives
+    the oracle's gradients."""
+    import torch
+    S = setup
+    T = S["T"]
+    form = snisr.FORM_PLAIN_FP32
+    vf, vd, W = (T(S[k]).requires_grad_(True) for k in ("vf", "vd", "W"))
+    g = np.random.default_rng(5).standard_normal((S["d"].shape[0], 3))
+    gt = torch.from_numpy(g).float().cuda()
+    first = tile_field(vf, vd, W, S["sc"], T(S["o"]), T(S["d"]), T(S["rt"]), form)
+    vf2, vd2, W2 = (T(S[k]).requires_grad_(True) for k in ("vf", "vd", "W"))
+    second = tile_field(vf2, vd2, W2, S["sc"], T(S["o"]), T(S["d"]), T(S["rt"]), form)
+    with pytest.raises(snisr.SnisrError, match="generation"):
+        (first * gt).sum().backward()
+    (second * gt).sum().backward()
+    gF, gG, gW = S["osc"].train_backward(S["vf"], S["vd"], S["W"], S["o"], S["d"], S["rt"], g)
+    assert _rel(vf2.grad.cpu().numpy(), gF) <= 1e-3
+    assert _rel(vd2.grad.cpu().numpy(), gG) <= 1e-3
+    assert _rel(W2.grad.cpu().numpy(), gW) <= 1e-3
