@@ -34,11 +34,52 @@ CUBINS = {
     "reorder": "rendering/src/reorder.cu",
     "Sample_kernel": "training/src/Sample_kernel.cu",
     "Helper_kernel": "training/src/Helper_kernel.cu",
+    "cuda_func": "training/src/cuda_func.cu",
 }
 # rayreflection_render.cu:5-6 include two ATen quantized CPU headers that it
 # does not use and that this torch no longer ships; empty stand-ins are found
 # first on the include path.
 _STUBS = ("ATen/native/quantized/cpu/embedding_packed_params.h", "ATen/native/quantized/cpu/fbgemm_utils.h")
+# training/src/cuda_func.cu's host code (image and .npy file loading, a
+# progress bar) uses OpenCV, cnpy and tqdm, which are not installed.  Only its
+# device code goes into the cubin, but nvcc still parses the host code, so
+# these stand-ins declare the few names it uses (nothing is defined: no host
+# code is compiled or linked).
+_DECL_STUBS = {
+    "opencv2/opencv.hpp": """#pragma once
+#include <string>
+#define CV_8UC3 16
+#define CV_32FC3 21
+namespace cv {
+enum { COLOR_BGR2RGB = 4, COLOR_RGB2BGR = 4 };
+struct Mat {
+  unsigned char* data;
+  bool isContinuous() const;
+  void convertTo(Mat& dst, int type, double alpha = 1.0, double beta = 0.0) const;
+  static Mat zeros(int rows, int cols, int type);
+};
+Mat imread(const std::string& path, int flags = 1);
+bool imwrite(const std::string& path, const Mat& img);
+void cvtColor(const Mat& src, Mat& dst, int code);
+}  // namespace cv
+""",
+    "cnpy.h": """#pragma once
+#include <string>
+namespace cnpy {
+struct NpyArray {
+  template <class T> T* data();
+};
+NpyArray npy_load(std::string path);
+}  // namespace cnpy
+""",
+    "tqdm.h": """#pragma once
+class tqdm {
+ public:
+  void progress(int i, int n);
+  void finish();
+};
+""",
+}
 
 
 def cubin_path(name: str) -> str:
@@ -68,6 +109,12 @@ def build_cubins(force: bool = False):
         os.makedirs(os.path.dirname(p), exist_ok=True)
         if not os.path.exists(p):
             open(p, "w").close()
+    for h, text in _DECL_STUBS.items():
+        p = os.path.join(stub, h)
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        if not os.path.exists(p) or open(p).read() != text:
+            with open(p, "w") as f:
+                f.write(text)
     jobs = []
     for name, rel in CUBINS.items():
         src = os.path.join(REF, rel)
