@@ -1917,7 +1917,8 @@ void oracle_train_rays(const float* K, const float* C, int H, int W, float* ro, 
     const int y = (int)(i / W), x = (int)(i % W);
     const float u = ((float)x - K[2]) / K[0], v = ((float)y - K[5]) / K[4];
     for (int a = 0; a < 3; ++a) {
-      rd[3 * i + a] = (C[4 * a] * u + C[4 * a + 1] * v) + C[4 * a + 2];
+      // the reference build fuses the left product: fma(C0, u, C1 * v) + C2
+      rd[3 * i + a] = fmac(C[4 * a], u, C[4 * a + 1] * v) + C[4 * a + 2];
       ro[3 * i + a] = C[4 * a + 3];
     }
   }
@@ -2057,18 +2058,34 @@ void oracle_train_bgdepth(int train_tile, const int32_t* visited, const float* h
   }
 }
 
+// Multi-view diffuse estimate of gen_diffuse_in_tile_kernel
+// (training/src/cuda_func.cu:1197-1339) with the fused multiply-adds of the
+// reference's build: in `a*b + c*d + e*f + g` the first add fuses its left
+// product and each further product is fused into the running sum
+// (fma(e, f, fma(a, b, c*d)) + g); `p + t*d` is fma(t, d, p).  normalize()
+// multiplies by 1/sqrt of the squared length: correctly rounded here, CUDA's
+// rsqrtf in the reference and in the library's kernel.  The two agree except
+// where rsqrtf is off by an ulp; that decides only the training view's own
+// weight (1 - cos)^2, a rounding residue that rsqrtf leaves non-zero for most
+// pixels (the pixel then takes its own colour when no other view sees its
+// hit) and that is often exactly 0 here (the pixel keeps 0).
 void oracle_gen_diffuse(const float* origins, int train_tile, const float* ro, const float* rd, const float* hits,
                         const int32_t* visited, const float* images, const float* depths, const float* ms, int K,
                         int nimg, int H, int W, float* diffuse, float* bgdepth, int threads) {
   const int64_t npix = (int64_t)H * W;
+  auto dot_f = [](const float* a, const float* b) { return fmac(a[2], b[2], fmac(a[0], b[0], a[1] * b[1])); };
   auto project = [&](const float* m, const float p[3], float& z, float& px, float& py) {
-    const float x = ((m[0] * p[0] + m[1] * p[1]) + m[2] * p[2]) + m[3];
-    const float y = ((m[4] * p[0] + m[5] * p[1]) + m[6] * p[2]) + m[7];
-    z = ((m[8] * p[0] + m[9] * p[1]) + m[10] * p[2]) + m[11];
+    const float x = fmac(m[2], p[2], fmac(m[0], p[0], m[1] * p[1])) + m[3];
+    const float y = fmac(m[6], p[2], fmac(m[4], p[0], m[5] * p[1])) + m[7];
+    z = fmac(m[10], p[2], fmac(m[8], p[0], m[9] * p[1])) + m[11];
     if (z <= 0.0f) return false;
     px = x / z;
     py = y / z;
     return !(px < 0.0f || px >= (float)(W - 1) || py < 0.0f || py >= (float)(H - 1));
+  };
+  auto normalize = [&](const float* v, float* out) {
+    const float inv = (float)(1.0 / std::sqrt((double)dot_f(v, v)));
+    for (int a = 0; a < 3; ++a) out[a] = v[a] * inv;
   };
   parallel_for(npix, threads, [&](int64_t i) {
     const float* h = hits + 2 * i * K;
@@ -2085,7 +2102,7 @@ void oracle_gen_diffuse(const float* origins, int train_tile, const float* ro, c
     if (first == -1.0f) return;
     if (bgdepth[i] != -1.0f) {
       float p[3];
-      for (int a = 0; a < 3; ++a) p[a] = o[a] + bgdepth[i] * d[a];
+      for (int a = 0; a < 3; ++a) p[a] = fmac(bgdepth[i], d[a], o[a]);
       bool visible = false;
       for (int j = 0; j < nimg && !visible; ++j) {
         float z, px, py;
@@ -2097,8 +2114,8 @@ void oracle_gen_diffuse(const float* origins, int train_tile, const float* ro, c
       if (!visible) bgdepth[i] = -1.0f;
     }
     float hp[3], dn[3];
-    for (int a = 0; a < 3; ++a) hp[a] = o[a] + first * d[a];
-    normalize3(d, dn);
+    for (int a = 0; a < 3; ++a) hp[a] = fmac(first, d[a], o[a]);
+    normalize(d, dn);
     float sum[3] = {0.0f, 0.0f, 0.0f}, weight = 0.0f;
     for (int j = 0; j < nimg; ++j) {
       float z, px, py;
@@ -2107,17 +2124,17 @@ void oracle_gen_diffuse(const float* origins, int train_tile, const float* ro, c
       if (std::fabs(z - dep) > 0.01f) continue;
       float v[3], vp[3];
       for (int a = 0; a < 3; ++a) v[a] = hp[a] - origins[3 * j + a];
-      normalize3(v, vp);
+      normalize(v, vp);
       const int x0 = (int)px, y0 = (int)py;
       const float fx = px - (float)x0, fy = py - (float)y0;
       const float w00 = (1.0f - fx) * (1.0f - fy), w11 = fx * fy, w01 = (1.0f - fx) * fy, w10 = fx * (1.0f - fy);
       const int64_t i00 = (int64_t)j * npix + (int64_t)y0 * W + x0, i10 = i00 + 1, i01 = i00 + W, i11 = i01 + 1;
-      float wc = 1.0f - ((dn[0] * vp[0] + dn[1] * vp[1]) + dn[2] * vp[2]);
+      float wc = 1.0f - dot_f(dn, vp);
       wc = wc * wc;
       for (int a = 0; a < 3; ++a) {
-        const float c = ((images[3 * i00 + a] * w00 + images[3 * i01 + a] * w01) + images[3 * i10 + a] * w10) +
-                        images[3 * i11 + a] * w11;
-        sum[a] = sum[a] + wc * c;
+        const float c = fmac(images[3 * i11 + a], w11,
+                             fmac(images[3 * i10 + a], w10, fmac(images[3 * i00 + a], w00, images[3 * i01 + a] * w01)));
+        sum[a] = fmac(wc, c, sum[a]);
       }
       weight = weight + wc;
     }

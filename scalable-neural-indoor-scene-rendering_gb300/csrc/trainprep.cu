@@ -63,7 +63,8 @@ __global__ void train_rays_kernel(const float* __restrict__ Km, const float* __r
     const float v = fdiv(fsub((float)y, cy), fy);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      rd[3 * i + a] = fadd(fadd(fmul(C[4 * a], u), fmul(C[4 * a + 1], v)), C[4 * a + 2]);
+      // C0 u + C1 v + C2 with the reference build's contraction: fma(C0, u, C1 v) + C2
+      rd[3 * i + a] = fadd(ffma(C[4 * a], u, fmul(C[4 * a + 1], v)), C[4 * a + 2]);
       ro[3 * i + a] = C[4 * a + 3];
     }
   }
@@ -225,11 +226,28 @@ __global__ void train_bgdepth_kernel(int train_tile, const int32_t* __restrict__
   }
 }
 
+// The diffuse estimate's arithmetic as the reference's compiled kernel does
+// it (gen_diffuse_in_tile_kernel, training/src/cuda_func.cu:1197-1339, built
+// by nvcc with its default contraction): every `a*b + c*d + ...` chain fuses
+// the left product of the first add and then each further product into a
+// multiply-add, and normalize() multiplies by CUDA's rsqrtf of the squared
+// length (training/src/include/cutil_math.h).  rsqrtf matters here: for the
+// training view itself the view-angle weight (1 - cos)^2 is a rounding
+// residue, non-zero for most pixels, so a hit seen by no other view takes its
+// own pixel colour.
+__device__ __forceinline__ float dot3_fused(const float a[3], const float b[3]) {
+  return ffma(a[2], b[2], ffma(a[0], b[0], fmul(a[1], b[1])));
+}
+__device__ __forceinline__ void normalize3_rsqrt(const float v[3], float out[3]) {
+  const float inv = rsqrtf(dot3_fused(v, v));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) out[a] = fmul(v[a], inv);
+}
 __device__ __forceinline__ bool project(const float* m, const float p[3], int H, int W, float& z, float& px,
                                         float& py) {
-  const float x = fadd(fadd(fadd(fmul(m[0], p[0]), fmul(m[1], p[1])), fmul(m[2], p[2])), m[3]);
-  const float y = fadd(fadd(fadd(fmul(m[4], p[0]), fmul(m[5], p[1])), fmul(m[6], p[2])), m[7]);
-  z = fadd(fadd(fadd(fmul(m[8], p[0]), fmul(m[9], p[1])), fmul(m[10], p[2])), m[11]);
+  const float x = fadd(ffma(m[2], p[2], ffma(m[0], p[0], fmul(m[1], p[1]))), m[3]);
+  const float y = fadd(ffma(m[6], p[2], ffma(m[4], p[0], fmul(m[5], p[1]))), m[7]);
+  z = fadd(ffma(m[10], p[2], ffma(m[8], p[0], fmul(m[9], p[1]))), m[11]);
   if (z <= 0.0f) return false;
   px = fdiv(x, z);
   py = fdiv(y, z);
@@ -259,7 +277,7 @@ __global__ void gen_diffuse_kernel(const float* __restrict__ origins, int train_
     if (bg != -1.0f) {
       float p[3];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) p[a] = fadd(o[a], fmul(bg, d[a]));
+      for (int a = 0; a < 3; ++a) p[a] = ffma(bg, d[a], o[a]);
       bool visible = false;
       for (int j = 0; j < nimg && !visible; ++j) {
         float z, px, py;
@@ -273,8 +291,8 @@ __global__ void gen_diffuse_kernel(const float* __restrict__ origins, int train_
     }
     float hp[3], dn[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) hp[a] = fadd(o[a], fmul(first, d[a]));
-    normalize3(d, dn);
+    for (int a = 0; a < 3; ++a) hp[a] = ffma(first, d[a], o[a]);
+    normalize3_rsqrt(d, dn);
     float sum[3] = {0.0f, 0.0f, 0.0f}, weight = 0.0f;
     for (int j = 0; j < nimg; ++j) {
       float z, px, py;
@@ -285,7 +303,7 @@ __global__ void gen_diffuse_kernel(const float* __restrict__ origins, int train_
       float v[3], vp[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) v[a] = fsub(hp[a], __ldg(origins + 3 * j + a));
-      normalize3(v, vp);
+      normalize3_rsqrt(v, vp);
       const int x0 = (int)px, y0 = (int)py;
       const float fx = fsub(px, (float)x0), fy = fsub(py, (float)y0);
       const float w00 = fmul(fsub(1.0f, fx), fsub(1.0f, fy));
@@ -294,14 +312,14 @@ __global__ void gen_diffuse_kernel(const float* __restrict__ origins, int train_
       const float w10 = fmul(fx, fsub(1.0f, fy));
       const int64_t i00 = (int64_t)j * npix + (int64_t)y0 * W + x0;
       const int64_t i10 = i00 + 1, i01 = i00 + W, i11 = i01 + 1;
-      float wc = fsub(1.0f, fadd(fadd(fmul(dn[0], vp[0]), fmul(dn[1], vp[1])), fmul(dn[2], vp[2])));
+      float wc = fsub(1.0f, dot3_fused(dn, vp));
       wc = fmul(wc, wc);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const float c = fadd(fadd(fadd(fmul(__ldg(images + 3 * i00 + a), w00), fmul(__ldg(images + 3 * i01 + a), w01)),
-                                  fmul(__ldg(images + 3 * i10 + a), w10)),
-                             fmul(__ldg(images + 3 * i11 + a), w11));
-        sum[a] = fadd(sum[a], fmul(wc, c));
+        const float c00 = __ldg(images + 3 * i00 + a), c01 = __ldg(images + 3 * i01 + a);
+        const float c10 = __ldg(images + 3 * i10 + a), c11 = __ldg(images + 3 * i11 + a);
+        const float c = ffma(c11, w11, ffma(c10, w10, ffma(c00, w00, fmul(c01, w01))));
+        sum[a] = ffma(wc, c, sum[a]);
       }
       weight = fadd(weight, wc);
     }

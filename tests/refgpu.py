@@ -305,3 +305,67 @@ def dilate_boundary(nodes_flag, num_voxel):
     module("Helper_kernel").launch("dilate_boundary_cuda_kernel", nb, 512,
                                    [ptr(nodes_flag), ptr(tmp), i32(num_voxel), i32(base), i32(add)])
     nodes_flag.copy_(tmp)
+
+
+# ---------------------------------------------------------------------------
+# training-data preparation (training/src/cuda_func.cu), launched as
+# get_trainData_v3 launches them (cuda_func.cu:1428-1439, 1500-1521): 512
+# threads, one job per pixel (or per pixel x visited-tile slot)
+# ---------------------------------------------------------------------------
+def int3(a):
+    return (C.c_int * 3)(*[int(v) for v in a])
+
+
+def computing_rays(H, W, K, C2W, rays_o, rays_d):
+    """cuda_func.cu:15-50; K [9], C2W [12] device arrays; rays [H*W, 3]."""
+    nb, base, add = _split_train(H * W)
+    module("cuda_func").launch("computing_rays_kernel", nb, 512,
+                               [i32(H), i32(W), ptr(K), ptr(C2W), ptr(rays_o), ptr(rays_d), i32(add), i32(base)])
+
+
+def tracing_tile(H, W, rays_o, rays_d, IndexMap, tile_shape, tile_size, K, visited, scene_min_corner):
+    """cuda_func.cu:52-128; visited [H*W, K]."""
+    nb, base, add = _split_train(H * W)
+    module("cuda_func").launch("tracingTile_kernel", nb, 512,
+                               [i32(H), i32(W), ptr(rays_o), ptr(rays_d), ptr(IndexMap), int3(tile_shape),
+                                f32(tile_size), i32(K), ptr(visited), float3(scene_min_corner), i32(add), i32(base)])
+
+
+def ray_double_hit_in_tile(H, W, rays_o, rays_d, vertices, faces, centers, BConFaceIdx, BConFaceNum, tile_size, K,
+                           num_block, visited, double_hits):
+    """cuda_func.cu:284-444; one job per (pixel, visited slot); double_hits [H*W, K, 2]."""
+    nb, base, add = _split_train(H * W * K)
+    module("cuda_func").launch("ray_doubleHit_inTile_kernel", nb, 512,
+                               [i32(H), i32(W), ptr(rays_o), ptr(rays_d), ptr(vertices), ptr(faces), ptr(centers),
+                                ptr(BConFaceIdx), ptr(BConFaceNum), f32(tile_size), i32(K), i32(num_block),
+                                ptr(visited), ptr(double_hits), i32(add), i32(base)])
+
+
+def get_train_data(train_tile, rays_o, rays_d, vertices, faces, visited, double_hits, K, bgdepth, valid):
+    """cuda_func.cu:587-663; bgdepth / valid [H*W] (the host zeroes valid per view)."""
+    nb, base, add = _split_train(valid.numel())
+    module("cuda_func").launch("get_trainData_kernel", nb, 512,
+                               [i32(train_tile), ptr(rays_o), ptr(rays_d), ptr(vertices), ptr(faces), ptr(visited),
+                                ptr(double_hits), i32(K), ptr(bgdepth), ptr(valid), i32(add), i32(base)])
+
+
+def gen_diffuse_in_tile(origins, train_tile, rays_o, rays_d, double_hits, visited, images, depths, ms, K, num_images,
+                        H, W, diffuses, bgdepth):
+    """cuda_func.cu:1197-1339; diffuses [H*W, 3]; bgdepth is read and updated."""
+    nb, base, add = _split_train(H * W)
+    module("cuda_func").launch("gen_diffuse_in_tile_kernel", nb, 512,
+                               [ptr(origins), i32(train_tile), ptr(rays_o), ptr(rays_d), ptr(double_hits),
+                                ptr(visited), ptr(images), ptr(depths), ptr(ms), i32(K), i32(num_images), i32(H),
+                                i32(W), ptr(diffuses), ptr(bgdepth), i32(add), i32(base)])
+
+
+def render_diffuse(train_tile, rays_o, rays_d, visited, sparse_to_group, K, tile_size, num_voxel, voxel_size,
+                   sample_step, centers, voxels, nodes, diffuses, depths, valid):
+    """cuda_func.cu:1687-1802 (the FP32 sparse-voxel renderer of the second
+    training iteration); note its (base_jobs, add_num) parameter order."""
+    n = valid.numel()
+    nb, base, add = _split_train(n)
+    module("cuda_func").launch("render_diffuse_kernel", nb, 512,
+                               [i32(train_tile), ptr(rays_o), ptr(rays_d), ptr(visited), ptr(sparse_to_group), i32(K),
+                                f32(tile_size), i32(num_voxel), f32(voxel_size), f32(sample_step), ptr(centers),
+                                ptr(voxels), ptr(nodes), ptr(diffuses), ptr(depths), ptr(valid), i32(base), i32(add)])
