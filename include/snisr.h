@@ -529,7 +529,8 @@ snisr_status snisr_scene_frame_footprint(snisr_scene* scene, int64_t* out, void*
  * D [128][N] FP32 = A * B^T.  mode 1/2 (N = 64): At [128][64], Bt [128][64]
  * stored sample-major and consumed as MN-major operands, D [128][64] with
  * D[m][n] = sum_k At[k][m] Bt[k][n] for m < 64 (two stride conventions).
- * Synchronises `stream`. */
+ * mode 3: as mode 0 with A read from tensor memory (each row stored into
+ * its lane by tcgen05.st).  Synchronises `stream`. */
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev,
                             int32_t N, int32_t bf16, int32_t mode, void* stream);
 

@@ -932,8 +932,8 @@ snisr_status snisr_diag_wait_timeout(int64_t limit_ns, int64_t* waited_ns, void*
 
 snisr_status snisr_diag_mma(const uint16_t* A_dev, const uint16_t* B_dev, float* D_dev, int32_t N, int32_t bf16,
                             int32_t mode, void* stream) {
-  if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1) || mode < 0 || mode > 2 ||
-      (mode != 0 && N != 64))
+  if (!A_dev || !B_dev || !D_dev || (N != 32 && N != 64) || (bf16 != 0 && bf16 != 1) || mode < 0 || mode > 3 ||
+      ((mode == 1 || mode == 2) && N != 64))
     return set_error(SNISR_INVALID_ARG, "diag_mma: bad argument");
   cudaError_t e = launch_diag_mma(A_dev, B_dev, D_dev, N, bf16, mode, (cudaStream_t)stream);
   if (e == cudaErrorLaunchTimeout) return set_error(SNISR_DEVICE_TIMEOUT, "diag_mma: MMA completion wait ran out");

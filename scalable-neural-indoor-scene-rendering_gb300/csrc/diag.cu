@@ -2,6 +2,9 @@
 //
 // mode 0: A [128][64], B [N][64] K-major (the MLP's forward layout),
 //         D = A B^T (K = 64).
+// mode 3: as mode 0 with A taken from tensor memory: every thread stores its
+//         row of A into columns [64, 96) of the CTA's allocation
+//         (tcgen05.st 32x32b), the MMA reads it as the TMEM A operand.
 // mode 1/2: At [128][64], Bt [128][64] stored sample-major (row = K index,
 //         the layout the epilogues write), consumed as MN-major operands,
 //         D[m][n] = sum_k At[k][m] Bt[k][n] for m < 64 (K = 128), the second
@@ -46,7 +49,7 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   // zero [Zs, base + 64 KB): the zero tile, the B tile and its slack
   for (int k = tid; k < (65536 - 16384) / 16; k += 128) reinterpret_cast<uint4*>(Zs)[k] = make_uint4(0, 0, 0, 0);
   __syncthreads();
-  const int brows = mode == 0 ? N : 128;
+  const int brows = (mode == 0 || mode == 3) ? N : 128;
   for (int c = 0; c < 8; ++c) {
     *reinterpret_cast<uint4*>(As + tc::sw128_offset(tid, c)) = *reinterpret_cast<const uint4*>(A + tid * 64 + 8 * c);
     if (tid < brows)
@@ -57,7 +60,7 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(slot), 64);
+    tc::tmem_alloc(tc::smem_addr(slot), 128);
     tc::tmem_relinquish();
   }
   tc::fence_proxy_async();
@@ -65,8 +68,26 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *slot;
+  if (mode == 3) {
+    // row tid of A (64 16-bit values = 32 columns) into lane tid, columns 64..95
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(A + tid * 64);
+    uint32_t v[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = row[c];
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    tc::tmem_st16(lane_base + 64, v);
+    tc::tmem_st16(lane_base + 80, v + 16);
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  }
   if (tid == 0) {
-    if (mode == 0) {
+    if (mode == 3) {
+      const uint32_t idesc = tc::idesc_f16(N, bf16);
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_f16_ta(tmem, tmem + 64 + 8 * kk, tc::sdesc_sw128(tc::smem_addr(Bs) + 32 * kk), idesc, kk > 0);
+    } else if (mode == 0) {
       const uint32_t idesc = tc::idesc_f16(N, bf16);
       for (int kk = 0; kk < 4; ++kk)
         tc::mma_f16(tmem, tc::sdesc_sw128(tc::smem_addr(As) + 32 * kk), tc::sdesc_sw128(tc::smem_addr(Bs) + 32 * kk),
@@ -90,7 +111,7 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
       *status = drained ? 1 : 2;
     }
   } else {
-    const int nc = mode == 0 ? N : 64;
+    const int nc = (mode == 0 || mode == 3) ? N : 64;
     float v[64];
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     for (int cc = 0; cc < nc; cc += 16) tc::tmem_ld16(taddr + cc, v + cc);
@@ -100,7 +121,7 @@ __global__ void __launch_bounds__(128) diag_mma_kernel(const uint16_t* A, const 
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when the MMAs did not drain (status 2)
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 __global__ void diag_wait_kernel(uint64_t limit_ns, long long* out) {

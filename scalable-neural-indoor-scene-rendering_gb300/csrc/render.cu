@@ -461,11 +461,20 @@ __global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* 
   }
 }
 
+// Tensor-memory columns of one MLP CTA: the H-column accumulator and the
+// H/2-column A operand of the hidden layers (two FP16 values per column),
+// rounded up to the allocation granularity (a power of two >= 32).
+constexpr int mlp_tmem_cols(int H) { return H + H / 2 <= 64 ? 64 : 128; }
+
 // Stage 4: per-tile MLP on tcgen05.  One CTA = 4 warps; each chunk is 128
-// samples of one tile.  A operands (gathered trilinear features + view
-// encoding, hidden activations) are written by the threads in the 128-byte
-// swizzled K-major layout; weights arrive by bulk copy (TMA) once per tile
-// change; accumulators live in tensor memory (H columns x 128 lanes).
+// samples of one tile.  The first layer's A operand (gathered trilinear
+// features + view encoding) is written by the threads into shared memory in
+// the 128-byte swizzled K-major layout; the hidden activations stay in tensor
+// memory: each thread reads its row of the accumulator, applies ReLU, packs
+// FP16 pairs and stores them into its own lane of the A-operand columns
+// (tcgen05.st), which the next layer's MMA reads as a TMEM A operand -- no
+// shared-memory traffic for them.  Weights arrive by bulk copy (TMA) once per
+// tile change; accumulators live in tensor memory (H columns x 128 lanes).
 // Every Linear, the output one included (N = 16, 3 used), is FP16 x FP16 ->
 // FP32 on tcgen05; biases enter as one extra K = 16 step (A = 1/16
 // everywhere, B slice = 16 copies of the bias).  The epilogue applies ReLU
@@ -497,7 +506,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(tmem_slot), H);
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), mlp_tmem_cols(H));
     tc::tmem_relinquish();
   }
   // every fp16 of the atom is 1/16: D += (1/16) * sum_{k<16} bias = bias (exact)
@@ -668,10 +677,14 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         const uint32_t a_base = tc::smem_addr(A0);
         const bool last = l == L;
         const uint32_t b_base = tc::smem_addr(Wsm + (last ? L * H * 128 : l * H * 128));
-        const int ksteps = l == 0 ? 4 : H / 16;  // K = 64 (padded input) or H
         const uint32_t id = last ? idesc_out : idesc;
-        for (int kk = 0; kk < ksteps; ++kk)
-          tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), id, kk > 0);
+        if (l == 0) {  // K = 64 (padded input) from the shared-memory A tile
+          for (int kk = 0; kk < 4; ++kk)
+            tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(b_base + 32 * kk), id, kk > 0);
+        } else {  // K = H from the activations in tensor memory (8 columns per K = 16 step)
+          for (int kk = 0; kk < H / 16; ++kk)
+            tc::mma_f16_ta(tmem, tmem + H + 8 * kk, tc::sdesc_sw128(b_base + 32 * kk), id, kk > 0);
+        }
         const uint32_t bias_tile = tc::smem_addr(Wsm + (last ? L * H * 128 + 2048 + H * 128 : L * H * 128 + 2048));
         tc::mma_f16(tmem, ones_desc, tc::sdesc_sw128(bias_tile + (last ? 0 : 32 * l)), id, 1);
         tc::mma_commit(mbar);
@@ -685,24 +698,20 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
       if (l < L) {
-        // ReLU + FP16 pack of 32 columns at a time into the A tile
+        // ReLU + FP16 pack of 32 columns at a time into this row's lane of
+        // the A-operand columns [H, H + H/2)
 #pragma unroll
         for (int half = 0; half < H / 32; ++half) {
           float v[32];
           tc::tmem_ld16(taddr + 32 * half, v);
           tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
           tc::tmem_wait_ld();
+          uint32_t packed[16];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint4 o;
-            o.x = pack_relu_h2(v[8 * q + 0], v[8 * q + 1]);
-            o.y = pack_relu_h2(v[8 * q + 2], v[8 * q + 3]);
-            o.z = pack_relu_h2(v[8 * q + 4], v[8 * q + 5]);
-            o.w = pack_relu_h2(v[8 * q + 6], v[8 * q + 7]);
-            *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(tid, 4 * half + q)) = o;
-          }
+          for (int q = 0; q < 16; ++q) packed[q] = pack_relu_h2(v[2 * q], v[2 * q + 1]);
+          tc::tmem_st16(taddr + H + 16 * half, packed);
         }
-        tc::fence_proxy_async();
+        tc::tmem_wait_st();
         tc::fence_before_sync();
         __syncthreads();
       } else {
@@ -742,7 +751,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when in-flight work did not drain
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, H);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, mlp_tmem_cols(H));
 }
 
 inline int grid_for(int64_t n, int threads, int cap_blocks) {
@@ -781,7 +790,7 @@ cudaError_t mlp_tc_t(const SceneDev& S, const Workspace& ws, float* rgb, int num
     const int regs_cta = ((fa.numRegs + 7) & ~7) * 128;
     int n = smem_sm / (smem + reserved);
     n = min(n, 65536 / max(regs_cta, 1));
-    n = min(n, 512 / H);  // tensor-memory columns per SM
+    n = min(n, 512 / mlp_tmem_cols(H));  // tensor-memory columns per SM
     per_sm = max(1, min(n, 8));
     return cudaSuccess;
   });

@@ -42,7 +42,8 @@ def _np(t):
     return t.detach().cpu().numpy()
 
 
-def test_diag_mma_fp16_bf16(cuda):
+@pytest.mark.parametrize("mode", [0, 3])  # A from shared memory / from tensor memory
+def test_diag_mma_fp16_bf16(cuda, mode):
     import torch
     g = torch.Generator().manual_seed(0)
     for bf16 in (0, 1):
@@ -54,7 +55,7 @@ def test_diag_mma_fp16_bf16(cuda):
             # keep the device copies referenced for the duration of the call
             Ad, Bd = Ah.cuda().view(torch.int16), Bh.cuda().view(torch.int16)
             D = torch.empty(128, N, device=cuda)
-            snisr._lib.check(snisr.lib().snisr_diag_mma(Ad.data_ptr(), Bd.data_ptr(), D.data_ptr(), N, bf16, 0,
+            snisr._lib.check(snisr.lib().snisr_diag_mma(Ad.data_ptr(), Bd.data_ptr(), D.data_ptr(), N, bf16, mode,
                                                         torch.cuda.current_stream().cuda_stream))
             ref = Ah.double() @ Bh.double().T
             err = (D.cpu().double() - ref).abs().max().item()
