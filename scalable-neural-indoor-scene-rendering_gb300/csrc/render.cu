@@ -591,22 +591,26 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       for (int k = 0; k < 8; ++k) cv[k] = __ldg(fp + k * G);
 #pragma unroll
       for (int j = 0; j < NENC; ++j) e[j] = __ldg(enc + (size_t)ray * 4 + my_g + j * G);
-      float acc[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+      // channel pairs accumulate with packed FP32x2 fused multiply-adds (two
+      // round-to-nearest FMAs per instruction: the same results as scalar FMAs)
+      uint64_t acc2[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         const float wk = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
+        const uint64_t w2 = f32x2(wk, wk);
         const __half2* hv = reinterpret_cast<const __half2*>(&cv[k]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          float2 pp = __half22float2(hv[q]);
-          acc[2 * q] = fmaf(wk, pp.x, acc[2 * q]);
-          acc[2 * q + 1] = fmaf(wk, pp.y, acc[2 * q + 1]);
+          const float2 pp = __half22float2(hv[q]);
+          acc2[q] = ffma2(w2, f32x2(pp.x, pp.y), acc2[q]);
         }
       }
-      f.x = pack_h2(acc[0], acc[1]); f.y = pack_h2(acc[2], acc[3]);
-      f.z = pack_h2(acc[4], acc[5]); f.w = pack_h2(acc[6], acc[7]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float lo, hi;
+        split_f32x2(acc2[q], lo, hi);
+        (&f.x)[q] = pack_h2(lo, hi);
+      }
     }
   };
   // the held rows into the A tile (8 consecutive rows per 8-lane phase: conflict-free)

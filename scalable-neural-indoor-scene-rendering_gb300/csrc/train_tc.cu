@@ -225,14 +225,19 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
         v0[k] = __ldg(src);
         v1[k] = __ldg(src + 1);
       }
-      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      // channel pairs accumulate with packed FP32x2 fused multiply-adds
+      uint64_t acc2[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        acc[0] = fmaf(w[k], v0[k].x, acc[0]); acc[1] = fmaf(w[k], v0[k].y, acc[1]);
-        acc[2] = fmaf(w[k], v0[k].z, acc[2]); acc[3] = fmaf(w[k], v0[k].w, acc[3]);
-        acc[4] = fmaf(w[k], v1[k].x, acc[4]); acc[5] = fmaf(w[k], v1[k].y, acc[5]);
-        acc[6] = fmaf(w[k], v1[k].z, acc[6]); acc[7] = fmaf(w[k], v1[k].w, acc[7]);
+        const uint64_t w2 = f32x2(w[k], w[k]);
+        acc2[0] = ffma2(w2, f32x2(v0[k].x, v0[k].y), acc2[0]);
+        acc2[1] = ffma2(w2, f32x2(v0[k].z, v0[k].w), acc2[1]);
+        acc2[2] = ffma2(w2, f32x2(v1[k].x, v1[k].y), acc2[2]);
+        acc2[3] = ffma2(w2, f32x2(v1[k].z, v1[k].w), acc2[3]);
       }
+      float acc[8];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) split_f32x2(acc2[j], acc[2 * j], acc[2 * j + 1]);
       uint32_t h[4], l[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) split_bf2(acc[2 * j], acc[2 * j + 1], h[j], l[j]);
