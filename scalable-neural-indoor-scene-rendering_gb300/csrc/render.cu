@@ -573,32 +573,52 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   // A row holds chunks [0,G) features, [G,G+4) view encoding, the rest 0.
   constexpr int RPI = 32 / G, NENC = 4 / G;
   const int my_g = lane / RPI, my_row = lane % RPI;
-  uint4 hf[G], he[G][NENC];  // the next chunk's rows, held until the A tile is free
-  auto gather_group = [&](int it, const uint4& ra, const uint4& rb, uint4& f, uint4* e) {
+  // A row group in flight: the corner and encoding loads of one group are
+  // issued one layer before they are interpolated (gather_issue at layer l,
+  // gather_finish at layer l + 1), so their latency hides behind a whole
+  // layer's MMA and epilogue instead of stalling the issuing warp.
+  struct Pending {
+    bool valid;
+    float fx, fy, fz;
+    uint4 cv[8];
+    uint4 e[NENC];
+  };
+  auto gather_issue = [&](int it, const uint4& ra, const uint4& rb, Pending& p) {
     const int src = it * RPI + my_row;
     const uint32_t rec = __shfl_sync(kFull, ra.x, src);
     const uint32_t ray = __shfl_sync(kFull, ra.y, src);
-    const float fx = __uint_as_float(__shfl_sync(kFull, rb.x, src));
-    const float fy = __uint_as_float(__shfl_sync(kFull, rb.y, src));
-    const float fz = __uint_as_float(__shfl_sync(kFull, rb.z, src));
-    f = make_uint4(0, 0, 0, 0);
+    p.fx = __uint_as_float(__shfl_sync(kFull, rb.x, src));
+    p.fy = __uint_as_float(__shfl_sync(kFull, rb.y, src));
+    p.fz = __uint_as_float(__shfl_sync(kFull, rb.z, src));
+    p.valid = rec != kInvalid;
+    if (p.valid) {
+      const uint4* fp = S.feat16 + (size_t)rec * 8 * G + my_g;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) p.cv[k] = __ldg(fp + k * G);
+#pragma unroll
+      for (int j = 0; j < NENC; ++j) p.e[j] = __ldg(enc + (size_t)ray * 4 + my_g + j * G);
+    }
+  };
+  // interpolates a group in flight and stores it into rows it*RPI.. of this
+  // warp's slice of the A tile (8 consecutive rows per 8-lane phase:
+  // conflict-free); chunks [0,G) features, [G,G+4) view encoding, the rest 0
+  auto gather_finish = [&](int it, const Pending& p) {
+    uint4 f = make_uint4(0, 0, 0, 0);
+    uint4 e[NENC];
 #pragma unroll
     for (int j = 0; j < NENC; ++j) e[j] = make_uint4(0, 0, 0, 0);
-    if (rec != kInvalid) {
-      const uint4* fp = S.feat16 + (size_t)rec * 8 * G + my_g;
-      uint4 cv[8];
+    if (p.valid) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) cv[k] = __ldg(fp + k * G);
-#pragma unroll
-      for (int j = 0; j < NENC; ++j) e[j] = __ldg(enc + (size_t)ray * 4 + my_g + j * G);
+      for (int j = 0; j < NENC; ++j) e[j] = p.e[j];
       // channel pairs accumulate with packed FP32x2 fused multiply-adds (two
       // round-to-nearest FMAs per instruction: the same results as scalar FMAs)
       uint64_t acc2[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        const float wk = ((k & 4) ? fx : 1.0f - fx) * ((k & 2) ? fy : 1.0f - fy) * ((k & 1) ? fz : 1.0f - fz);
+        const float wk = ((k & 4) ? p.fx : 1.0f - p.fx) * ((k & 2) ? p.fy : 1.0f - p.fy) *
+                         ((k & 1) ? p.fz : 1.0f - p.fz);
         const uint64_t w2 = f32x2(wk, wk);
-        const __half2* hv = reinterpret_cast<const __half2*>(&cv[k]);
+        const __half2* hv = reinterpret_cast<const __half2*>(&p.cv[k]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float2 pp = __half22float2(hv[q]);
@@ -612,20 +632,15 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         (&f.x)[q] = pack_h2(lo, hi);
       }
     }
+    const int r = warp * 32 + it * RPI + my_row;
+    *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, my_g)) = f;
+#pragma unroll
+    for (int j = 0; j < NENC; ++j) *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, G + my_g + j * G)) = e[j];
+#pragma unroll
+    for (int ch = G + 4 + my_g; ch < 8; ch += G)
+      *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
   };
-  // the held rows into the A tile (8 consecutive rows per 8-lane phase: conflict-free)
-  auto write_rows = [&]() {
-#pragma unroll
-    for (int it = 0; it < G; ++it) {
-      const int r = warp * 32 + it * RPI + my_row;
-      *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, my_g)) = hf[it];
-#pragma unroll
-      for (int j = 0; j < NENC; ++j) *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, G + my_g + j * G)) = he[it][j];
-#pragma unroll
-      for (int ch = G + 4 + my_g; ch < 8; ch += G)
-        *reinterpret_cast<uint4*>(A0 + tc::sw128_offset(r, ch)) = make_uint4(0, 0, 0, 0);
-    }
-  };
+  Pending pend;
 
   if (tid == 0) {
     chunk_slot[0] = atomicAdd(ctrl + CTRL_WORK, 1);
@@ -645,8 +660,10 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     cur_tile = cr.tile;
     w_pending = true;
 #pragma unroll
-    for (int it = 0; it < G; ++it) gather_group(it, my_ra, my_rb, hf[it], he[it]);
-    write_rows();
+    for (int it = 0; it < G; ++it) {
+      gather_issue(it, my_ra, my_rb, pend);
+      gather_finish(it, pend);
+    }
     tc::fence_proxy_async();
   }
   for (int iter = 0;; ++iter) {
@@ -670,9 +687,11 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
 
     // L hidden Linear layers and the output Linear (N = 16, 3 used), all on
     // the tensor core; each layer's bias enters as one extra K = 16 step.
-    // During each layer's MMA the threads gather their share of the next
-    // chunk's row groups.
+    // The next chunk's row groups are gathered alongside: group l's loads
+    // are issued during layer l and interpolated during layer l + 1, when
+    // the A tile (read only by layer 0) is free to take them.
     uint4 nra, nrb;
+    load_row(nx, nra, nrb);
     float out3[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int l = 0; l <= L; ++l) {
@@ -693,27 +712,26 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         tc::mma_f16(tmem, ones_desc, tc::sdesc_sw128(bias_tile + (last ? 0 : 32 * l)), id, 1);
         tc::mma_commit(mbar);
       }
-      if (l == 0) load_row(nx, nra, nrb);
-#pragma unroll
-      for (int it = l * G / (L + 1); it < (l + 1) * G / (L + 1); ++it) gather_group(it, nra, nrb, hf[it], he[it]);
+      if (l >= 1 && l - 1 < G) gather_finish(l - 1, pend);  // layer 0 has read the A tile
+      if (l < G) gather_issue(l, nra, nrb, pend);
       bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
       mphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
       if (l < L) {
-        // ReLU + FP16 pack of 32 columns at a time into this row's lane of
-        // the A-operand columns [H, H + H/2)
+        // ReLU + FP16 pack of 16 columns at a time into this row's lane of
+        // the A-operand columns [H, H + H/2) (16 at a time keeps the
+        // registers of the row group in flight free)
 #pragma unroll
-        for (int half = 0; half < H / 32; ++half) {
-          float v[32];
-          tc::tmem_ld16(taddr + 32 * half, v);
-          tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+        for (int part = 0; part < H / 16; ++part) {
+          float v[16];
+          tc::tmem_ld16(taddr + 16 * part, v);
           tc::tmem_wait_ld();
-          uint32_t packed[16];
+          uint32_t packed[8];
 #pragma unroll
-          for (int q = 0; q < 16; ++q) packed[q] = pack_relu_h2(v[2 * q], v[2 * q + 1]);
-          tc::tmem_st16(taddr + H + 16 * half, packed);
+          for (int q = 0; q < 8; ++q) packed[q] = pack_relu_h2(v[2 * q], v[2 * q + 1]);
+          tc::tmem_st8(taddr + H + 8 * part, packed);
         }
         tc::tmem_wait_st();
         tc::fence_before_sync();
@@ -737,7 +755,13 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
       w_pending = true;
     }
     tc::fence_before_sync();  // output columns read before the next chunk's MMA (barrier at the loop top)
-    write_rows();  // chunk c's last MMA has completed: the A tile is free
+    // the groups not yet interpolated (the one issued during the last layer,
+    // and any beyond one per layer)
+#pragma unroll
+    for (int it = L; it < G; ++it) {
+      if (it > L) gather_issue(it, nra, nrb, pend);
+      gather_finish(it, pend);
+    }
     tc::fence_proxy_async();
     if (tid < cnt) {
 #pragma unroll
