@@ -490,7 +490,7 @@ typedef struct snisr_tuning {
   int32_t scatter_blocks_per_sm; /* per-tile bucketing grid: 1..64 blocks per SM           */
   int32_t mlp_ctas_per_sm;       /* persistent MLP CTAs per SM: 0 = resident maximum, 1..8 */
   int32_t train_march_threads;   /* training march block size: 32..256, multiple of 32     */
-  int32_t train_fwd_ctas_per_sm; /* training TC forward CTAs per SM: 1 or 2                */
+  int32_t train_fwd_warps;       /* training TC forward warps per CTA: 4 or 8 (1 CTA / SM)  */
 } snisr_tuning;
 snisr_status snisr_scene_get_tuning(const snisr_scene* scene, snisr_tuning* out);
 snisr_status snisr_scene_set_tuning(snisr_scene* scene, const snisr_tuning* tuning);

@@ -117,7 +117,12 @@ def _p(a: np.ndarray | None):
     return a.ctypes.data_as(C.c_void_p)
 
 
-_EMUL = {None: 0, "tc": 1}
+# operand emulation of the tensor-core training form: "tc" is the kernels'
+# (three-part split BF16 forward for the colours, two-part split in the
+# backward's recomputation, single BF16 backward products); the others
+# attribute its error: the two-part split in both passes ("tc_split2"), its
+# forward or backward rounding alone, the three-part split in both passes
+_EMUL = {None: 0, "tc": 5, "tc_split2": 1, "tc_forward": 2, "tc_backward": 3, "tc_split3": 4}
 
 
 def threads() -> int:
@@ -177,7 +182,8 @@ class OracleScene:
     def train_forward(self, vfeat, vdens, mlp, o, d, ray_tile, nthreads: int | None = None, emulate: str | None = None):
         """FP64 colours [n,3] and sample counts [n] of ray segments (ray i inside tile ray_tile[i]).
         emulate: None (exact) or "tc" -- round the MLP operands as the tensor-core form does
-        (split BF16 hi+lo forward operands, BF16 backward operands)."""
+        (split BF16 hi+mid+lo forward operands, BF16 backward operands); the other keys of
+        _EMUL attribute that form's error."""
         n = o.shape[0]
         rgb = np.zeros((n, 3))
         cnt = np.zeros(n, np.int32)

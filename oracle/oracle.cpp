@@ -842,26 +842,55 @@ struct TrainParams {
   const float* vfeat;  // [NV][F]
   const float* vdens;  // [NV]
   const float* mlp;    // [NT][P]
-  // emul = 1: operand emulation of the tensor-core training form.  Forward
-  // products (and the backward's recomputation) use split BF16 operands,
-  // v = hi + lo with hi = bf16(v), lo = bf16(v - hi): MLP inputs, weights,
-  // biases and post-ReLU activations (rf).  A product of two split operands
-  // is taken as three BF16 products, hi*hi + hi*lo + lo*hi: the lo*lo term
-  // is dropped, as the kernels issue three MMAs per K step (product3).
-  // Backward products use single BF16 operands (rb): the output-logit
-  // gradient, each hidden delta, W^T in the data gradient and the activation
-  // in the weight gradient.
+  // emul = 5: operand emulation of the tensor-core training form.  The
+  // forward pass that produces the colours splits its operands in three
+  // BF16 parts, v = hi + mid + lo (hi = bf16(v), mid = bf16(v - hi),
+  // lo = bf16(v - hi - mid)): MLP inputs, weights, biases and post-ReLU
+  // activations (rf).  A product of two split operands is taken down to the
+  // 2^-24 terms, hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid (six
+  // MMAs per K step).  The backward pass recomputes the activations with a
+  // two-part split, v = hi + lo and hi.hi + hi.lo + lo.hi (three MMAs);
+  // they set the ReLU masks and, rounded once more, the weight-gradient
+  // operands.  The colour pass adds the exact biases, the recomputation
+  // their three-part split.  Backward products use single BF16 operands (rb): the
+  // output-logit gradient, each hidden delta, W^T in the data gradient and
+  // the activation in the weight gradient.
+  // emul = 1: the two-part split in both passes; 4: the three-part split in
+  // both; 2 / 3: only the forward / only the backward rounding of emul = 1
+  // (these attribute the tensor-core form's error).
   int emul = 0;
-  double rf(double v) const {
-    if (emul == 0) return v;
+  // parts of the forward operand split: 0 (exact), 2 or 3; `colour` selects
+  // the pass that produces the colours, otherwise the backward's recomputation
+  int split(bool colour) const {
+    switch (emul) {
+      case 1: case 2: return 2;
+      case 4: return 3;
+      case 5: return colour ? 3 : 2;
+      default: return 0;
+    }
+  }
+  int bias_split(bool colour) const { return emul == 5 ? (colour ? 0 : 3) : split(colour); }
+  bool bwd_r() const { return emul == 1 || emul == 3 || emul == 4 || emul == 5; }
+  static double rf(double v, int parts) {
+    if (parts == 0) return v;
     const float hi = round_bf16((float)v);
+    if (parts == 3) {
+      const float mid = round_bf16((float)v - hi);
+      return (double)hi + (double)mid + (double)round_bf16(((float)v - hi) - mid);
+    }
     return (double)hi + (double)round_bf16((float)v - hi);
   }
-  double rb(double v) const { return emul == 0 ? v : (double)round_bf16((float)v); }
-  // w * x for the forward products (exact when emul == 0)
-  double product3(double w, double x) const {
-    if (emul == 0) return w * x;
+  double rb(double v) const { return bwd_r() ? (double)round_bf16((float)v) : v; }
+  // w * x for the forward products (exact without forward rounding)
+  static double product(double w, double x, int parts) {
+    if (parts == 0) return w * x;
     const float wh = round_bf16((float)w), xh = round_bf16((float)x);
+    if (parts == 3) {
+      const float wm = round_bf16((float)w - wh), xm = round_bf16((float)x - xh);
+      const double wl = (double)round_bf16(((float)w - wh) - wm), xl = (double)round_bf16(((float)x - xh) - xm);
+      return (double)wh * xh + (double)wh * xm + (double)wm * xh + (double)wh * xl + wl * (double)xh +
+             (double)wm * xm;
+    }
     const double wl = (double)round_bf16((float)w - wh), xl = (double)round_bf16((float)x - xh);
     return (double)wh * (double)xh + (double)wh * xl + wl * (double)xh;
   }
@@ -892,26 +921,35 @@ void train_forward_ray(const Scene& s, const TrainParams& p, int tile, const flo
       ts.dv = (double)(g.interval * s.inv_voxel);
       ts.alpha = 1.0 - std::exp(-ts.sigma * ts.dv);
       ts.T = T;
-      ts.x.assign((size_t)s.in, 0.0);
-      for (int c = 0; c < s.F; ++c) {
-        for (int k = 0; k < 8; ++k) ts.x[(size_t)c] += ts.w[k] * (double)p.vfeat[(int64_t)cn[k] * s.F + c];
-        ts.x[(size_t)c] = p.rf(ts.x[(size_t)c]);
-      }
-      for (int i = 0; i < 27; ++i) ts.x[(size_t)(s.F + i)] = p.rf(enc[(size_t)i]);
-      // MLP with stored activations
-      std::vector<double> cur = ts.x;
-      int64_t off = 0;
-      for (int l = 0; l <= s.L; ++l) {
-        int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
-        std::vector<double> nx((size_t)fo);
-        for (int oo = 0; oo < fo; ++oo) {
-          double acc = p.rf(W[off + (int64_t)fi * fo + oo]);
-          for (int i = 0; i < fi; ++i) acc += p.product3(W[off + (int64_t)oo * fi + i], cur[(size_t)i]);
-          nx[(size_t)oo] = l < s.L ? p.rf(std::max(acc, 0.0)) : acc;
+      std::vector<double> xe((size_t)s.in, 0.0);  // exact inputs
+      for (int c = 0; c < s.F; ++c)
+        for (int k = 0; k < 8; ++k) xe[(size_t)c] += ts.w[k] * (double)p.vfeat[(int64_t)cn[k] * s.F + c];
+      for (int i = 0; i < 27; ++i) xe[(size_t)(s.F + i)] = enc[(size_t)i];
+      // MLP with operands split in `parts`; the hidden activations go to hs
+      auto mlp = [&](int parts, int bparts, std::vector<double>& x, std::vector<std::vector<double>>* hs) {
+        x.resize(xe.size());
+        for (size_t i = 0; i < xe.size(); ++i) x[i] = TrainParams::rf(xe[i], parts);
+        std::vector<double> cur = x;
+        int64_t off = 0;
+        for (int l = 0; l <= s.L; ++l) {
+          int fi = l == 0 ? s.in : s.H, fo = l == s.L ? 3 : s.H;
+          std::vector<double> nx((size_t)fo);
+          for (int oo = 0; oo < fo; ++oo) {
+            double acc = TrainParams::rf(W[off + (int64_t)fi * fo + oo], bparts);
+            for (int i = 0; i < fi; ++i) acc += TrainParams::product(W[off + (int64_t)oo * fi + i], cur[(size_t)i], parts);
+            nx[(size_t)oo] = l < s.L ? TrainParams::rf(std::max(acc, 0.0), parts) : acc;
+          }
+          off += (int64_t)fi * fo + fo;
+          if (l < s.L && hs) hs->push_back(nx);
+          cur.swap(nx);
         }
-        off += (int64_t)fi * fo + fo;
-        if (l < s.L) ts.h.push_back(nx);
-        cur.swap(nx);
+        return cur;
+      };
+      // stored activations: the backward's recomputation; colours: the forward
+      std::vector<double> cur = mlp(p.split(false), p.bias_split(false), ts.x, &ts.h);
+      if (p.split(true) != p.split(false) || p.bias_split(true) != p.bias_split(false)) {
+        std::vector<double> xc;
+        cur = mlp(p.split(true), p.bias_split(true), xc, nullptr);
       }
       for (int c = 0; c < 3; ++c) {
         ts.c[c] = sigmoid<double>(cur[(size_t)c]);

@@ -766,7 +766,7 @@ snisr_status snisr_scene_get_tuning(const snisr_scene* sc, snisr_tuning* out) {
     return set_error(SNISR_INVALID_ARG, "get_tuning: null argument");
   const Tuning& t = sc->ws.tune;
   *out = snisr_tuning{t.traverse_threads, t.scatter_blocks_per_sm, t.mlp_ctas_per_sm, t.train_march_threads,
-                      t.train_fwd_ctas_per_sm};
+                      t.train_fwd_warps};
   return SNISR_OK;
 }
 
@@ -775,10 +775,10 @@ snisr_status snisr_scene_set_tuning(snisr_scene* sc, const snisr_tuning* t) {
   auto warps_ok = [](int v) { return v >= 32 && v <= 256 && v % 32 == 0; };
   if (!warps_ok(t->traverse_threads) || !warps_ok(t->train_march_threads) || t->scatter_blocks_per_sm < 1 ||
       t->scatter_blocks_per_sm > 64 || t->mlp_ctas_per_sm < 0 || t->mlp_ctas_per_sm > 8 ||
-      (t->train_fwd_ctas_per_sm != 1 && t->train_fwd_ctas_per_sm != 2))
+      (t->train_fwd_warps != 4 && t->train_fwd_warps != 8))
     return set_error(SNISR_INVALID_ARG, "set_tuning: value out of range");
   sc->ws.tune = Tuning{t->traverse_threads, t->scatter_blocks_per_sm, t->mlp_ctas_per_sm, t->train_march_threads,
-                       t->train_fwd_ctas_per_sm};
+                       t->train_fwd_warps};
   return SNISR_OK;
 }
 
@@ -912,7 +912,7 @@ snisr_status snisr_scene_autotune_train(snisr_scene* sc, const float* vfeat, con
   };
   const std::vector<std::pair<int Tuning::*, std::vector<int>>> knobs = {
       {&Tuning::train_march_threads, {64, 128, 256}},
-      {&Tuning::train_fwd_ctas_per_sm, {1, 2}},
+      {&Tuning::train_fwd_warps, {4, 8}},
   };
   snisr_status s = tune_descent(sc, knobs, eval, best_ms);
   cudaEventDestroy(e0);

@@ -21,7 +21,7 @@ struct Tuning {
   int scatter_blocks_per_sm = 16; // scatter_kernel grid = SMs x this
   int mlp_ctas_per_sm = 0;        // persistent mlp_tc_kernel CTAs per SM (0 = resident maximum)
   int train_march_threads = 128;  // tr_march_kernel block size (multiple of 32, <= 256)
-  int train_fwd_ctas_per_sm = 2;  // tr_mlp_fwd_tc CTAs per SM (1 or 2)
+  int train_fwd_warps = 8;        // tr_mlp_fwd_tc warps per CTA (4 or 8; one CTA per SM)
 };
 
 // Per-scene workspace, sized at creation; nothing is allocated per frame.
@@ -99,7 +99,7 @@ struct TrainTcArgs {
   float* gmlp;
   float* gstage;  // [NT][4][64 x 64 + 64] weight-gradient staging of the backward kernel
   int num_sms;
-  int fwd_ctas_per_sm;
+  int fwd_warps;
 };
 int train_tc_image_bytes(int H, int L);
 int train_tc_bwd_smem_bytes(int H, int L);

@@ -537,7 +537,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   const int img_stride = (train_tc_image_bytes(64, 3) + 127) & ~127;
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
               al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al((NT + 2) * 4) + al(16) +
-              al(rays * 128) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
+              al(rays * 192) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
               al((size_t)nvox * 32) + al((size_t)NT * 4 * (64 * 64 + 64) * 4);
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, sz);
@@ -556,7 +556,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   T->dlt = (float*)take(cap * kDltStride * 4);
   T->coff = (int32_t*)take((NT + 2) * 4);
   T->work = (int*)take(16);
-  T->enc = (uint4*)take(rays * 128);
+  T->enc = (uint4*)take(rays * 192);  // 12 uint4 per ray: BF16 hi, mid, lo of the view encoding
   T->wimg = (uint8_t*)take((size_t)img_stride * NT);
   T->stage = (TrainRec*)take((size_t)rays * kStage * sizeof(TrainRec));
   T->dcache = (float4*)take((size_t)nvox * 32);
@@ -646,7 +646,7 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   cudaError_t e;
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, nullptr, nullptr, nullptr, num_sms, ws.tune.train_fwd_ctas_per_sm};
+                  T->c, T->dout, nullptr, nullptr, nullptr, num_sms, ws.tune.train_fwd_warps};
     e = launch_train_tc(S, a, false, st);
     if (e == cudaErrorInvalidValue) return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
   } else if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
@@ -701,7 +701,7 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   if (T->last_form != form) return set_error(SNISR_INVALID_ARG, "train_backward: the forward call used another form");
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, gvfeat, gmlp, T->gstage, num_sms, ws.tune.train_fwd_ctas_per_sm};
+                  T->c, T->dout, gvfeat, gmlp, T->gstage, num_sms, ws.tune.train_fwd_warps};
     e = launch_train_tc(S, a, true, st);
   } else if (F == 32 && H == 64 && L == 3)
     e = train_plain_mlp_bwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->dout, T->act, T->dlt, gvfeat,

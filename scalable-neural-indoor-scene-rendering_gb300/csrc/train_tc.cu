@@ -10,14 +10,21 @@
 // stay in tensor memory across all chunks of a tile and are flushed with
 // atomics when the CTA moves to another tile.
 //
-// Precision.  Forward products (and the backward's recomputation of them)
-// use split BF16 operands: v = hi + lo, hi = bf16(v), lo = bf16(v - hi), and
-// A.B = A_hi.B_hi + A_lo.B_hi + A_hi.B_lo, about 16 significant bits.  The
-// ReLU masks of the backward then follow an FP32 evaluation except within
-// ~2^-16 of a kink; with single BF16 operands the masks of units near a kink
-// flip and the feature gradients move by several percent.  Backward products
-// (hidden deltas, weight gradients) use single BF16 operands: their rounding
-// error is smooth (~2^-9 per operand).
+// Precision.  The forward pass that produces the colours splits its operands
+// in three BF16 parts, v = hi + mid + lo (hi = bf16(v), mid = bf16(v - hi),
+// lo = bf16(v - hi - mid)), and takes A.B down to the 2^-24 terms:
+// A_hi.B_hi + A_mid.B_hi + A_hi.B_mid + A_mid.B_mid + A_lo.B_hi + A_hi.B_lo,
+// as accurate as an FP32 evaluation.  The colours feed the loss, whose
+// residuals near convergence are small: a two-part split (~2^-17 per
+// operand) moved the loss gradient of the MLP parameters by ~1 %.  The
+// backward's recomputation of the activations uses the two-part split
+// v = hi + mid, A_hi.B_hi + A_mid.B_hi + A_hi.B_mid (about 16 significant
+// bits): it only sets the ReLU masks, which then follow an FP32 evaluation
+// except within ~2^-16 of a kink, and the weight-gradient operands, which
+// are rounded to BF16 anyway.  The colour pass adds the FP32 biases; the
+// recomputation takes them in three BF16 parts.
+// Backward products (hidden deltas, weight gradients) use single BF16
+// operands: their rounding error is smooth (~2^-9 per operand).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -36,6 +43,7 @@ struct __align__(16) TrainRecT {  // mirror of the record written by the march k
 };
 
 constexpr uint32_t kBf16Eighth = 0x3E003E00u;  // 1/8, two lanes
+constexpr uint32_t kBf16Quarter = 0x3E803E80u; // 1/4, two lanes
 constexpr uint32_t kBf16One = 0x3F803F80u;     // 1.0, two lanes
 
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
@@ -50,10 +58,20 @@ __device__ __forceinline__ void split_bf2(float a, float b, uint32_t& hi, uint32
   hi = pack_bf2(a, b);
   lo = pack_bf2(a - bf_lo(hi), b - bf_hi(hi));
 }
-__device__ __forceinline__ void split_bf16(float v, uint16_t& hi, uint16_t& lo) {
+// three-part split of two values: hi, mid = bf16(v - hi), lo = bf16(v - hi - mid)
+__device__ __forceinline__ void split3_bf2(float a, float b, uint32_t& hi, uint32_t& mid, uint32_t& lo) {
+  hi = pack_bf2(a, b);
+  const float ra = a - bf_lo(hi), rb = b - bf_hi(hi);
+  mid = pack_bf2(ra, rb);
+  lo = pack_bf2(ra - bf_lo(mid), rb - bf_hi(mid));
+}
+__device__ __forceinline__ void split3_bf16(float v, uint16_t& hi, uint16_t& mid, uint16_t& lo) {
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   hi = __bfloat16_as_ushort(h);
-  lo = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+  const float r = v - __bfloat162float(h);
+  const __nv_bfloat16 m = __float2bfloat16_rn(r);
+  mid = __bfloat16_as_ushort(m);
+  lo = __bfloat16_as_ushort(__float2bfloat16_rn(r - __bfloat162float(m)));
 }
 // positive BF16 value in the low / high half (sign clear, not zero)
 __device__ __forceinline__ bool pos_lo(uint32_t v) { return (v & 0x8000u) == 0 && (v & 0x7FFFu) != 0; }
@@ -73,20 +91,29 @@ __device__ __forceinline__ uint32_t idesc_bf16(int n, bool a_mn, bool b_mn) {
 // ---- per-tile weight image -------------------------------------------------
 // All sub-tiles K-major, 128-byte swizzled, 64 K columns:
 //   hi part : W_l [H][64] (l < L), W_out [16][64]
-//   lo part : the same shapes holding bf16(w - hi)
-//   bias    : [H][64], K slice 16l..16l+15 of row o = 8 x hi(b_l[o]), 8 x lo(b_l[o])
+//   mid part: the same shapes holding bf16(w - hi)
+//   bias    : [H][64], K slice 16l..16l+15 of row o = 8 x hi, 4 x mid, 4 x lo
+//             of b_l[o] (the MMA's A operand is 1/8 in K columns 0..7 and
+//             1/4 in 8..15, so that the slice sums to hi + mid + lo)
 //   out bias: [16][64], K slice 0..15 likewise for the output layer
 //   W^T     : per layer l <= L, [64 rows = inputs of l][K = outputs] (hi only)
+//   lo part : the shapes of the hi part holding bf16(w - hi - mid)
+//   FP32 biases: per layer l <= L, 64 floats
+// The backward's copy ends at the W^T part (bwd_bytes); the forward copies
+// the hi and mid parts, then the lo part and the FP32 biases.
 struct ImageLayout {
-  int hi_part, lo_off, bias_off, obias_off, fwd_bytes, t_off, total;
+  int hi_part, mid_off, bias_off, obias_off, fwd_bytes, t_off, bwd_bytes, lo_off, fbias_off, total;
   __host__ __device__ ImageLayout(int H, int L) {
     hi_part = L * H * 128 + 2048;
-    lo_off = hi_part;
+    mid_off = hi_part;
     bias_off = 2 * hi_part;
     obias_off = bias_off + H * 128;
     fwd_bytes = obias_off + 2048;
     t_off = fwd_bytes;
-    total = t_off + (L + 1) * 8192;
+    bwd_bytes = t_off + (L + 1) * 8192;
+    lo_off = bwd_bytes;
+    fbias_off = lo_off + hi_part;
+    total = fbias_off + (L + 1) * 256;
   }
 };
 
@@ -107,28 +134,33 @@ __global__ void pack_train_weights(const float* __restrict__ mlp, int P, int IN,
     const int fi = l == 0 ? IN : H, fo = l == L ? 3 : H;
     const int wofs = l < L ? l * H * 128 : L * H * 128;
     uint8_t* whi = img + wofs;
+    uint8_t* wmid = img + lay.mid_off + wofs;
     uint8_t* wlo = img + lay.lo_off + wofs;
     uint8_t* btile = img + (l < L ? lay.bias_off : lay.obias_off);
     uint8_t* tt = img + lay.t_off + l * 8192;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * fi; e += gridDim.x * blockDim.x) {
       const int o = e / fi, i = e % fi;
-      uint16_t h, lo;
-      split_bf16(p[off + e], h, lo);
+      uint16_t h, m, lo;
+      split3_bf16(p[off + e], h, m, lo);
       *reinterpret_cast<uint16_t*>(whi + sw_off(o, i)) = h;
+      *reinterpret_cast<uint16_t*>(wmid + sw_off(o, i)) = m;
       *reinterpret_cast<uint16_t*>(wlo + sw_off(o, i)) = lo;
       *reinterpret_cast<uint16_t*>(tt + sw_off(i, o)) = h;
     }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * 16; e += gridDim.x * blockDim.x) {
       const int o = e / 16, k = e % 16;
-      uint16_t h, lo;
-      split_bf16(p[off + (int64_t)fi * fo + o], h, lo);
-      *reinterpret_cast<uint16_t*>(btile + sw_off(o, (l < L ? 16 * l : 0) + k)) = k < 8 ? h : lo;
+      uint16_t h, m, lo;
+      split3_bf16(p[off + (int64_t)fi * fo + o], h, m, lo);
+      *reinterpret_cast<uint16_t*>(btile + sw_off(o, (l < L ? 16 * l : 0) + k)) = k < 8 ? h : k < 12 ? m : lo;
+      if (k == 0) reinterpret_cast<float*>(img + lay.fbias_off)[64 * l + o] = p[off + (int64_t)fi * fo + o];
     }
     off += (int64_t)fi * fo + fo;
   }
 }
 
-// per-ray view encoding (27 values + 5 zeros) as BF16 hi [0,4) and lo [4,8) uint4s
+// per-ray view encoding (27 values + 5 zeros) as BF16 hi [0,4), mid [4,8)
+// and lo [8,12) uint4s
+constexpr int kEncQuads = 12;
 __global__ void ray_enc_kernel(const float* __restrict__ dirs, int64_t n, uint4* enc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     float d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
@@ -136,11 +168,22 @@ __global__ void ray_enc_kernel(const float* __restrict__ dirs, int64_t n, uint4*
     dir_encoding(d, 4, e);
     for (int k = 27; k < 32; ++k) e[k] = 0.f;
     for (int q = 0; q < 4; ++q) {
-      uint32_t h[4], l[4];
-      for (int j = 0; j < 4; ++j) split_bf2(e[8 * q + 2 * j], e[8 * q + 2 * j + 1], h[j], l[j]);
-      enc[8 * i + q] = make_uint4(h[0], h[1], h[2], h[3]);
-      enc[8 * i + 4 + q] = make_uint4(l[0], l[1], l[2], l[3]);
+      uint32_t h[4], m[4], l[4];
+      for (int j = 0; j < 4; ++j) split3_bf2(e[8 * q + 2 * j], e[8 * q + 2 * j + 1], h[j], m[j], l[j]);
+      enc[kEncQuads * i + q] = make_uint4(h[0], h[1], h[2], h[3]);
+      enc[kEncQuads * i + 4 + q] = make_uint4(m[0], m[1], m[2], m[3]);
+      enc[kEncQuads * i + 8 + q] = make_uint4(l[0], l[1], l[2], l[3]);
     }
+  }
+}
+
+// the A operand of the bias MMAs: 8 rows of 64 K columns (128-byte swizzle),
+// 1/8 in K columns 0..7 and 1/4 in 8..15 of every 16-column slice
+__device__ __forceinline__ void init_bias_ones(uint8_t* ones, int tid, int nth) {
+  for (int k = tid; k < 64; k += nth) {
+    const int r = k >> 3, c = (k & 7) ^ r;  // 16-byte chunk k of the tile holds K chunk c of row r
+    const uint32_t v = (c & 1) ? kBf16Quarter : kBf16Eighth;
+    reinterpret_cast<uint4*>(ones)[k] = make_uint4(v, v, v, v);
   }
 }
 
@@ -171,18 +214,21 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
   return p;
 }
 
-// Gather of the split input rows [0,128) of the chunk into Xhi / Xlo: lane
-// (g, row) interpolates 8 FP32 channels over the 8 corners of each of its G
-// rows; view encoding copied from the per-ray split table.  Loads are issued
-// in stages across the lane's rows (records, then corner ids and encodings,
-// then features) so that each stage waits for memory once, not once per row.
-template <int F, int NW = 4>
+// Gather of the split input rows [0,128) of the chunk into the NP part tiles
+// X[0..NP) (hi, mid and, for NP = 3, lo): lane (g, row) interpolates 8 FP32
+// channels over the 8 corners of each of its rows; view encoding copied from
+// the per-ray split table.  Loads are issued in stages across the lane's rows
+// (records, then corner ids and encodings, then features) so that each stage
+// waits for memory once, not once per row.
+template <int F, int NW, int NP>
 __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restrict__ vfeat,
                                          const TrainRecT* __restrict__ recs, int row0, int cnt,
-                                         const uint4* __restrict__ enc, uint8_t* Xhi, uint8_t* Xlo, int warp, int lane) {
+                                         const uint4* __restrict__ enc, uint8_t* const (&X)[NP], int warp,
+                                         int lane) {
   // NW warps share the 128 rows: RPW rows per warp, RPI rows per lane pass
   constexpr int G = F / 8, RPI = 32 / G, RPW = 128 / NW, ITS = RPW / RPI;
   static_assert(RPW % RPI == 0, "rows per warp must be a multiple of rows per pass");
+  static_assert(NP == 2 || NP == 3, "two or three parts");
   const int my_g = lane / RPI, my_row = lane % RPI;
   const uint4 z = make_uint4(0, 0, 0, 0);
   uint4 head[ITS], fr[ITS];  // {rec, ray, tile, pad}, {f0, f1, f2, dv}
@@ -196,7 +242,7 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
     }
   }
   int4 ca[ITS], cb[ITS];
-  uint4 eh[ITS], el[ITS];
+  uint4 ev[ITS][NP];
 #pragma unroll
   for (int it = 0; it < ITS; ++it) {
     const int r = warp * RPW + it * RPI + my_row;
@@ -205,8 +251,8 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
       ca[it] = __ldg(cn);
       cb[it] = __ldg(cn + 1);
       if (my_g < 4) {  // G >= 4 lanes share a row: lane group g copies encoding chunk g (and g + G)
-        eh[it] = __ldg(enc + (size_t)head[it].y * 8 + my_g);
-        el[it] = __ldg(enc + (size_t)head[it].y * 8 + 4 + my_g);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) ev[it][q] = __ldg(enc + (size_t)head[it].y * kEncQuads + 4 * q + my_g);
       }
     }
   }
@@ -238,79 +284,74 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
       float acc[8];
 #pragma unroll
       for (int j = 0; j < 4; ++j) split_f32x2(acc2[j], acc[2 * j], acc[2 * j + 1]);
-      uint32_t h[4], l[4];
+      uint32_t pv[3][4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) split_bf2(acc[2 * j], acc[2 * j + 1], h[j], l[j]);
-      *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, my_g)) = make_uint4(h[0], h[1], h[2], h[3]);
-      *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, my_g)) = make_uint4(l[0], l[1], l[2], l[3]);
+      for (int j = 0; j < 4; ++j) {
+        if (NP == 3)
+          split3_bf2(acc[2 * j], acc[2 * j + 1], pv[0][j], pv[1][j], pv[2][j]);
+        else
+          split_bf2(acc[2 * j], acc[2 * j + 1], pv[0][j], pv[1][j]);
+      }
+#pragma unroll
+      for (int q = 0; q < NP; ++q)
+        *reinterpret_cast<uint4*>(X[q] + tc::sw128_offset(r, my_g)) = make_uint4(pv[q][0], pv[q][1], pv[q][2], pv[q][3]);
       if (my_g < 4) {
-        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, G + my_g)) = eh[it];
-        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, G + my_g)) = el[it];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) *reinterpret_cast<uint4*>(X[q] + tc::sw128_offset(r, G + my_g)) = ev[it][q];
       }
       if (G < 4 && my_g + G < 4) {  // G = 2: the second half of the encoding
-        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, 2 * G + my_g)) =
-            __ldg(enc + (size_t)head[it].y * 8 + G + my_g);
-        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, 2 * G + my_g)) =
-            __ldg(enc + (size_t)head[it].y * 8 + 4 + G + my_g);
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+          *reinterpret_cast<uint4*>(X[q] + tc::sw128_offset(r, 2 * G + my_g)) =
+              __ldg(enc + (size_t)head[it].y * kEncQuads + 4 * q + G + my_g);
       }
 #pragma unroll
       for (int ch = G + 4 + my_g; ch < 8; ch += G) {
-        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, ch)) = z;
-        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, ch)) = z;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) *reinterpret_cast<uint4*>(X[q] + tc::sw128_offset(r, ch)) = z;
       }
     } else {
 #pragma unroll
       for (int ch = my_g; ch < 8; ch += G) {
-        *reinterpret_cast<uint4*>(Xhi + tc::sw128_offset(r, ch)) = z;
-        *reinterpret_cast<uint4*>(Xlo + tc::sw128_offset(r, ch)) = z;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) *reinterpret_cast<uint4*>(X[q] + tc::sw128_offset(r, ch)) = z;
       }
     }
   }
 }
 
-// ReLU + split BF16 pack of a 128 x H accumulator into hi / lo activation
-// tiles (dst_lo may be null: hi only)
-template <int H>
-__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_lo, int row) {
+// ReLU + split BF16 pack of one of NC column parts of a 128 x H accumulator
+// (H / NC columns, a multiple of 16; part p covers [p H / NC, (p + 1) H / NC))
+// into the NP part tiles dst[0..NP) (hi, mid, lo); a null dst[q], q > 0,
+// skips that part.
+template <int H, int NC, int NP>
+__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* const (&dst)[NP], int row, int part) {
+  constexpr int CP = H / NC, SUB = CP < 32 ? CP : 32;
+  static_assert(CP % 16 == 0 && CP % SUB == 0, "column parts of 16");
 #pragma unroll
-  for (int half = 0; half < H / 32; ++half) {
-    float v[32];
-    tc::tmem_ld16(taddr + 32 * half, v);
-    tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+  for (int s0 = 0; s0 < CP; s0 += SUB) {
+    float v[SUB];
+#pragma unroll
+    for (int j = 0; j < SUB; j += 16) tc::tmem_ld16(taddr + part * CP + s0 + j, v + j);
     tc::tmem_wait_ld();
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t h[4], l[4];
+    for (int q = 0; q < SUB / 8; ++q) {
+      const int chunk = (part * CP + s0) / 8 + q;
+      uint32_t pv[3][4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-        split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], l[j]);
-      *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, 4 * half + q)) = make_uint4(h[0], h[1], h[2], h[3]);
-      if (dst_lo)
-        *reinterpret_cast<uint4*>(dst_lo + tc::sw128_offset(row, 4 * half + q)) = make_uint4(l[0], l[1], l[2], l[3]);
+      for (int j = 0; j < 4; ++j) {
+        const float a0 = fmaxf(v[8 * q + 2 * j], 0.f), a1 = fmaxf(v[8 * q + 2 * j + 1], 0.f);
+        if (NP == 3)
+          split3_bf2(a0, a1, pv[0][j], pv[1][j], pv[2][j]);
+        else
+          split_bf2(a0, a1, pv[0][j], pv[1][j]);
+      }
+#pragma unroll
+      for (int k = 0; k < NP; ++k)
+        if (k == 0 || dst[k])
+          *reinterpret_cast<uint4*>(dst[k] + tc::sw128_offset(row, chunk)) =
+              make_uint4(pv[k][0], pv[k][1], pv[k][2], pv[k][3]);
     }
-  }
-}
-
-// The same for one of NP column parts of the accumulator (H / NP columns,
-// a multiple of 16): part p covers columns [p H / NP, (p + 1) H / NP).
-template <int H, int NP>
-__device__ __forceinline__ void epi_relu_split_part(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_lo, int row,
-                                                    int part) {
-  constexpr int CP = H / NP;
-  static_assert(CP % 16 == 0, "column parts of 16");
-  float v[CP];
-#pragma unroll
-  for (int j = 0; j < CP; j += 16) tc::tmem_ld16(taddr + part * CP + j, v + j);
-  tc::tmem_wait_ld();
-#pragma unroll
-  for (int q = 0; q < CP / 8; ++q) {
-    const int chunk = part * (CP / 8) + q;
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], l[j]);
-    *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, chunk)) = make_uint4(h[0], h[1], h[2], h[3]);
-    if (dst_lo) *reinterpret_cast<uint4*>(dst_lo + tc::sw128_offset(row, chunk)) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -328,43 +369,135 @@ __device__ __forceinline__ bool wait_mma(Bars& b, int tid) {
 }
 
 // One split-precision forward layer: tmem = A.W^T + bias with N = n outputs,
-// K = 16 * ksteps.  A_hi.W_hi + A_lo.W_hi + A_hi.W_lo, then the bias step
-// (A = 1/8 everywhere, B slice = 8 x hi, 8 x lo of the bias).
-__device__ __forceinline__ void issue_split_layer(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t w_hi,
-                                                  uint32_t w_lo, uint32_t bias_slice, uint64_t ones8, int n,
-                                                  int ksteps) {
+// K = 16 * ksteps; a[q] / w[q] are the shared-memory part tiles (hi, mid,
+// lo) of the activations and the weights.  np = 2: A_hi.W_hi + A_mid.W_hi +
+// A_hi.W_mid; np = 3 adds A_mid.W_mid + A_lo.W_hi + A_hi.W_lo.  Then the
+// bias step (A = 1/8 in K columns 0..7 and 1/4 in 8..15, B slice = 8 x hi,
+// 4 x mid, 4 x lo of the bias).
+__device__ __forceinline__ void issue_split_layer(uint32_t tmem, const uint32_t (&a)[3], const uint32_t (&w)[3],
+                                                  int np, uint32_t bias_slice, uint64_t ones8, int n, int ksteps) {
   const uint32_t id = idesc_bf16(n, false, false);
   for (int kk = 0; kk < ksteps; ++kk) {
-    const uint64_t ah = tc::sdesc_sw128(a_hi + 32 * kk), al = tc::sdesc_sw128(a_lo + 32 * kk);
-    const uint64_t wh = tc::sdesc_sw128(w_hi + 32 * kk), wl = tc::sdesc_sw128(w_lo + 32 * kk);
+    const uint64_t ah = tc::sdesc_sw128(a[0] + 32 * kk), am = tc::sdesc_sw128(a[1] + 32 * kk);
+    const uint64_t wh = tc::sdesc_sw128(w[0] + 32 * kk), wm = tc::sdesc_sw128(w[1] + 32 * kk);
     tc::mma_f16(tmem, ah, wh, id, kk > 0);
-    tc::mma_f16(tmem, al, wh, id, 1);
-    tc::mma_f16(tmem, ah, wl, id, 1);
+    tc::mma_f16(tmem, am, wh, id, 1);
+    tc::mma_f16(tmem, ah, wm, id, 1);
+    if (np == 3) {
+      tc::mma_f16(tmem, am, wm, id, 1);
+      tc::mma_f16(tmem, tc::sdesc_sw128(a[2] + 32 * kk), wh, id, 1);
+      tc::mma_f16(tmem, ah, tc::sdesc_sw128(w[2] + 32 * kk), id, 1);
+    }
   }
   tc::mma_f16(tmem, ones8, tc::sdesc_sw128(bias_slice), id, 1);
 }
 
 // ---------------------------------------------------------------------------
-// Forward: per-sample colour c = sigmoid(MLP(x)) on tcgen05.
+// Forward: per-sample colour c = sigmoid(MLP(x)) on tcgen05, three-part
+// split operands.  One CTA of NTH = 128 or 256 threads per SM (the part
+// tiles and the weight image take 130 KB of shared memory): the gather is
+// spread over all warps; warps w and w + 4 share tensor-memory lane quarter
+// w % 4 and split the accumulator columns in the epilogues.
+//
+// Accumulation.  The tensor core's FP32 accumulation is not a
+// round-to-nearest sum: chained into one accumulator over the 24 MMAs of a
+// layer, its error was biased and moved the loss gradient by ~0.5 %.  So
+// the products A_hi.W_hi of K step kk, the bulk of the value, go to an
+// accumulator of their own (columns 64 kk, a single MMA), the five smaller
+// terms of all K steps to the one at columns 64 ksteps (their error is
+// 2^-8 smaller), and the epilogue adds them and the FP32 bias on the CUDA
+// cores.
 // ---------------------------------------------------------------------------
-template <int F, int H, int L>
-__global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
+template <int NTH>
+int fwd_smem_bytes(const ImageLayout& lay) {
+  return 1024 + 3 * 16384 + (lay.total - lay.lo_off) + 2 * lay.hi_part + 64;
+}
+
+__device__ __forceinline__ void issue_fwd_layer(uint32_t tmem, const uint32_t (&a)[3], const uint32_t (&w)[3], int n,
+                                                int ksteps) {
+  const uint32_t id = idesc_bf16(n, false, false);
+  const uint32_t small = tmem + 64u * (uint32_t)ksteps;
+  for (int kk = 0; kk < ksteps; ++kk) {
+    const uint64_t ah = tc::sdesc_sw128(a[0] + 32 * kk), am = tc::sdesc_sw128(a[1] + 32 * kk);
+    const uint64_t al = tc::sdesc_sw128(a[2] + 32 * kk);
+    const uint64_t wh = tc::sdesc_sw128(w[0] + 32 * kk), wm = tc::sdesc_sw128(w[1] + 32 * kk);
+    const uint64_t wl = tc::sdesc_sw128(w[2] + 32 * kk);
+    tc::mma_f16(tmem + 64u * (uint32_t)kk, ah, wh, id, 0u);
+    tc::mma_f16(small, am, wh, id, kk > 0);
+    tc::mma_f16(small, ah, wm, id, 1u);
+    tc::mma_f16(small, am, wm, id, 1u);
+    tc::mma_f16(small, al, wh, id, 1u);
+    tc::mma_f16(small, ah, wl, id, 1u);
+  }
+}
+
+// columns [col, col + 16) of this thread's row: the sum of the KS
+// per-K-step accumulators, the small-term accumulator and the FP32 bias
+template <int KS>
+__device__ __forceinline__ void fwd_sum16(uint32_t taddr, int col, const float* bias, float (&x)[16]) {
+  float t[16];
+  tc::tmem_ld16(taddr + col, x);
+  tc::tmem_ld16(taddr + 64 * KS + col, t);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int kk = 1; kk < KS; ++kk) {
+    float u[16];
+    tc::tmem_ld16(taddr + 64 * kk + col, u);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] += u[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j) x[j] = (x[j] + t[j]) + bias[col + j];
+}
+
+// hidden-layer epilogue: ReLU of the summed accumulators, three-part split
+// into the A part tiles (columns [part H / NC, (part + 1) H / NC))
+template <int H, int NC, int KS>
+__device__ __forceinline__ void epi_fwd_hidden(uint32_t taddr, const float* bias, uint8_t* const (&dst)[3], int row,
+                                               int part) {
+  constexpr int CP = H / NC;
+  static_assert(CP % 16 == 0, "column parts of 16");
+#pragma unroll
+  for (int s0 = 0; s0 < CP; s0 += 16) {
+    const int col = part * CP + s0;
+    float x[16];
+    fwd_sum16<KS>(taddr, col, bias, x);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      uint32_t pv[3][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        split3_bf2(fmaxf(x[8 * q + 2 * j], 0.f), fmaxf(x[8 * q + 2 * j + 1], 0.f), pv[0][j], pv[1][j], pv[2][j]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        *reinterpret_cast<uint4*>(dst[k] + tc::sw128_offset(row, col / 8 + q)) =
+            make_uint4(pv[k][0], pv[k][1], pv[k][2], pv[k][3]);
+    }
+  }
+}
+
+template <int F, int H, int L, int NTH>
+__global__ void __launch_bounds__(NTH, 1) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
                                                         const TrainRecT* __restrict__ recs,
                                                         const int32_t* __restrict__ tstart,
                                                         const int32_t* __restrict__ coff, int* work,
                                                         const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
                                                         int img_stride, float4* cout) {
+  constexpr int NW = NTH / 32, NC = NTH / 128, KH = H / 16;
+  static_assert(NTH == 128 || NTH == 256, "one or two threads per accumulator row");
+  static_assert(64 * (4 > KH ? 4 : KH) + 64 <= 512, "accumulators fit tensor memory");
   const ImageLayout lay(H, L);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* Ahi = base;
-  uint8_t* Alo = base + 16384;
-  uint8_t* Wsm = base + 32768;
-  uint8_t* ones = Wsm + ((lay.fwd_bytes + 1023) & ~1023);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 1024);
+  uint8_t* const A[3] = {base, base + 16384, base + 32768};  // hi, mid, lo part tiles
+  uint8_t* Wsm = base + 49152;                              // image: hi, mid parts, then lo part, FP32 biases
+  const float* fbias = reinterpret_cast<const float*>(Wsm + 3 * lay.hi_part);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Wsm + 2 * lay.hi_part + (lay.total - lay.lo_off));
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = tid & 127, part = tid >> 7;
   const int NT = S.num_tiles;
   Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
   if (tid == 0) {
@@ -373,17 +506,13 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(tmem_slot), 64);
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
     tc::tmem_relinquish();
   }
-  for (int k = tid; k < 64; k += 128)
-    reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16Eighth, kBf16Eighth, kBf16Eighth, kBf16Eighth);
-  tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
-  const uint64_t ones8 = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
   const int total = coff[NT];
   int cur_tile = -1;
   bool failed = false;
@@ -396,11 +525,14 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
     const ChunkPos cp = chunk_pos(c, coff, tstart, NT);
     const bool new_w = cp.tile != cur_tile;
     if (new_w && tid == 0) {
-      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.fwd_bytes);
-      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.fwd_bytes, B.wbar);
+      const uint8_t* img = wimg + (size_t)cp.tile * img_stride;
+      const uint32_t tail = (uint32_t)(lay.total - lay.lo_off);
+      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)(2 * lay.hi_part) + tail);
+      tc::bulk_g2s(tc::smem_addr(Wsm), img, (uint32_t)(2 * lay.hi_part), B.wbar);
+      tc::bulk_g2s(tc::smem_addr(Wsm + 2 * lay.hi_part), img + lay.lo_off, tail, B.wbar);
     }
     cur_tile = cp.tile;
-    gather_x<F>(S, vfeat, recs, cp.row0, cp.cnt, enc, Ahi, Alo, warp, lane);
+    gather_x<F, NW, 3>(S, vfeat, recs, cp.row0, cp.cnt, enc, A, warp, lane);
     tc::fence_proxy_async();
     __syncthreads();
     if (new_w) {
@@ -408,34 +540,37 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
       B.wphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
     }
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    const uint32_t ahi = tc::smem_addr(Ahi), alo = tc::smem_addr(Alo), w = tc::smem_addr(Wsm);
+    const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint32_t w = tc::smem_addr(Wsm);
+    const uint32_t a3[3] = {tc::smem_addr(A[0]), tc::smem_addr(A[1]), tc::smem_addr(A[2])};
     float out3[3] = {0.f, 0.f, 0.f};
     for (int l = 0; l <= L; ++l) {
       if (tid == 0) {
         tc::fence_after_sync();
         const uint32_t wofs = (uint32_t)(l < L ? l * H * 128 : L * H * 128);
-        const uint32_t bias = l < L ? w + lay.bias_off + 32 * l : w + lay.obias_off;
-        issue_split_layer(tmem, ahi, alo, w + wofs, w + lay.lo_off + wofs, bias, ones8, l < L ? H : 16,
-                          l == 0 ? 4 : H / 16);
+        const uint32_t w3[3] = {w + wofs, w + lay.hi_part + wofs, w + 2 * lay.hi_part + wofs};
+        issue_fwd_layer(tmem, a3, w3, l < L ? H : 16, l == 0 ? 4 : KH);
         tc::mma_commit(B.mbar);
       }
       if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
       if (l < L) {
-        epi_relu_split<H>(taddr, Ahi, Alo, tid);  // the output layer also takes split inputs
+        // the output layer also takes split inputs
+        if (l == 0)
+          epi_fwd_hidden<H, NC, 4>(taddr, fbias, A, row, part);
+        else
+          epi_fwd_hidden<H, NC, KH>(taddr, fbias + 64 * l, A, row, part);
         tc::fence_proxy_async();
       } else {
-        float v[4];
-        tc::tmem_ld4(taddr, v);
-        tc::tmem_wait_ld();
-        out3[0] = v[0]; out3[1] = v[1]; out3[2] = v[2];
+        float x[16];
+        fwd_sum16<KH>(taddr, 0, fbias + 64 * L, x);
+        out3[0] = x[0]; out3[1] = x[1]; out3[2] = x[2];
       }
       tc::fence_before_sync();
       __syncthreads();
     }
     if (failed) break;
-    if (tid < cp.cnt)
-      cout[cp.row0 + tid] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
+    if (part == 0 && row < cp.cnt)
+      cout[cp.row0 + row] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
   }
   bool drained = true;
   if (failed && tid == 0) {
@@ -445,7 +580,7 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when in-flight work did not drain
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -456,7 +591,8 @@ __global__ void __launch_bounds__(128, 2) tr_mlp_fwd_tc(SceneDev S, const float*
 //
 // Shared memory tiles (16 KB, one sample per 128-byte row), in this order:
 //   D (hidden delta), X (input hi), H1..HL (activation hi), DO (output-logit
-//   gradient), LoA, LoB (lo halves during the recomputation, ping-pong).
+//   gradient), MidA, MidB (the mid parts of the recomputation's two-part
+//   split operands, ping-pong).
 // An MN-major M = 128 operand spans two 64-wide atoms 16 KB apart: for D and
 // DO the second atom is the next tile, whose products land in accumulator
 // lanes 64..127 (output units that do not exist) and are never read.
@@ -508,10 +644,10 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   uint8_t* Xt = base + 16384;
   uint8_t* Ht = base + 2 * 16384;  // H_l at Ht + (l-1)*16384, l = 1..L
   uint8_t* DOt = base + (2 + L) * 16384;
-  uint8_t* LoA = DOt + 16384;
-  uint8_t* LoB = LoA + 16384;
+  uint8_t* MidA = DOt + 16384;
+  uint8_t* MidB = MidA + 16384;
   uint8_t* Wsm = base + kTiles * 16384;
-  uint8_t* ones = Wsm + ((lay.total + 1023) & ~1023);  // 1 KB of 1/8, 1 KB of 1.0
+  uint8_t* ones = Wsm + ((lay.bwd_bytes + 1023) & ~1023);  // 1 KB bias-step A operand, 1 KB of 1.0
   uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 2048);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
@@ -530,10 +666,9 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
     tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
     tc::tmem_relinquish();
   }
-  for (int k = tid; k < 64; k += 256) {
-    reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16Eighth, kBf16Eighth, kBf16Eighth, kBf16Eighth);
+  init_bias_ones(ones, tid, 256);
+  for (int k = tid; k < 64; k += 256)
     reinterpret_cast<uint4*>(ones + 1024)[k] = make_uint4(kBf16One, kBf16One, kBf16One, kBf16One);
-  }
   // all tiles start zeroed: DO columns beyond 3 and the columns beyond H of
   // the activation / delta tiles are never written afterwards
   for (int k = tid; k < kTiles * 16384 / 16; k += 256) reinterpret_cast<uint4*>(base)[k] = make_uint4(0, 0, 0, 0);
@@ -608,8 +743,8 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       __syncthreads();
     }
     if (new_w && tid == 0) {
-      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.total);
-      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.total, B.wbar);
+      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.bwd_bytes);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.bwd_bytes, B.wbar);
     }
     const bool first_of_tile = new_w;
     cur_tile = cp.tile;
@@ -627,7 +762,10 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       my_fr = __ldg(src + 1);
       my_cn = __ldg(reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8) + part);
     }
-    gather_x<F, 8>(S, vfeat, recs, cp.row0, cp.cnt, enc, Xt, LoA, warp, lane);
+    {
+      uint8_t* const X2[2] = {Xt, MidA};
+      gather_x<F, 8, 2>(S, vfeat, recs, cp.row0, cp.cnt, enc, X2, warp, lane);
+    }
     // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
     if (part == 0)
       *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(row, 0)) =
@@ -640,20 +778,21 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
     }
     const uint32_t w = tc::smem_addr(Wsm);
-    // forward recomputation of the hidden activations H1..HL (split operands;
-    // the lo halves alternate between LoA and LoB)
+    // forward recomputation of the hidden activations H1..HL (two-part split
+    // operands; the mid parts alternate between MidA and MidB)
     for (int l = 0; l < L; ++l) {
-      uint8_t* lo_in = (l & 1) ? LoB : LoA;
-      uint8_t* lo_out = (l & 1) ? LoA : LoB;
+      uint8_t* mid_in = (l & 1) ? MidB : MidA;
+      uint8_t* mid_out = (l & 1) ? MidA : MidB;
       if (tid == 0) {
         tc::fence_after_sync();
-        issue_split_layer(tw, tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(lo_in),
-                          w + l * H * 128, w + lay.lo_off + l * H * 128, w + lay.bias_off + 32 * l, ones8, H,
-                          l == 0 ? 4 : H / 16);
+        const uint32_t a2[3] = {tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(mid_in), 0u};
+        const uint32_t w2[3] = {w + l * H * 128, w + lay.mid_off + l * H * 128, 0u};
+        issue_split_layer(tw, a2, w2, 2, w + lay.bias_off + 32 * l, ones8, H, l == 0 ? 4 : H / 16);
         tc::mma_commit(B.mbar);
       }
       if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
-      epi_relu_split_part<H, 2>(taddr, Ht + l * 16384, l + 1 < L ? lo_out : nullptr, row, part);
+      uint8_t* const dst[2] = {Ht + l * 16384, l + 1 < L ? mid_out : nullptr};
+      epi_relu_split<H, 2, 2>(taddr, dst, row, part);
       tc::fence_proxy_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -757,7 +896,7 @@ int train_tc_image_bytes(int H, int L) { return ImageLayout(H, L).total; }
 
 // dynamic shared memory of the backward kernel (checked against the 227 KB limit)
 int train_tc_bwd_smem_bytes(int H, int L) {
-  return 1024 + 16384 * (5 + L) + ((ImageLayout(H, L).total + 1023) & ~1023) + 2048 + 64;
+  return 1024 + 16384 * (5 + L) + ((ImageLayout(H, L).bwd_bytes + 1023) & ~1023) + 2048 + 64;
 }
 
 template <int F, int H, int L>
@@ -778,16 +917,19 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
   e = cudaMemsetAsync(a.work, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   if (!backward) {
-    const int smem = 1024 + 32768 + ((lay.fwd_bytes + 1023) & ~1023) + 1024 + 64;
+    // one CTA per SM of 4 or 8 warps
+    const int smem = fwd_smem_bytes<128>(lay);
+    auto kern = a.fwd_warps == 4 ? tr_mlp_fwd_tc<F, H, L, 128> : tr_mlp_fwd_tc<F, H, L, 256>;
     static unsigned long long cfg = 0;
     e = once_per_device(&cfg, [&]() {
-      return cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      cudaError_t r = cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           smem);
+      if (r != cudaSuccess) return r;
+      return cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     });
     if (e != cudaSuccess) return e;
-    // up to two CTAs per SM (shared memory and 2 x 64 tensor-memory columns allow it)
-    const int per_sm = a.fwd_ctas_per_sm == 1 ? 1 : 2;
-    tr_mlp_fwd_tc<F, H, L><<<per_sm * a.num_sms, 128, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
-                                                             a.work, a.enc, a.wimg, a.img_stride, a.cout);
+    kern<<<a.num_sms, a.fwd_warps == 4 ? 128 : 256, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart,
+                                                                 a.coff, a.work, a.enc, a.wimg, a.img_stride, a.cout);
   } else {
     const int smem = train_tc_bwd_smem_bytes(H, L);
     static unsigned long long cfg = 0;

@@ -76,7 +76,7 @@ class Camera(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [
         ("traverse_threads", C.c_int32), ("scatter_blocks_per_sm", C.c_int32), ("mlp_ctas_per_sm", C.c_int32),
-        ("train_march_threads", C.c_int32), ("train_fwd_ctas_per_sm", C.c_int32),
+        ("train_march_threads", C.c_int32), ("train_fwd_warps", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

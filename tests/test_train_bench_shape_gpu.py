@@ -7,10 +7,12 @@ benchmark reports.
 
 Checked against, per parameter group (features, density logits, MLP):
 * the exact FP64 oracle adjoint: relative error <= 1e-2 for the tensor-core
-  form (split BF16 forward operands, BF16 backward operands), <= 1e-3 for the
-  plain FP32 form; forward colour RMSE <= 1e-3 (TC), max-abs <= 1e-5 (plain);
+  form (three-part split BF16 forward operands, BF16 backward operands),
+  <= 1e-3 for the plain FP32 form; forward colour max-abs <= 1e-5 (both);
+* the same under the benchmark's own MSE loss, where each form's colour
+  errors enter its loss residuals (small near convergence);
 * the oracle's emulation of the tensor-core operand rounding: colours
-  max-abs <= 1e-4, gradients relative <= 2e-3 (the kernels are exact up to
+  max-abs <= 1e-5, gradients relative <= 2e-3 (the kernels are exact up to
   FP32 summation order);
 * autograd of the reference-style graph (grid_sample lookup, Linear/ReLU MLP,
   cumprod compositing; tests/reference_graph.py), float64 on the CPU;
@@ -110,15 +112,40 @@ def test_bench_shape_against_fp64_oracle(tile, form, dens):
         assert np.abs(rgb - ref[0]).max() <= 1e-5
         assert max(errs) <= 1e-3
     else:
-        assert rmse <= 1e-3
+        assert np.abs(rgb - ref[0]).max() <= 1e-5
         assert max(errs) <= 1e-2
         emu = _oracle(P, dens, vd, "tc")
         eerr = (_rel(gF, emu[2]), _rel(gG, emu[3]), _rel(gW, emu[4]))
         print(f"   against the tensor-core emulation: colour max-abs {np.abs(rgb - emu[0]).max():.2e}, gradients "
               f"({eerr[0]:.2e}, {eerr[1]:.2e}, {eerr[2]:.2e})")
-        assert np.abs(rgb - emu[0]).max() <= 1e-4
+        assert np.abs(rgb - emu[0]).max() <= 1e-5
         assert max(eerr) <= 2e-3
     P["cache"][(form, dens)] = (gF, gG, gW)
+
+
+@pytest.mark.parametrize("form,tol", [(snisr.FORM_PLAIN_FP32, 1e-3), (snisr.FORM_TC, 1e-2)])
+def test_bench_shape_own_mse_loss(tile, form, tol):
+    """Each form differentiates its own MSE loss against a target rendered
+    from features + N(0, 0.02), the benchmark's loss: the form's colour
+    errors enter the residuals, which are small (RMS ~1e-3), so a biased
+    colour error moves the gradients far more than under a fixed dL/dC.
+    Reference: the FP64 adjoint of the FP64 loss."""
+    import torch
+    P, T = tile, tile["T"]
+    vd = P["vd"]
+    rng = np.random.default_rng(7)
+    vf_t = (P["vf"] + rng.normal(0, 0.02, P["vf"].shape)).astype(np.float32)
+    target, _ = P["osc"].train_forward(vf_t, vd, P["W"], P["o"], P["d"], P["rt"])
+    rgb64 = _oracle(P, "synthetic", vd, None)[0]
+    ref = P["osc"].train_backward(P["vf"], vd, P["W"], P["o"], P["d"], P["rt"], 2 * (rgb64 - target))
+    leaves = [T(x).requires_grad_(True) for x in (P["vf"], vd, P["W"])]
+    rgb = tile_field(*leaves, P["sc"], T(P["o"]), T(P["d"]), T(P["rt"]), form)
+    ((rgb - torch.from_numpy(target).float().cuda()) ** 2).sum().backward()
+    P["sc"].check()
+    errs = [_rel(x.grad.cpu().numpy(), y) for x, y in zip(leaves, ref)]
+    print(f"form {form}: residual RMS {np.sqrt(((rgb64 - target) ** 2).mean()):.2e}; own-loss gradient relative "
+          f"errors vs FP64 {['%.2e' % e for e in errs]}")
+    assert max(errs) <= tol
 
 
 @pytest.mark.parametrize("form,tol", [(snisr.FORM_PLAIN_FP32, 1e-3), (snisr.FORM_TC, 1e-2)])

@@ -59,8 +59,8 @@ def test_training_independent_of_launch_shapes(cfg1):
         return [x.grad for x in leaves]
 
     ref = grads()
-    for march, fwd in ((64, 1), (256, 2), (160, 1)):
-        sc.set_tuning(train_march_threads=march, train_fwd_ctas_per_sm=fwd)
+    for march, fwd in ((64, 4), (256, 8), (160, 4)):
+        sc.set_tuning(train_march_threads=march, train_fwd_warps=fwd)
         for x, r in zip(grads(), ref):
             assert float((x - r).norm() / r.norm()) <= 1e-5
     sc.set_tuning(**default)
@@ -69,7 +69,7 @@ def test_training_independent_of_launch_shapes(cfg1):
 def test_bad_tuning_rejected(cfg1):
     _, sc = cfg1
     for bad in (dict(traverse_threads=48), dict(traverse_threads=512), dict(scatter_blocks_per_sm=0),
-                dict(mlp_ctas_per_sm=9), dict(train_fwd_ctas_per_sm=3)):
+                dict(mlp_ctas_per_sm=9), dict(train_fwd_warps=6)):
         with pytest.raises(snisr.SnisrError):
             sc.set_tuning(**bad)
 
@@ -90,4 +90,4 @@ def test_autotune_render_and_train(cfg1):
                                                        a["mlp_params"].copy()))
     cfg2, ms2 = sc.autotune_train(vf, vd, W, o, d, rt, reps=2)
     assert ms2 > 0 and cfg2 == sc.tuning()
-    assert cfg2["train_march_threads"] in (64, 128, 256) and cfg2["train_fwd_ctas_per_sm"] in (1, 2)
+    assert cfg2["train_march_threads"] in (64, 128, 256) and cfg2["train_fwd_warps"] in (4, 8)
