@@ -103,7 +103,8 @@ struct TrainTcArgs {
 };
 int train_tc_image_bytes(int H, int L);
 int train_tc_bwd_smem_bytes(int H, int L);
-// enc: [n][8] uint4 (BF16 hi / lo view encoding)
+// enc: [n][12] uint4 (BF16 hi / mid / lo view encoding); coff: [2][NT + 2]
+// chunk offsets per tile (128-row chunks, then 256-row units)
 cudaError_t launch_train_tc(const SceneDev& S, const TrainTcArgs& a, bool backward, cudaStream_t st);
 
 // distinct voxels / vertices read by the last batched frame -> counts[0], counts[1]

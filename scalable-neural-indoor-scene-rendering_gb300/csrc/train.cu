@@ -536,7 +536,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const int img_stride = (train_tc_image_bytes(64, 3) + 127) & ~127;
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
-              al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al((NT + 2) * 4) + al(16) +
+              al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al(2 * (NT + 2) * 4) + al(16) +
               al(rays * 192) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
               al((size_t)nvox * 32) + al((size_t)NT * 4 * (64 * 64 + 64) * 4);
   void* p = nullptr;
@@ -554,7 +554,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   T->dout = (float4*)take(cap * 16);
   T->act = (float*)take(cap * kActStride * 4);
   T->dlt = (float*)take(cap * kDltStride * 4);
-  T->coff = (int32_t*)take((NT + 2) * 4);
+  T->coff = (int32_t*)take(2 * (NT + 2) * 4);  // chunk offsets per tile: 128-row chunks, then 256-row units
   T->work = (int*)take(16);
   T->enc = (uint4*)take(rays * 192);  // 12 uint4 per ray: BF16 hi, mid, lo of the view encoding
   T->wimg = (uint8_t*)take((size_t)img_stride * NT);

@@ -187,21 +187,27 @@ __device__ __forceinline__ void init_bias_ones(uint8_t* ones, int tid, int nth) 
   }
 }
 
-// chunk lists: chunks of 128 samples never straddle tiles
-__global__ void train_chunks_kernel(const int32_t* __restrict__ tstart, int NT, int32_t* coff) {
+// chunk lists: chunks of 128 samples (coff) and units of 256 samples (coff2)
+// never straddle tiles
+__global__ void train_chunks_kernel(const int32_t* __restrict__ tstart, int NT, int32_t* coff, int32_t* coff2) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int c = 0;
+  int c = 0, c2 = 0;
   for (int t = 0; t < NT; ++t) {
     coff[t] = c;
+    coff2[t] = c2;
     c += (tstart[t + 1] - tstart[t] + 127) / 128;
+    c2 += (tstart[t + 1] - tstart[t] + 255) / 256;
   }
   coff[NT] = c;
+  coff2[NT] = c2;
 }
 
 struct ChunkPos {
   int tile, row0, cnt;
 };
-__device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const int32_t* tstart, int NT) {
+// chunk c of the lists coff of `rows`-row chunks: its tile, first row and row count
+__device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const int32_t* tstart, int NT,
+                                              int rows = 128) {
   int lo = 0, hi = NT;
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
@@ -209,8 +215,8 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
   }
   ChunkPos p;
   p.tile = lo;
-  p.row0 = __ldg(tstart + lo) + (c - __ldg(coff + lo)) * 128;
-  p.cnt = min(128, __ldg(tstart + lo + 1) - p.row0);
+  p.row0 = __ldg(tstart + lo) + (c - __ldg(coff + lo)) * rows;
+  p.cnt = min(rows, __ldg(tstart + lo + 1) - p.row0);
   return p;
 }
 
@@ -220,11 +226,16 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
 // the per-ray split table.  Loads are issued in stages across the lane's rows
 // (records, then corner ids and encodings, then features) so that each stage
 // waits for memory once, not once per row.
+template <int NP>
+struct PartTiles {
+  uint8_t* p[NP];
+};
+
 template <int F, int NW, int NP>
 __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restrict__ vfeat,
                                          const TrainRecT* __restrict__ recs, int row0, int cnt,
-                                         const uint4* __restrict__ enc, uint8_t* const (&X)[NP], int warp,
-                                         int lane) {
+                                         const uint4* __restrict__ enc, PartTiles<NP> Xt, int warp, int lane) {
+  uint8_t* const* X = Xt.p;
   // NW warps share the 128 rows: RPW rows per warp, RPI rows per lane pass
   constexpr int G = F / 8, RPI = 32 / G, RPW = 128 / NW, ITS = RPW / RPI;
   static_assert(RPW % RPI == 0, "rows per warp must be a multiple of rows per pass");
@@ -320,38 +331,27 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
   }
 }
 
-// ReLU + split BF16 pack of one of NC column parts of a 128 x H accumulator
-// (H / NC columns, a multiple of 16; part p covers [p H / NC, (p + 1) H / NC))
-// into the NP part tiles dst[0..NP) (hi, mid, lo); a null dst[q], q > 0,
-// skips that part.
-template <int H, int NC, int NP>
-__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* const (&dst)[NP], int row, int part) {
-  constexpr int CP = H / NC, SUB = CP < 32 ? CP : 32;
-  static_assert(CP % 16 == 0 && CP % SUB == 0, "column parts of 16");
+// ReLU + two-part split BF16 pack of one of NC column parts of a 128 x H
+// accumulator (H / NC columns, a multiple of 16; part p covers
+// [p H / NC, (p + 1) H / NC)) into the hi and mid activation tiles (dst_mid
+// may be null: hi only)
+template <int H, int NC>
+__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_mid, int row, int part) {
+  constexpr int CP = H / NC;
+  static_assert(CP % 16 == 0, "column parts of 16");
+  float v[CP];
 #pragma unroll
-  for (int s0 = 0; s0 < CP; s0 += SUB) {
-    float v[SUB];
+  for (int j = 0; j < CP; j += 16) tc::tmem_ld16(taddr + part * CP + j, v + j);
+  tc::tmem_wait_ld();
 #pragma unroll
-    for (int j = 0; j < SUB; j += 16) tc::tmem_ld16(taddr + part * CP + s0 + j, v + j);
-    tc::tmem_wait_ld();
+  for (int q = 0; q < CP / 8; ++q) {
+    const int chunk = part * (CP / 8) + q;
+    uint32_t h[4], m[4];
 #pragma unroll
-    for (int q = 0; q < SUB / 8; ++q) {
-      const int chunk = (part * CP + s0) / 8 + q;
-      uint32_t pv[3][4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float a0 = fmaxf(v[8 * q + 2 * j], 0.f), a1 = fmaxf(v[8 * q + 2 * j + 1], 0.f);
-        if (NP == 3)
-          split3_bf2(a0, a1, pv[0][j], pv[1][j], pv[2][j]);
-        else
-          split_bf2(a0, a1, pv[0][j], pv[1][j]);
-      }
-#pragma unroll
-      for (int k = 0; k < NP; ++k)
-        if (k == 0 || dst[k])
-          *reinterpret_cast<uint4*>(dst[k] + tc::sw128_offset(row, chunk)) =
-              make_uint4(pv[k][0], pv[k][1], pv[k][2], pv[k][3]);
-    }
+    for (int j = 0; j < 4; ++j)
+      split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], m[j]);
+    *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, chunk)) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (dst_mid) *reinterpret_cast<uint4*>(dst_mid + tc::sw128_offset(row, chunk)) = make_uint4(m[0], m[1], m[2], m[3]);
   }
 }
 
@@ -368,101 +368,90 @@ __device__ __forceinline__ bool wait_mma(Bars& b, int tid) {
   return ok;
 }
 
-// One split-precision forward layer: tmem = A.W^T + bias with N = n outputs,
-// K = 16 * ksteps; a[q] / w[q] are the shared-memory part tiles (hi, mid,
-// lo) of the activations and the weights.  np = 2: A_hi.W_hi + A_mid.W_hi +
-// A_hi.W_mid; np = 3 adds A_mid.W_mid + A_lo.W_hi + A_hi.W_lo.  Then the
-// bias step (A = 1/8 in K columns 0..7 and 1/4 in 8..15, B slice = 8 x hi,
-// 4 x mid, 4 x lo of the bias).
-__device__ __forceinline__ void issue_split_layer(uint32_t tmem, const uint32_t (&a)[3], const uint32_t (&w)[3],
-                                                  int np, uint32_t bias_slice, uint64_t ones8, int n, int ksteps) {
+// One two-part split layer of the backward's recomputation: tmem = A.W^T +
+// bias with N = n outputs, K = 16 * ksteps: A_hi.W_hi + A_mid.W_hi +
+// A_hi.W_mid, then the bias step (A = 1/8 in K columns 0..7 and 1/4 in
+// 8..15, B slice = 8 x hi, 4 x mid, 4 x lo of the bias).
+__device__ __forceinline__ void issue_split_layer(uint32_t tmem, uint32_t a_hi, uint32_t a_mid, uint32_t w_hi,
+                                                  uint32_t w_mid, uint32_t bias_slice, uint64_t ones8, int n,
+                                                  int ksteps) {
   const uint32_t id = idesc_bf16(n, false, false);
   for (int kk = 0; kk < ksteps; ++kk) {
-    const uint64_t ah = tc::sdesc_sw128(a[0] + 32 * kk), am = tc::sdesc_sw128(a[1] + 32 * kk);
-    const uint64_t wh = tc::sdesc_sw128(w[0] + 32 * kk), wm = tc::sdesc_sw128(w[1] + 32 * kk);
+    const uint64_t ah = tc::sdesc_sw128(a_hi + 32 * kk), am = tc::sdesc_sw128(a_mid + 32 * kk);
+    const uint64_t wh = tc::sdesc_sw128(w_hi + 32 * kk), wm = tc::sdesc_sw128(w_mid + 32 * kk);
     tc::mma_f16(tmem, ah, wh, id, kk > 0);
     tc::mma_f16(tmem, am, wh, id, 1);
     tc::mma_f16(tmem, ah, wm, id, 1);
-    if (np == 3) {
-      tc::mma_f16(tmem, am, wm, id, 1);
-      tc::mma_f16(tmem, tc::sdesc_sw128(a[2] + 32 * kk), wh, id, 1);
-      tc::mma_f16(tmem, ah, tc::sdesc_sw128(w[2] + 32 * kk), id, 1);
-    }
   }
   tc::mma_f16(tmem, ones8, tc::sdesc_sw128(bias_slice), id, 1);
 }
 
 // ---------------------------------------------------------------------------
 // Forward: per-sample colour c = sigmoid(MLP(x)) on tcgen05, three-part
-// split operands.  One CTA of NTH = 128 or 256 threads per SM (the part
-// tiles and the weight image take 130 KB of shared memory): the gather is
-// spread over all warps; warps w and w + 4 share tensor-memory lane quarter
-// w % 4 and split the accumulator columns in the epilogues.
+// split operands.  One CTA per SM of NG groups of 4 warps: a work unit is
+// NG x 128 rows of one tile, group g gathers, and runs the epilogues of,
+// rows [128 g, 128 g + 128) with its own part tiles and tensor-memory
+// accumulators; the weight image (hi, mid, lo parts, FP32 biases) is shared.
+// Within a unit the groups run their layer chains apart: each has its own
+// MMA issuer (its first thread), mbarrier and named barrier, so that one
+// group's epilogue overlaps the other group's MMAs.
 //
 // Accumulation.  The tensor core's FP32 accumulation is not a
 // round-to-nearest sum: chained into one accumulator over the 24 MMAs of a
 // layer, its error was biased and moved the loss gradient by ~0.5 %.  So
-// the products A_hi.W_hi of K step kk, the bulk of the value, go to an
-// accumulator of their own (columns 64 kk, a single MMA), the five smaller
-// terms of all K steps to the one at columns 64 ksteps (their error is
-// 2^-8 smaller), and the epilogue adds them and the FP32 bias on the CUDA
-// cores.
+// the products A_hi.W_hi, the bulk of the value, go to two accumulators of
+// their own (K steps [0, ks/2) and [ks/2, ks), two MMAs each), the five
+// smaller terms of all K steps to a third (their error is 2^-8 smaller),
+// and the epilogue adds them and the FP32 bias on the CUDA cores.  Per
+// group, 3 x 64 tensor-memory columns at 256 g.
 // ---------------------------------------------------------------------------
-template <int NTH>
-int fwd_smem_bytes(const ImageLayout& lay) {
-  return 1024 + 3 * 16384 + (lay.total - lay.lo_off) + 2 * lay.hi_part + 64;
+constexpr int kFwdTileBytes = 3 * 16384;  // hi, mid, lo part tiles of one group
+
+int fwd_smem_bytes(const ImageLayout& lay, int ng) {
+  return 1024 + ng * kFwdTileBytes + (lay.total - lay.lo_off) + 2 * lay.hi_part + 64;  // + 3 mbarriers, slots
 }
 
-__device__ __forceinline__ void issue_fwd_layer(uint32_t tmem, const uint32_t (&a)[3], const uint32_t (&w)[3], int n,
+// one layer's MMAs for one group: acc + 0 / acc + 64 = the hi.hi products of
+// the first / second half of the K steps, acc + 128 = the smaller terms
+__device__ __forceinline__ void issue_fwd_layer(uint32_t acc, const uint32_t (&a)[3], const uint32_t (&w)[3], int n,
                                                 int ksteps) {
   const uint32_t id = idesc_bf16(n, false, false);
-  const uint32_t small = tmem + 64u * (uint32_t)ksteps;
+  const int half = ksteps / 2;
   for (int kk = 0; kk < ksteps; ++kk) {
     const uint64_t ah = tc::sdesc_sw128(a[0] + 32 * kk), am = tc::sdesc_sw128(a[1] + 32 * kk);
     const uint64_t al = tc::sdesc_sw128(a[2] + 32 * kk);
     const uint64_t wh = tc::sdesc_sw128(w[0] + 32 * kk), wm = tc::sdesc_sw128(w[1] + 32 * kk);
     const uint64_t wl = tc::sdesc_sw128(w[2] + 32 * kk);
-    tc::mma_f16(tmem + 64u * (uint32_t)kk, ah, wh, id, 0u);
-    tc::mma_f16(small, am, wh, id, kk > 0);
-    tc::mma_f16(small, ah, wm, id, 1u);
-    tc::mma_f16(small, am, wm, id, 1u);
-    tc::mma_f16(small, al, wh, id, 1u);
-    tc::mma_f16(small, ah, wl, id, 1u);
+    tc::mma_f16(acc + 64u * (uint32_t)(kk / half), ah, wh, id, kk % half != 0);
+    tc::mma_f16(acc + 128u, am, wh, id, kk > 0);
+    tc::mma_f16(acc + 128u, ah, wm, id, 1u);
+    tc::mma_f16(acc + 128u, am, wm, id, 1u);
+    tc::mma_f16(acc + 128u, al, wh, id, 1u);
+    tc::mma_f16(acc + 128u, ah, wl, id, 1u);
   }
 }
 
-// columns [col, col + 16) of this thread's row: the sum of the KS
-// per-K-step accumulators, the small-term accumulator and the FP32 bias
-template <int KS>
+// columns [col, col + 16) of this thread's row: the two hi.hi accumulators,
+// the small-term accumulator and the FP32 bias, summed
 __device__ __forceinline__ void fwd_sum16(uint32_t taddr, int col, const float* bias, float (&x)[16]) {
-  float t[16];
+  float u[16], t[16];
   tc::tmem_ld16(taddr + col, x);
-  tc::tmem_ld16(taddr + 64 * KS + col, t);
+  tc::tmem_ld16(taddr + 64 + col, u);
+  tc::tmem_ld16(taddr + 128 + col, t);
   tc::tmem_wait_ld();
 #pragma unroll
-  for (int kk = 1; kk < KS; ++kk) {
-    float u[16];
-    tc::tmem_ld16(taddr + 64 * kk + col, u);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int j = 0; j < 16; ++j) x[j] += u[j];
-  }
-#pragma unroll
-  for (int j = 0; j < 16; ++j) x[j] = (x[j] + t[j]) + bias[col + j];
+  for (int j = 0; j < 16; ++j) x[j] = ((x[j] + u[j]) + t[j]) + bias[col + j];
 }
 
 // hidden-layer epilogue: ReLU of the summed accumulators, three-part split
-// into the A part tiles (columns [part H / NC, (part + 1) H / NC))
-template <int H, int NC, int KS>
-__device__ __forceinline__ void epi_fwd_hidden(uint32_t taddr, const float* bias, uint8_t* const (&dst)[3], int row,
-                                               int part) {
-  constexpr int CP = H / NC;
-  static_assert(CP % 16 == 0, "column parts of 16");
+// into the group's part tiles
+template <int H>
+__device__ __forceinline__ void epi_fwd_hidden(uint32_t taddr, const float* bias, uint8_t* const (&dst)[3],
+                                               int row) {
 #pragma unroll
-  for (int s0 = 0; s0 < CP; s0 += 16) {
-    const int col = part * CP + s0;
+  for (int col = 0; col < H; col += 16) {
     float x[16];
-    fwd_sum16<KS>(taddr, col, bias, x);
+    fwd_sum16(taddr, col, bias, x);
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       uint32_t pv[3][4];
@@ -477,110 +466,131 @@ __device__ __forceinline__ void epi_fwd_hidden(uint32_t taddr, const float* bias
   }
 }
 
-template <int F, int H, int L, int NTH>
-__global__ void __launch_bounds__(NTH, 1) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
-                                                        const TrainRecT* __restrict__ recs,
-                                                        const int32_t* __restrict__ tstart,
-                                                        const int32_t* __restrict__ coff, int* work,
-                                                        const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
-                                                        int img_stride, float4* cout) {
-  constexpr int NW = NTH / 32, NC = NTH / 128, KH = H / 16;
-  static_assert(NTH == 128 || NTH == 256, "one or two threads per accumulator row");
-  static_assert(64 * (4 > KH ? 4 : KH) + 64 <= 512, "accumulators fit tensor memory");
+template <int F, int H, int L, int NG>
+__global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
+                                                             const TrainRecT* __restrict__ recs,
+                                                             const int32_t* __restrict__ tstart,
+                                                             const int32_t* __restrict__ uoff, int* work,
+                                                             const uint4* __restrict__ enc,
+                                                             const uint8_t* __restrict__ wimg, int img_stride,
+                                                             float4* cout) {
+  constexpr int KH = H / 16, NTMEM = NG == 1 ? 256 : 512;
+  static_assert(NG == 1 || NG == 2, "one or two groups");
+  static_assert(KH % 2 == 0 && H <= 64, "two hi.hi accumulators of up to 64 columns");
   const ImageLayout lay(H, L);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* const A[3] = {base, base + 16384, base + 32768};  // hi, mid, lo part tiles
-  uint8_t* Wsm = base + 49152;                              // image: hi, mid parts, then lo part, FP32 biases
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int grp = warp >> 2, gw = warp & 3, row = tid & 127;
+  const int leader = 128 * grp;  // the group's MMA issuer
+  const uint32_t gbar = 1u + (uint32_t)grp;
+  uint8_t* gbase = base + grp * kFwdTileBytes;
+  uint8_t* const A[3] = {gbase, gbase + 16384, gbase + 32768};  // this group's hi, mid, lo part tiles
+  uint8_t* Wsm = base + NG * kFwdTileBytes;                    // image: hi, mid parts, then lo part, FP32 biases
   const float* fbias = reinterpret_cast<const float*>(Wsm + 3 * lay.hi_part);
   uint64_t* bars = reinterpret_cast<uint64_t*>(Wsm + 2 * lay.hi_part + (lay.total - lay.lo_off));
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
-  int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int row = tid & 127, part = tid >> 7;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
+  int* unit_slot = reinterpret_cast<int*>(tmem_slot + 1);
   const int NT = S.num_tiles;
-  Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
+  const uint32_t wbar = tc::smem_addr(bars), mbar = tc::smem_addr(bars + 1 + grp);
+  uint32_t wphase = 0, mphase = 0;
   if (tid == 0) {
-    tc::mbar_init(B.wbar, 1);
-    tc::mbar_init(B.mbar, 1);
+    tc::mbar_init(wbar, 1);
+    for (int g = 0; g < NG; ++g) tc::mbar_init(tc::smem_addr(bars + 1 + g), 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), NTMEM);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
-  const int total = coff[NT];
+  const uint32_t gacc = tmem + 256u * (uint32_t)grp;  // the group's accumulators
+  const uint32_t taddr = gacc + ((uint32_t)(gw * 32) << 16);  // this thread's row (lane quarter gw)
+  const uint32_t a3[3] = {tc::smem_addr(A[0]), tc::smem_addr(A[1]), tc::smem_addr(A[2])};
+  const int total = uoff[NT];
   int cur_tile = -1;
   bool failed = false;
-  tc::Drain drain;
+  tc::Drain drain;  // on the group leaders: in-flight weight copy or MMAs at a timeout
   for (;;) {
-    if (tid == 0) *chunk_slot = atomicAdd(work, 1);
+    if (tid == 0) *unit_slot = atomicAdd(work, 1);
     __syncthreads();
-    const int c = *chunk_slot;
+    const int c = *unit_slot;
     if (c >= total) break;
-    const ChunkPos cp = chunk_pos(c, coff, tstart, NT);
+    const ChunkPos cp = chunk_pos(c, uoff, tstart, NT, 128 * NG);
+    const int my_cnt = min(128, cp.cnt - 128 * grp);  // rows of this group (uniform per group)
     const bool new_w = cp.tile != cur_tile;
     if (new_w && tid == 0) {
       const uint8_t* img = wimg + (size_t)cp.tile * img_stride;
       const uint32_t tail = (uint32_t)(lay.total - lay.lo_off);
-      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)(2 * lay.hi_part) + tail);
-      tc::bulk_g2s(tc::smem_addr(Wsm), img, (uint32_t)(2 * lay.hi_part), B.wbar);
-      tc::bulk_g2s(tc::smem_addr(Wsm + 2 * lay.hi_part), img + lay.lo_off, tail, B.wbar);
+      tc::mbar_arrive_expect_tx(wbar, (uint32_t)(2 * lay.hi_part) + tail);
+      tc::bulk_g2s(tc::smem_addr(Wsm), img, (uint32_t)(2 * lay.hi_part), wbar);
+      tc::bulk_g2s(tc::smem_addr(Wsm + 2 * lay.hi_part), img + lay.lo_off, tail, wbar);
     }
     cur_tile = cp.tile;
-    gather_x<F, NW, 3>(S, vfeat, recs, cp.row0, cp.cnt, enc, A, warp, lane);
+    if (my_cnt > 0)
+      gather_x<F, 4, 3>(S, vfeat, recs, cp.row0 + 128 * grp, my_cnt, enc, PartTiles<3>{{A[0], A[1], A[2]}}, gw, lane);
     tc::fence_proxy_async();
-    __syncthreads();
     if (new_w) {
-      bool ok = tid == 0 ? tc::mbar_wait(B.wbar, B.wphase) : true;
-      B.wphase ^= 1u;
-      if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
-    }
-    const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    const uint32_t w = tc::smem_addr(Wsm);
-    const uint32_t a3[3] = {tc::smem_addr(A[0]), tc::smem_addr(A[1]), tc::smem_addr(A[2])};
-    float out3[3] = {0.f, 0.f, 0.f};
-    for (int l = 0; l <= L; ++l) {
-      if (tid == 0) {
-        tc::fence_after_sync();
-        const uint32_t wofs = (uint32_t)(l < L ? l * H * 128 : L * H * 128);
-        const uint32_t w3[3] = {w + wofs, w + lay.hi_part + wofs, w + 2 * lay.hi_part + wofs};
-        issue_fwd_layer(tmem, a3, w3, l < L ? H : 16, l == 0 ? 4 : KH);
-        tc::mma_commit(B.mbar);
+      bool ok = tid == 0 ? tc::mbar_wait(wbar, wphase) : true;
+      wphase ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        if (tid == 0) drain.set(wbar, wphase ^ 1u);
+        break;
       }
-      if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
-      if (l < L) {
-        // the output layer also takes split inputs
-        if (l == 0)
-          epi_fwd_hidden<H, NC, 4>(taddr, fbias, A, row, part);
-        else
-          epi_fwd_hidden<H, NC, KH>(taddr, fbias + 64 * l, A, row, part);
-        tc::fence_proxy_async();
-      } else {
-        float x[16];
-        fwd_sum16<KH>(taddr, 0, fbias + 64 * L, x);
-        out3[0] = x[0]; out3[1] = x[1]; out3[2] = x[2];
-      }
-      tc::fence_before_sync();
+    } else {
       __syncthreads();
     }
-    if (failed) break;
-    if (part == 0 && row < cp.cnt)
-      cout[cp.row0 + row] = make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
+    // the group's layer chain
+    const uint32_t w = tc::smem_addr(Wsm);
+    float out3[3] = {0.f, 0.f, 0.f};
+    bool gfail = false;
+    if (my_cnt > 0) {
+      for (int l = 0; l <= L; ++l) {
+        if (tid == leader) {
+          tc::fence_after_sync();
+          const uint32_t wofs = (uint32_t)(l < L ? l * H * 128 : L * H * 128);
+          const uint32_t w3[3] = {w + wofs, w + lay.hi_part + wofs, w + 2 * lay.hi_part + wofs};
+          issue_fwd_layer(gacc, a3, w3, l < L ? H : 16, l == 0 ? 4 : KH);
+          tc::mma_commit(mbar);
+        }
+        const bool ok = tid == leader ? tc::mbar_wait(mbar, mphase) : true;
+        mphase ^= 1u;
+        if (tc::bar_or(gbar, 128, !ok)) {
+          gfail = true;
+          if (tid == leader) drain.set(mbar, mphase ^ 1u);
+          break;
+        }
+        tc::fence_after_sync();
+        if (l < L) {
+          epi_fwd_hidden<H>(taddr, fbias + 64 * l, A, row);  // the output layer also takes split inputs
+          tc::fence_proxy_async();
+        } else {
+          float x[16];
+          fwd_sum16(taddr, 0, fbias + 64 * L, x);
+          out3[0] = x[0]; out3[1] = x[1]; out3[2] = x[2];
+        }
+        tc::fence_before_sync();
+        tc::bar_sync(gbar, 128);
+      }
+    }
+    if (__syncthreads_or(gfail)) { failed = true; break; }
+    if (row < my_cnt)
+      cout[cp.row0 + 128 * grp + row] =
+          make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
   }
   bool drained = true;
-  if (failed && tid == 0) {
-    atomicOr(S.err, ERR_TIMEOUT);
+  if (failed && tid % 128 == 0) {
+    if (tid == 0) atomicOr(S.err, ERR_TIMEOUT);
     drained = drain.run();
     if (!drained) atomicOr(S.err, ERR_DRAIN);
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when in-flight work did not drain
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, NTMEM);
 }
 
 // ---------------------------------------------------------------------------
@@ -762,10 +772,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       my_fr = __ldg(src + 1);
       my_cn = __ldg(reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8) + part);
     }
-    {
-      uint8_t* const X2[2] = {Xt, MidA};
-      gather_x<F, 8, 2>(S, vfeat, recs, cp.row0, cp.cnt, enc, X2, warp, lane);
-    }
+    gather_x<F, 8, 2>(S, vfeat, recs, cp.row0, cp.cnt, enc, PartTiles<2>{{Xt, MidA}}, warp, lane);
     // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
     if (part == 0)
       *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(row, 0)) =
@@ -785,14 +792,13 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       uint8_t* mid_out = (l & 1) ? MidA : MidB;
       if (tid == 0) {
         tc::fence_after_sync();
-        const uint32_t a2[3] = {tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(mid_in), 0u};
-        const uint32_t w2[3] = {w + l * H * 128, w + lay.mid_off + l * H * 128, 0u};
-        issue_split_layer(tw, a2, w2, 2, w + lay.bias_off + 32 * l, ones8, H, l == 0 ? 4 : H / 16);
+        issue_split_layer(tw, tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(mid_in),
+                          w + l * H * 128, w + lay.mid_off + l * H * 128, w + lay.bias_off + 32 * l, ones8, H,
+                          l == 0 ? 4 : H / 16);
         tc::mma_commit(B.mbar);
       }
       if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
-      uint8_t* const dst[2] = {Ht + l * 16384, l + 1 < L ? mid_out : nullptr};
-      epi_relu_split<H, 2, 2>(taddr, dst, row, part);
+      epi_relu_split<H, 2>(taddr, Ht + l * 16384, l + 1 < L ? mid_out : nullptr, row, part);
       tc::fence_proxy_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -911,25 +917,24 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     ray_enc_kernel<<<(int)((a.n + 127) / 128 < 65536 ? (a.n + 127) / 128 : 65536), 128, 0, st>>>(a.dirs, a.n, a.enc);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    train_chunks_kernel<<<1, 32, 0, st>>>(a.tstart, S.num_tiles, a.coff);
+    train_chunks_kernel<<<1, 32, 0, st>>>(a.tstart, S.num_tiles, a.coff, a.coff + S.num_tiles + 2);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   e = cudaMemsetAsync(a.work, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   if (!backward) {
-    // one CTA per SM of 4 or 8 warps
-    const int smem = fwd_smem_bytes<128>(lay);
-    auto kern = a.fwd_warps == 4 ? tr_mlp_fwd_tc<F, H, L, 128> : tr_mlp_fwd_tc<F, H, L, 256>;
-    static unsigned long long cfg = 0;
-    e = once_per_device(&cfg, [&]() {
-      cudaError_t r = cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           smem);
-      if (r != cudaSuccess) return r;
-      return cudaFuncSetAttribute(tr_mlp_fwd_tc<F, H, L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // one CTA per SM of one or two 4-warp groups (128 or 256 rows per work unit)
+    const int ng = a.fwd_warps == 4 ? 1 : 2;
+    const int smem = fwd_smem_bytes(lay, ng);
+    static unsigned long long cfg1 = 0, cfg2 = 0;
+    e = once_per_device(ng == 1 ? &cfg1 : &cfg2, [&]() {
+      return cudaFuncSetAttribute(ng == 1 ? tr_mlp_fwd_tc<F, H, L, 1> : tr_mlp_fwd_tc<F, H, L, 2>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     });
     if (e != cudaSuccess) return e;
-    kern<<<a.num_sms, a.fwd_warps == 4 ? 128 : 256, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart,
-                                                                 a.coff, a.work, a.enc, a.wimg, a.img_stride, a.cout);
+    const int32_t* uoff = ng == 1 ? a.coff : a.coff + S.num_tiles + 2;
+    (ng == 1 ? tr_mlp_fwd_tc<F, H, L, 1> : tr_mlp_fwd_tc<F, H, L, 2>)<<<a.num_sms, 128 * ng, smem, st>>>(
+        S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, uoff, a.work, a.enc, a.wimg, a.img_stride, a.cout);
   } else {
     const int smem = train_tc_bwd_smem_bytes(H, L);
     static unsigned long long cfg = 0;
