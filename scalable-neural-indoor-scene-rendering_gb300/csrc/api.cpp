@@ -284,13 +284,16 @@ snisr_status render_impl(snisr_scene* sc, const CamDev* cam, const float* origin
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t* ev = sc->profiling ? sc->ev : nullptr;
   if (ev) CUDA_TRY(cudaEventRecord(ev[5], st), "render: event");
-  CUDA_TRY(launch_raygen(sc->S, cam, origins, dirs, n, sc->ws, form == SNISR_FORM_TC, st), "render: ray generation");
+  // camera frames march in 4 x 8 pixel warp tiles; the caller's rays in their order
+  const RayOrder ord = cam ? frame_ray_order(cam->W, cam->H, n) : RayOrder{};
+  CUDA_TRY(launch_raygen(sc->S, cam, origins, dirs, n, sc->ws, form == SNISR_FORM_TC, st, ord),
+           "render: ray generation");
   if (ev) CUDA_TRY(cudaEventRecord(ev[6], st), "render: event");
   if (form == SNISR_FORM_PLAIN_FP32) {
-    CUDA_TRY(launch_render_plain(sc->S, sc->ws, n, rgb, depth, opac, st), "render: plain kernel");
+    CUDA_TRY(launch_render_plain(sc->S, sc->ws, n, rgb, depth, opac, st, ord), "render: plain kernel");
     if (ev) CUDA_TRY(cudaEventRecord(ev[7], st), "render: event");
   } else {
-    CUDA_TRY(launch_render_tc(sc->S, sc->ws, n, rgb, depth, opac, sc->num_sms, st, ev), "render: batched kernels");
+    CUDA_TRY(launch_render_tc(sc->S, sc->ws, n, rgb, depth, opac, sc->num_sms, st, ev, ord), "render: batched kernels");
   }
   sc->last_form = form;
   return SNISR_OK;

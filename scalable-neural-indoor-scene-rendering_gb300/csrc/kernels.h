@@ -28,7 +28,7 @@ struct Tuning {
 struct Workspace {
   float4* ray_o = nullptr;     // [max_rays] origin
   float4* ray_d = nullptr;     // [max_rays] direction, w = start distance
-  uint4* enc = nullptr;        // [max_rays][4] FP16 view encoding (32 halves)
+  uint4* enc = nullptr;        // [max_rays][4] FP16 view encoding (32 halves), by pixel
   SampleRec* recs = nullptr;   // [cap] compacted samples
   SampleRec* sorted = nullptr; // [cap] samples grouped by tile
   uint32_t* blk_count = nullptr;  // [cap/256 + 1] valid samples per 256-slot block
@@ -65,14 +65,55 @@ bool mlp_shape_supported(int F, int H, int L);
 // Bytes of one tile's tensor-core weight image (see build in api.cpp).
 int tc_image_bytes(int H, int L);
 
+// Order of the rays of a camera frame.  Ray i of the frame (its slot in the
+// ray arrays and its lane in the traversal) is pixel ray_pixel(i): each warp
+// of 32 rays takes a 4 x 8 pixel tile (tiles row by row; with `grouped`, in
+// 2 x 2 groups, so that the 4 warps of a 128-thread block cover 8 x 16
+// pixels).  Rays of one warp then start close together and cross the same
+// voxels, which cuts the traversal's divergence and scattered loads.  The
+// outputs (colour, depth, opacity) and the view encodings are indexed by
+// pixel.  w = 0: ray i is pixel i (the caller's own rays, or an image the
+// tiles do not divide).
+struct RayOrder {
+  int w = 0;
+  bool grouped = false;
+};
+constexpr int kRayTileW = 4, kRayTileH = 8;
+inline RayOrder frame_ray_order(int W, int H, int64_t n) {
+  RayOrder o;
+  if (n != (int64_t)W * H || W % kRayTileW != 0 || H % kRayTileH != 0) return o;
+  o.w = W;
+  o.grouped = W % (2 * kRayTileW) == 0 && H % (2 * kRayTileH) == 0;
+  return o;
+}
+__host__ __device__ inline int64_t ray_pixel(int64_t i, RayOrder o) {
+  if (o.w == 0) return i;
+  const int64_t t = i >> 5;  // warp tile
+  const int k = (int)(i & 31);
+  const int tpr = o.w / kRayTileW;  // tiles per row
+  int64_t ty;
+  int tx;
+  if (o.grouped) {
+    const int64_t g = t >> 2;
+    const int r = (int)(t & 3);
+    ty = (g / (tpr / 2)) * 2 + (r >> 1);
+    tx = (int)(g % (tpr / 2)) * 2 + (r & 1);
+  } else {
+    ty = t / tpr;
+    tx = (int)(t % tpr);
+  }
+  return (ty * kRayTileH + k / kRayTileW) * o.w + tx * kRayTileW + k % kRayTileW;
+}
+
 cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* origins, const float* dirs,
-                          int64_t n, const Workspace& ws, bool want_enc, cudaStream_t st);
+                          int64_t n, const Workspace& ws, bool want_enc, cudaStream_t st, RayOrder ord = RayOrder{});
 cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
-                                float* opac, cudaStream_t st);
+                                float* opac, cudaStream_t st, RayOrder ord = RayOrder{});
 // ev (optional, 5 events): recorded before traverse, after traverse, scan,
 // scatter and the MLP.
 cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
-                             float* opac, int num_sms, cudaStream_t st, cudaEvent_t* ev = nullptr);
+                             float* opac, int num_sms, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                             RayOrder ord = RayOrder{});
 cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int K, int32_t* visited,
                          int32_t* count, cudaStream_t st);
 cudaError_t launch_proxy(const SceneDev& S, const float* origins, const float* dirs, int64_t n, float* t,

@@ -39,13 +39,14 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // ---------------------------------------------------------------------------
 __global__ void raygen_kernel(SceneDev S, CamDev cam, const float* __restrict__ origins,
                               const float* __restrict__ dirs, int64_t n, float4* ray_o, float4* ray_d,
-                              uint4* enc, int want_enc) {
+                              uint4* enc, int want_enc, RayOrder ord) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     float o[3], d[3];
+    const int64_t pix = ray_pixel(i, ord);
     if (dirs) {
       for (int a = 0; a < 3; ++a) { o[a] = origins[3 * i + a]; d[a] = dirs[3 * i + a]; }
     } else {
-      int py = (int)(i / cam.W), px = (int)(i - (int64_t)py * cam.W);
+      int py = (int)(pix / cam.W), px = (int)(pix - (int64_t)py * cam.W);
       camera_dir(cam.c2w, cam.cx, cam.cy, cam.inv_f, px, py, d);
       o[0] = cam.c2w[3]; o[1] = cam.c2w[7]; o[2] = cam.c2w[11];
     }
@@ -81,7 +82,7 @@ __global__ void raygen_kernel(SceneDev S, CamDev cam, const float* __restrict__ 
       __align__(16) __half h[32];
       for (int k = 0; k < 32; ++k) h[k] = __float2half_rn(k < 27 ? e[k] : 0.0f);
       const uint4* src = reinterpret_cast<const uint4*>(h);
-      for (int k = 0; k < 4; ++k) enc[4 * i + k] = src[k];
+      for (int k = 0; k < 4; ++k) enc[4 * pix + k] = src[k];
     }
   }
 }
@@ -190,7 +191,7 @@ __device__ __forceinline__ void mlp_plain(const float* __restrict__ P, const flo
 template <int F, int H, int L>
 __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const float4* __restrict__ ray_o,
                                                            const float4* __restrict__ ray_d, int64_t n,
-                                                           float* rgb, float* depth, float* opac) {
+                                                           float* rgb, float* depth, float* opac, RayOrder ord) {
   constexpr int KIN = F + 27;
   constexpr int KP = (KIN + 3) & ~3;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -229,17 +230,20 @@ __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const flo
         if (T < S.early_stop) break;
       }
     }
-    rgb[3 * i] = C[0]; rgb[3 * i + 1] = C[1]; rgb[3 * i + 2] = C[2];
-    depth[i] = D;
-    opac[i] = 1.0f - T;
+    const int64_t p = ray_pixel(i, ord);
+    rgb[3 * p] = C[0]; rgb[3 * p + 1] = C[1]; rgb[3 * p + 2] = C[2];
+    depth[p] = D;
+    opac[p] = 1.0f - T;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Batched tensor-core form, stage 1: traversal with per-warp compaction.
-// Each lane marches one ray; every round the warp converges, ballots the
+// Each lane marches one ray (camera frames: a warp marches a 4 x 8 pixel
+// tile, RayOrder); every round the warp converges, ballots the
 // lanes that produced a sample and writes them to consecutive slots of a
 // per-warp block of the sample buffer (one global atomic per 256 samples).
+// Records and outputs carry the ray's pixel.
 // Depth and opacity are final here: density comes from the voxel data, so
 // transmittance and early stop do not wait for the MLP.
 // ---------------------------------------------------------------------------
@@ -252,7 +256,7 @@ constexpr uint32_t kBlk = 256;
 __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
                                                                 const float4* __restrict__ ray_d, int64_t n,
                                                                 SampleRec* recs, uint32_t cap, uint32_t* blk_count,
-                                                                int* ctrl, float* depth, float* opac) {
+                                                                int* ctrl, float* depth, float* opac, RayOrder ord) {
   // per-warp tile histogram (no CTA-wide barrier: warps finish independently)
   extern __shared__ uint32_t hist_all[];
   const int lane = threadIdx.x & 31;
@@ -268,7 +272,8 @@ __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S
     float o[3] = {o4.x, o4.y, o4.z}, d[3] = {d4.x, d4.y, d4.z};
     live = R.init(S, o, d, d4.w);
   }
-  const uint32_t ray_id = (uint32_t)i;
+  const int64_t pix = ray_pixel(i, ord);
+  const uint32_t ray_id = (uint32_t)pix;
   uint32_t cur = 0, end = 0;  // warp-uniform block cursor
   // Each round a live lane emits the samples of one voxel (up to kVoxSamples:
   // a voxel holds at most 4 samples at 0.5-voxel steps), so that a voxel's
@@ -355,8 +360,8 @@ __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S
   if (lane == 0 && end != 0 && (end - kBlk) / kBlk < (cap + kBlk - 1) / kBlk)
     blk_count[(end - kBlk) / kBlk] = cur - (end - kBlk);
   if (i < n) {
-    depth[i] = D;
-    opac[i] = 1.0f - T;
+    depth[pix] = D;
+    opac[pix] = 1.0f - T;
   }
   unsigned long long st = (i < n) ? R.steps : 0u;
 #pragma unroll
@@ -791,8 +796,9 @@ inline int grid_for(int64_t n, int threads, int cap_blocks) {
 
 template <int F, int H, int L>
 cudaError_t render_plain_t(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth, float* opac,
-                           cudaStream_t st) {
-  render_plain_kernel<F, H, L><<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, ws.ray_o, ws.ray_d, n, rgb, depth, opac);
+                           cudaStream_t st, RayOrder ord) {
+  render_plain_kernel<F, H, L><<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, ws.ray_o, ws.ray_d, n, rgb, depth, opac,
+                                                                        ord);
   return cudaGetLastError();
 }
 
@@ -849,11 +855,12 @@ bool mlp_shape_supported(int F, int H, int L) {
 int tc_image_bytes(int H, int L) { return L * H * 128 + 2048 + H * 128 + 2048; }
 
 cudaError_t launch_raygen(const SceneDev& S, const CamDev* cam, const float* origins, const float* dirs, int64_t n,
-                          const Workspace& ws, bool want_enc, cudaStream_t st) {
+                          const Workspace& ws, bool want_enc, cudaStream_t st, RayOrder ord) {
   CamDev c{};
   if (cam) c = *cam;
+  if (!cam) ord = RayOrder{};  // the caller's rays keep their order
   raygen_kernel<<<grid_for(n, 128, 1 << 20), 128, 0, st>>>(S, c, origins, dirs, n, ws.ray_o, ws.ray_d, ws.enc,
-                                                           want_enc ? 1 : 0);
+                                                           want_enc ? 1 : 0, ord);
   return cudaGetLastError();
 }
 
@@ -870,17 +877,17 @@ cudaError_t launch_trace(const SceneDev& S, const Workspace& ws, int64_t n, int 
 }
 
 cudaError_t launch_render_plain(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth,
-                                float* opac, cudaStream_t st) {
+                                float* opac, cudaStream_t st, RayOrder ord) {
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;
-  if (F == 16 && H == 32 && L == 2) return render_plain_t<16, 32, 2>(S, ws, n, rgb, depth, opac, st);
-  if (F == 32 && H == 64 && L == 3) return render_plain_t<32, 64, 3>(S, ws, n, rgb, depth, opac, st);
-  if (F == 16 && H == 64 && L == 3) return render_plain_t<16, 64, 3>(S, ws, n, rgb, depth, opac, st);
-  if (F == 32 && H == 32 && L == 2) return render_plain_t<32, 32, 2>(S, ws, n, rgb, depth, opac, st);
+  if (F == 16 && H == 32 && L == 2) return render_plain_t<16, 32, 2>(S, ws, n, rgb, depth, opac, st, ord);
+  if (F == 32 && H == 64 && L == 3) return render_plain_t<32, 64, 3>(S, ws, n, rgb, depth, opac, st, ord);
+  if (F == 16 && H == 64 && L == 3) return render_plain_t<16, 64, 3>(S, ws, n, rgb, depth, opac, st, ord);
+  if (F == 32 && H == 32 && L == 2) return render_plain_t<32, 32, 2>(S, ws, n, rgb, depth, opac, st, ord);
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, float* rgb, float* depth, float* opac,
-                             int num_sms, cudaStream_t st, cudaEvent_t* ev) {
+                             int num_sms, cudaStream_t st, cudaEvent_t* ev, RayOrder ord) {
   cudaError_t e = cudaMemsetAsync(ws.ctrl, 0, sizeof(int) * ws.ctrl_words, st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(rgb, 0, sizeof(float) * 3 * n, st);
@@ -889,7 +896,7 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   const int tt = ws.tune.traverse_threads;
   const int hist_bytes = (int)sizeof(uint32_t) * S.num_tiles * (tt / 32);
   traverse_kernel<<<grid_for(n, tt, 1 << 24), tt, hist_bytes, st>>>(S, ws.ray_o, ws.ray_d, n, ws.recs, ws.cap,
-                                                                     ws.blk_count, ws.ctrl, depth, opac);
+                                                                     ws.blk_count, ws.ctrl, depth, opac, ord);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles, ws.cap);
