@@ -167,9 +167,11 @@ __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
   return d;
 }
 
-// shared memory: A (16 KB) | W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) |
-// FP32 biases [6][64] (1.5 KB, added by the epilogues) | barriers, slots:
-// ~62 KB, three CTAs per SM
+// shared memory: A (16 KB, the position encodings: layer 0's operand) |
+// W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) | FP32 biases [6][64] (1.5 KB,
+// added by the epilogues) | barriers, slots: ~62 KB, three CTAs per SM.
+// Tensor memory (128 columns): the accumulator [0, 64) and the hidden
+// activations [64, 96) (FP16 pairs), the A operand of layers 1..5.
 constexpr int kSpA = 0, kSpW = 16384, kSpWout = kSpW + 5 * 8192, kSpBias = kSpWout + 4096,
               kSpBars = kSpBias + 6 * 64 * 4, kSpSmem = kSpBars + 64;
 
@@ -213,6 +215,13 @@ __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
   }
 }
 
+// One CTA: chunks of 128 samples of one network's pixel block.  Layer 0
+// reads the position encodings from shared memory; each hidden layer's
+// epilogue (bias, LeakyReLU, FP16 pack) writes its row of activations into
+// tensor memory with tcgen05.st, where the next layer's MMA reads its A
+// operand, so no activation goes through shared memory.  Software pipeline:
+// the next chunk's tasks are fetched during layer 0's MMA, and its encodings
+// computed and stored into the (then free) shared A tile during layer 1's.
 __global__ void __launch_bounds__(128, 3)
     inference_mlp_kernel(int spr, int num_block, float inv_far, float trans_stop, const int16_t* __restrict__ net,
                          int num_groups, const float* __restrict__ transparency, const int32_t* __restrict__ qpix,
@@ -231,7 +240,7 @@ __global__ void __launch_bounds__(128, 3)
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(tmem_slot), 64);
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 128);
     tc::tmem_relinquish();
   }
   tc::fence_proxy_async();
@@ -239,6 +248,7 @@ __global__ void __launch_bounds__(128, 3)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
+  const uint32_t tact = tmem + kSpH;  // activation columns (A operand of layers 1..5)
   const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
   const float* bias = reinterpret_cast<const float*>(sm + kSpBias);
   const uint32_t a_base = tc::smem_addr(sm + kSpA);
@@ -247,6 +257,47 @@ __global__ void __launch_bounds__(128, 3)
   int cur_net = -1;
   bool failed = false;
   tc::Drain drain;
+  // The task of this thread's A row: its pixel, whether it is live, the
+  // encoded position and the view direction.
+  struct Task {
+    bool live;
+    int64_t ori;
+    float p[3], d[3];
+  };
+  // this thread's row of the shared A tile: the position encoding of task k
+  // (zeros when it is not live).  sin/cos of 2^i p (i = 0..9): one accurate
+  // sincos per coordinate, then double-angle steps (error ~2^9 x FP32
+  // rounding at i = 9, below half an FP16 ulp)
+  auto encode_row = [&](const Task& k) {
+    uint32_t h[32];
+    if (k.live) {
+      float x[64];
+      x[0] = k.p[0]; x[1] = k.p[1]; x[2] = k.p[2];
+      float sn[3], cs[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) sincosf(k.p[a], &sn[a], &cs[a]);
+#pragma unroll
+      for (int i = 0; i < 10; ++i) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          x[3 + 6 * i + a] = sn[a];
+          x[6 + 6 * i + a] = cs[a];
+          const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
+          sn[a] = s2;
+          cs[a] = c2;
+        }
+      }
+      x[63] = 0.f;
+#pragma unroll
+      for (int q = 0; q < 32; ++q) h[q] = pack_h2(x[2 * q], x[2 * q + 1]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) h[q] = 0u;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, c)) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+  };
   for (;;) {
     __syncthreads();  // every thread has read the previous slot value
     if (tid == 0) *blk_slot = atomicAdd(work, 1);
@@ -263,16 +314,6 @@ __global__ void __launch_bounds__(128, 3)
     }
     const float cx = centers[3 * g], cy = centers[3 * g + 1], cz = centers[3 * g + 2];
     const int64_t t0 = (int64_t)pstarts[b] * spr, t1 = (int64_t)pstarts[b + 1] * spr;
-    // The task of this thread's A row in the chunk starting at c: its pixel,
-    // whether it is live, the encoded position and the view direction.  The
-    // next chunk's tasks are fetched during the current chunk's first MMA
-    // (three dependent loads), so that only arithmetic is left between the
-    // chunks.
-    struct Task {
-      bool live;
-      int64_t ori;
-      float p[3], d[3];
-    };
     auto fetch = [&](int64_t c) {
       Task k;
       const int64_t t = c + tid;
@@ -294,45 +335,11 @@ __global__ void __launch_bounds__(128, 3)
       return k;
     };
     Task cur = fetch(t0);
+    encode_row(cur);  // the block's first chunk
+    tc::fence_proxy_async();
     for (int64_t c0 = t0; c0 < t1; c0 += 128) {
-      // A row of this thread: position encoding of its task (zeros when skipped)
-      {
-        uint32_t h[32];
-        if (cur.live) {
-          const float* p = cur.p;
-          // sin/cos of 2^i p (i = 0..9): one accurate sincos per coordinate, then
-          // double-angle steps (error ~2^9 x FP32 rounding at i = 9, below half
-          // an FP16 ulp)
-          float x[64];
-          x[0] = p[0]; x[1] = p[1]; x[2] = p[2];
-          float sn[3], cs[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a) sincosf(p[a], &sn[a], &cs[a]);
-#pragma unroll
-          for (int i = 0; i < 10; ++i) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-              x[3 + 6 * i + a] = sn[a];
-              x[6 + 6 * i + a] = cs[a];
-              const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
-              sn[a] = s2;
-              cs[a] = c2;
-            }
-          }
-          x[63] = 0.f;
-#pragma unroll
-          for (int q = 0; q < 32; ++q) h[q] = pack_h2(x[2 * q], x[2 * q + 1]);
-        } else {
-#pragma unroll
-          for (int q = 0; q < 32; ++q) h[q] = 0u;
-        }
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, c)) =
-              make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
-      }
-      tc::fence_proxy_async();
-      __syncthreads();
+      const bool more = c0 + 128 < t1;
+      __syncthreads();  // this chunk's A rows are visible to the MMA issuer
       Task nxt;
       nxt.live = false;
       float out[32];
@@ -342,38 +349,44 @@ __global__ void __launch_bounds__(128, 3)
           const bool last = l == kSpHidden;
           const uint32_t wb = tc::smem_addr(sm + (last ? kSpWout : kSpW + l * 8192));
           const uint32_t id = last ? id_o : id_h;
-          for (int kk = 0; kk < 4; ++kk)
-            tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+          if (l == 0) {  // K = 64 position encodings from shared memory
+            for (int kk = 0; kk < 4; ++kk)
+              tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+          } else {  // K = 64 activations from tensor memory (8 columns per K = 16 step)
+            for (int kk = 0; kk < 4; ++kk)
+              tc::mma_f16_ta(tmem, tact + 8 * kk, tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+          }
           tc::mma_commit(mbar);
         }
-        if (l == 0 && c0 + 128 < t1) nxt = fetch(c0 + 128);
+        if (l == 0 && more) nxt = fetch(c0 + 128);
+        if (l == 1 && more) {  // layer 0 has read the A tile: the next chunk's encodings
+          encode_row(nxt);
+          tc::fence_proxy_async();
+        }
         const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
         mphase ^= 1u;
         if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
         tc::fence_after_sync();
         if (l < kSpHidden) {
+          // bias + LeakyReLU + FP16 pack of 16 columns at a time into this
+          // row's lane of the activation columns
 #pragma unroll
-          for (int half = 0; half < 2; ++half) {
-            float v[32];
-            tc::tmem_ld16(taddr + 32 * half, v);
-            tc::tmem_ld16(taddr + 32 * half + 16, v + 16);
+          for (int part = 0; part < kSpH / 16; ++part) {
+            float v[16];
+            tc::tmem_ld16(taddr + 16 * part, v);
             tc::tmem_wait_ld();
+            uint32_t o[8];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              uint32_t o[4];
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                const int col = 32 * half + 8 * q + 2 * j;
-                float a0 = v[8 * q + 2 * j] + bias[64 * l + col], a1 = v[8 * q + 2 * j + 1] + bias[64 * l + col + 1];
-                a0 = a0 < 0.f ? 0.01f * a0 : a0;
-                a1 = a1 < 0.f ? 0.01f * a1 : a1;
-                o[j] = pack_h2(a0, a1);
-              }
-              *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, 4 * half + q)) =
-                  make_uint4(o[0], o[1], o[2], o[3]);
+            for (int j = 0; j < 8; ++j) {
+              const int col = 16 * part + 2 * j;
+              float a0 = v[2 * j] + bias[64 * l + col], a1 = v[2 * j + 1] + bias[64 * l + col + 1];
+              a0 = a0 < 0.f ? 0.01f * a0 : a0;
+              a1 = a1 < 0.f ? 0.01f * a1 : a1;
+              o[j] = pack_h2(a0, a1);
             }
+            tc::tmem_st8(taddr + kSpH + 8 * part, o);
           }
-          tc::fence_proxy_async();
+          tc::tmem_wait_st();
         } else {
           tc::tmem_ld16(taddr, out);
           tc::tmem_ld16(taddr + 16, out + 16);
@@ -415,7 +428,7 @@ __global__ void __launch_bounds__(128, 3)
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when in-flight work did not drain
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 }  // namespace
