@@ -273,6 +273,56 @@ snisr_status scene_views(snisr_scene* sc, SceneDev* S, Workspace* ws, int* devic
 
 namespace {
 
+// Chebyshev distance, in 4^3 blocks, from every block of a tile's nb^3 block
+// grid to the nearest occupied block (0 for an occupied block), capped at
+// kBlkDistCap + 1: the L-infinity distance transform taken one axis at a
+// time (exact: max(|dx|, |dy|, |dz|) separates into three 1-D passes).
+void block_distance(const uint32_t* bmask, int nb, uint8_t* out) {
+  const int big = kBlkDistCap + 1;
+  const size_t n = (size_t)nb * nb * nb;
+  auto id = [nb](int x, int y, int z) { return ((size_t)x * nb + y) * nb + z; };
+  std::vector<uint8_t> a(n), b(n);
+  for (int x = 0; x < nb; ++x)  // z: distance to the nearest occupied block of the row
+    for (int y = 0; y < nb; ++y) {
+      int last = -1000000;
+      for (int z = 0; z < nb; ++z) {
+        const size_t k = id(x, y, z);
+        if ((bmask[k >> 5] >> (k & 31)) & 1u) last = z;
+        a[k] = (uint8_t)std::min(big, z - last);
+      }
+      int next = 1000000;
+      for (int z = nb - 1; z >= 0; --z) {
+        const size_t k = id(x, y, z);
+        if ((bmask[k >> 5] >> (k & 31)) & 1u) next = z;
+        a[k] = (uint8_t)std::min<int>(a[k], std::min(big, next - z));
+      }
+    }
+  auto pass = [&](const std::vector<uint8_t>& src, std::vector<uint8_t>& dst, int axis) {
+    for (int x = 0; x < nb; ++x)
+      for (int y = 0; y < nb; ++y)
+        for (int z = 0; z < nb; ++z) {
+          int c[3] = {x, y, z};
+          int m = src[id(x, y, z)];
+          for (int dd = 1; dd < m; ++dd)
+            for (int sgn = -1; sgn <= 1; sgn += 2) {
+              int q[3] = {c[0], c[1], c[2]};
+              q[axis] += sgn * dd;
+              if (q[axis] < 0 || q[axis] >= nb) continue;
+              m = std::min(m, std::max<int>(src[id(q[0], q[1], q[2])], dd));
+            }
+          dst[id(x, y, z)] = (uint8_t)m;
+        }
+  };
+  pass(a, b, 1);
+  std::vector<uint8_t> r(n);
+  pass(b, r, 0);
+  std::copy(r.begin(), r.end(), out);
+}
+
+}  // namespace
+
+namespace {
+
 snisr_status render_impl(snisr_scene* sc, const CamDev* cam, const float* origins, const float* dirs, int64_t n,
                          int32_t form, float* rgb, float* depth, float* opac, void* stream) {
   if (check_scene(sc) != SNISR_OK) return SNISR_INVALID_ARG;
@@ -399,12 +449,19 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
   S.mlp_layers = d->mlp_layers;
   S.params_per_tile = sc->P;
 
+  // per-tile block distances (jumps of the training march over empty space)
+  std::vector<uint8_t> bdist((size_t)NT * nb * nb * nb);
+  for (int t = 0; t < NT; ++t)
+    block_distance(bmask.data() + (size_t)t * bwords, nb, bdist.data() + (size_t)t * nb * nb * nb);
+
   int32_t* d_tindex = nullptr; float* d_cent = nullptr; OccWord* d_occ = nullptr; uint32_t* d_bmask = nullptr;
+  uint8_t* d_bdist = nullptr;
   if ((st = upload(sc, &d_tindex, d->tile_index, (size_t)ndense * 4, "tile index")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_cent, centers.data(), centers.size() * 4, "tile centres")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_occ, occ.data(), occ.size() * sizeof(OccWord), "occupancy")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_bmask, bmask.data(), bmask.size() * 4, "block masks")) != SNISR_OK) return fail(st);
-  S.tile_index = d_tindex; S.tile_center = d_cent; S.occ = d_occ; S.block_mask = d_bmask;
+  if ((st = upload(sc, &d_bdist, bdist.data(), bdist.size(), "block distances")) != SNISR_OK) return fail(st);
+  S.tile_index = d_tindex; S.tile_center = d_cent; S.occ = d_occ; S.block_mask = d_bmask; S.blk_dist = d_bdist;
 
   // per-voxel corner caches, expanded on the device
   const int64_t nvox = d->num_voxels, nv = d->num_vertices;

@@ -356,6 +356,61 @@ struct RayState {
       if (occupied(S, tile, vid, r)) { rec = r; return true; }
     }
   }
+
+  // next_voxel for training segments, which cross long stretches of empty
+  // space: when the current voxel's 4^3 block is empty, with block distance
+  // D, every block within Chebyshev distance D - 1 of it is empty too, and
+  // the DDA steps on through that box in a tight loop without occupancy
+  // loads.  The steps are the cell-by-cell march's own (the same additions
+  // and comparisons), so the voxels, their entry and exit distances and the
+  // samples are identical to next_voxel's.
+  __device__ bool next_voxel_skip(const SceneDev& S) {
+    const int N = S.res, nb = N >> 2;
+    for (;;) {
+      if (tile < 0) {
+        if (!tile_live) return false;
+        if (!pending_tile && !step_tile(S)) return false;
+        pending_tile = false;
+        if (!open_tile(S)) continue;
+      }
+      if (entry_pending) {
+        entry_pending = false;  // the entry voxel of a tile, or the first voxel past an empty box
+      } else {
+        bool in;
+        if (vmax[0] < vmax[1]) in = (vmax[0] < vmax[2]) ? voxel_axis_step<0>(N) : voxel_axis_step<2>(N);
+        else in = (vmax[1] < vmax[2]) ? voxel_axis_step<1>(N) : voxel_axis_step<2>(N);
+        near_ = far_;
+        if (!in) { tile = -1; continue; }
+      }
+      ++steps;
+      far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
+      const int bx = vc[0] >> 2, by = vc[1] >> 2, bz = vc[2] >> 2;
+      const int D = __ldg(S.blk_dist + (size_t)tile * nb * nb * nb + (size_t)((bx * nb + by) * nb + bz));
+      if (D == 0) {
+        int vid = (vc[0] * N + vc[1]) * N + vc[2];
+        uint32_t r;
+        if (occupied(S, tile, vid, r)) { rec = r; return true; }
+        continue;
+      }
+      // the empty box [lo, hi) in voxels: step through it without loads
+      const int r = 4 * (D - 1);
+      const int lo0 = 4 * bx - r, lo1 = 4 * by - r, lo2 = 4 * bz - r;
+      const int hi0 = 4 * bx + 4 + r, hi1 = 4 * by + 4 + r, hi2 = 4 * bz + 4 + r;
+      bool in = true;
+      for (;;) {
+        if (vmax[0] < vmax[1]) in = (vmax[0] < vmax[2]) ? voxel_axis_step<0>(N) : voxel_axis_step<2>(N);
+        else in = (vmax[1] < vmax[2]) ? voxel_axis_step<1>(N) : voxel_axis_step<2>(N);
+        near_ = far_;
+        if (!in) break;
+        ++steps;
+        far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
+        if (vc[0] < lo0 || vc[0] >= hi0 || vc[1] < lo1 || vc[1] >= hi1 || vc[2] < lo2 || vc[2] >= hi2) break;
+      }
+      if (!in) { tile = -1; continue; }
+      --steps;             // counted again when the voxel past the box is examined
+      entry_pending = true;  // examine the voxel past the box without stepping
+    }
+  }
 };
 
 // One sample inside an occupied voxel.
@@ -368,6 +423,8 @@ struct Sample {
 };
 
 // Produces the next sample of the ray; false when the ray left the scene.
+// SKIP: empty space is crossed with RayState::next_voxel_skip (training).
+template <bool SKIP = false>
 __device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Sample& s) {
   for (;;) {
     if (R.in_voxel && R.z < R.far_) {
@@ -383,7 +440,7 @@ __device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Samp
       R.z = march_next(R.z, S.step_len);
       return true;
     }
-    if (!R.next_voxel(S)) return false;
+    if (!(SKIP ? R.next_voxel_skip(S) : R.next_voxel(S))) return false;
     R.in_voxel = true;
     R.z = R.near_;
   }

@@ -21,6 +21,8 @@ struct __align__(16) BvhNodeDev {
   int32_t count;
 };
 
+constexpr int kBlkDistCap = 15;
+
 // Device view of a scene, passed to kernels by value.
 struct SceneDev {
   int gx, gy, gz;
@@ -33,6 +35,8 @@ struct SceneDev {
   const float* tile_center;      // [NT][3]
   const OccWord* occ;            // [NT][words_per_tile]
   const uint32_t* block_mask;    // [NT][(N/4)^3 / 32] coarse 4^3-block occupancy
+  const uint8_t* blk_dist;       // [NT][(N/4)^3] Chebyshev distance, in 4^3 blocks, to the nearest
+                                 // occupied block of the tile (0: occupied), at most kBlkDistCap + 1
   const float* dens;             // [NVOX][8] density logits per corner
   const int32_t* corners;        // [NVOX][8] vertex ids (training gathers/scatters)
   const float4* feat32;          // [NVOX][F/4][8] float4 per (channel group, corner)
