@@ -402,7 +402,8 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
   for (int t = 0; t < NT; ++t)
     if (!seen[(size_t)t]) return fail(set_error(SNISR_CORRUPT_SCENE, "scene_create: tile id without a grid cell"));
 
-  // occupancy words with global voxel bases, coarse 4^3 block masks
+  // occupancy words with global voxel bases, coarse 4^3 block masks (host only:
+  // they give the block distances below)
   std::vector<OccWord> occ((size_t)(NT * words));
   const int nb = N / 4;
   const int64_t bwords = ((int64_t)nb * nb * nb + 31) / 32;
@@ -454,14 +455,12 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
   for (int t = 0; t < NT; ++t)
     block_distance(bmask.data() + (size_t)t * bwords, nb, bdist.data() + (size_t)t * nb * nb * nb);
 
-  int32_t* d_tindex = nullptr; float* d_cent = nullptr; OccWord* d_occ = nullptr; uint32_t* d_bmask = nullptr;
-  uint8_t* d_bdist = nullptr;
+  int32_t* d_tindex = nullptr; float* d_cent = nullptr; OccWord* d_occ = nullptr; uint8_t* d_bdist = nullptr;
   if ((st = upload(sc, &d_tindex, d->tile_index, (size_t)ndense * 4, "tile index")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_cent, centers.data(), centers.size() * 4, "tile centres")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_occ, occ.data(), occ.size() * sizeof(OccWord), "occupancy")) != SNISR_OK) return fail(st);
-  if ((st = upload(sc, &d_bmask, bmask.data(), bmask.size() * 4, "block masks")) != SNISR_OK) return fail(st);
   if ((st = upload(sc, &d_bdist, bdist.data(), bdist.size(), "block distances")) != SNISR_OK) return fail(st);
-  S.tile_index = d_tindex; S.tile_center = d_cent; S.occ = d_occ; S.block_mask = d_bmask; S.blk_dist = d_bdist;
+  S.tile_index = d_tindex; S.tile_center = d_cent; S.occ = d_occ; S.blk_dist = d_bdist;
 
   // per-voxel corner caches, expanded on the device
   const int64_t nvox = d->num_voxels, nv = d->num_vertices;

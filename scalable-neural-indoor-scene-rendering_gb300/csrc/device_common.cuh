@@ -161,14 +161,6 @@ __device__ __forceinline__ bool occupied(const SceneDev& S, int tile, int vid, u
   return true;
 }
 
-__device__ __forceinline__ bool block_occupied(const SceneDev& S, int tile, int cx, int cy, int cz) {
-  int nb = S.res >> 2;
-  int bid = (cx * nb + cy) * nb + cz;
-  int words = (nb * nb * nb + 31) >> 5;
-  uint32_t w = __ldg(S.block_mask + (size_t)tile * words + (bid >> 5));
-  return (w >> (bid & 31)) & 1u;
-}
-
 // Ray state machine: tile DDA over the scene grid, voxel DDA inside each
 // visited tile, fixed-step samples inside each occupied voxel.
 //
@@ -320,51 +312,14 @@ struct RayState {
 
   // Moves to the next occupied voxel along the ray, crossing tiles as
   // needed.  Sets rec, near_, far_.  Returns false when the ray has left the
-  // scene.  Every iteration moves one DDA coordinate by one cell, so the loop
-  // ends after at most (grid + tile) extent steps.
+  // scene.  Every step moves one DDA coordinate by one cell, so the loop ends
+  // after at most (grid + tile) extent steps.  Empty space: when the current
+  // voxel's 4^3 block is empty, with block distance D, every block within
+  // Chebyshev distance D - 1 of it is empty too, and the DDA steps on through
+  // that box in a tight loop without occupancy loads -- the same steps (the
+  // same additions and comparisons) as examining the cells one by one, so the
+  // voxels met and their entry and exit distances are unchanged.
   __device__ bool next_voxel(const SceneDev& S) {
-    const int N = S.res;
-    for (;;) {
-      if (tile < 0) {
-        if (!tile_live) return false;
-        if (!pending_tile && !step_tile(S)) return false;
-        pending_tile = false;
-        if (!open_tile(S)) continue;
-      }
-      if (entry_pending) {
-        // the entry voxel of the freshly opened tile
-        entry_pending = false;
-        ++steps;
-        far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
-        int vid = (vc[0] * N + vc[1]) * N + vc[2];
-        uint32_t r;
-        if (block_occupied(S, tile, vc[0] >> 2, vc[1] >> 2, vc[2] >> 2) && occupied(S, tile, vid, r)) {
-          rec = r;
-          return true;
-        }
-      }
-      bool in;
-      if (vmax[0] < vmax[1]) in = (vmax[0] < vmax[2]) ? voxel_axis_step<0>(N) : voxel_axis_step<2>(N);
-      else in = (vmax[1] < vmax[2]) ? voxel_axis_step<1>(N) : voxel_axis_step<2>(N);
-      near_ = far_;
-      if (!in) { tile = -1; continue; }
-      ++steps;
-      far_ = fminf(fminf(vmax[0], vmax[1]), vmax[2]);
-      if (!block_occupied(S, tile, vc[0] >> 2, vc[1] >> 2, vc[2] >> 2)) continue;
-      int vid = (vc[0] * N + vc[1]) * N + vc[2];
-      uint32_t r;
-      if (occupied(S, tile, vid, r)) { rec = r; return true; }
-    }
-  }
-
-  // next_voxel for training segments, which cross long stretches of empty
-  // space: when the current voxel's 4^3 block is empty, with block distance
-  // D, every block within Chebyshev distance D - 1 of it is empty too, and
-  // the DDA steps on through that box in a tight loop without occupancy
-  // loads.  The steps are the cell-by-cell march's own (the same additions
-  // and comparisons), so the voxels, their entry and exit distances and the
-  // samples are identical to next_voxel's.
-  __device__ bool next_voxel_skip(const SceneDev& S) {
     const int N = S.res, nb = N >> 2;
     for (;;) {
       if (tile < 0) {
@@ -423,8 +378,6 @@ struct Sample {
 };
 
 // Produces the next sample of the ray; false when the ray left the scene.
-// SKIP: empty space is crossed with RayState::next_voxel_skip (training).
-template <bool SKIP = false>
 __device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Sample& s) {
   for (;;) {
     if (R.in_voxel && R.z < R.far_) {
@@ -440,7 +393,7 @@ __device__ __forceinline__ bool next_sample(const SceneDev& S, RayState& R, Samp
       R.z = march_next(R.z, S.step_len);
       return true;
     }
-    if (!(SKIP ? R.next_voxel_skip(S) : R.next_voxel(S))) return false;
+    if (!R.next_voxel(S)) return false;
     R.in_voxel = true;
     R.z = R.near_;
   }

@@ -34,7 +34,6 @@ struct SceneDev {
   const int32_t* tile_index;     // dense -> sparse
   const float* tile_center;      // [NT][3]
   const OccWord* occ;            // [NT][words_per_tile]
-  const uint32_t* block_mask;    // [NT][(N/4)^3 / 32] coarse 4^3-block occupancy
   const uint8_t* blk_dist;       // [NT][(N/4)^3] Chebyshev distance, in 4^3 blocks, to the nearest
                                  // occupied block of the tile (0: occupied), at most kBlkDistCap + 1
   const float* dens;             // [NVOX][8] density logits per corner

@@ -87,7 +87,7 @@ __global__ void tr_march_kernel(SceneDev S, const float4* __restrict__ dc, const
         float T = 1.0f;
         Sample s;
         const int64_t base = mode == 1 ? off[i] : 0;
-        while (next_sample<true>(S, R, s)) {
+        while (next_sample(S, R, s)) {
           float w[8];
           const float g = seg_logit(dc, s.rec, s.f, w);
           const float sig = softplusf(g);
