@@ -49,12 +49,12 @@ TRAIN_WORKLOAD = ("cfg3 training step (forward + backward): 1 tile of 256^3 over
 # the kernels of one frame / step, from one capture of the same workload; the
 # summaries with their commands are under profiles/.
 NCU_DRAM_BYTES_PER_LAUNCH = {
-    "mlp_tc": {"bytes": 294424576,
-               "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mlp_tc_kernel<32, 64, 3> with its "
-                         "activations in tensor memory, one launch of `bench.py --profile-run render --steps 2 "
-                         "--warmup 1` (profiles/mlp_tc_and_traverse_cfg2_frame.md)"},
-    "traverse": {"bytes": 166710272, "source": "same capture"},
-    "scatter": {"bytes": 364119339, "source": "profiles/launches_render_cfg2.md"},
+    "mlp_tc": {"bytes": 335270042,
+               "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of mlp_tc_kernel<32, 64, 3>, mean of the "
+                         "5 launches (5 poses) of `bench.py --profile-run render --steps 2 --warmup 1` "
+                         "(profiles/launches_render_cfg2.md)"},
+    "traverse": {"bytes": 193275546, "source": "same capture"},
+    "scatter": {"bytes": 350698496, "source": "same capture"},
 }
 
 
