@@ -48,6 +48,7 @@ TRAIN_WORKLOAD = ("cfg3 training step (forward + backward): 1 tile of 256^3 over
 # DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum) of
 # the kernels of one frame / step, from one capture of the same workload; the
 # summaries with their commands are under profiles/.
+SAMPLE_RECORD_BYTES = 16  # SampleRec: voxel id, 24-bit pixel + weight, 16-bit fixed-point position
 NCU_DRAM_BYTES_PER_LAUNCH = {
     "mlp_tc": {"bytes": 335270042,
                "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of mlp_tc_kernel<32, 64, 3>, mean of the "
@@ -1014,7 +1015,7 @@ def main():
     # algorithmic work per launch (one frame) is
     #   FLOP: 24,320 per sample (59-64x3-3 MLP, forward only);
     #   compulsory bytes: every distinct trilinear corner of the frame once
-    #     (32 FP16 features + FP16 density), every 32-byte sample record once,
+    #     (32 FP16 features + FP16 density), every 16-byte sample record once,
     #     every ray's 64-byte view encoding and 12 bytes of colour once, every
     #     tile's 36,864-byte weight image once.
     # roofline.frac is the larger of the tensor and compulsory-HBM fractions.
@@ -1023,8 +1024,9 @@ def main():
     # as a side figure only and can exceed the copy peak.
     img = TC_IMAGE_BYTES
     mlp_flop = samples * MLP_FLOP_PER_SAMPLE
-    mlp_bytes_compulsory = dvert * (32 + 1) * 2 + samples * 32 + n * (64 + 12) + synth.desc.num_tiles * img
-    mlp_bytes_gather = samples * (GATHER_BYTES_PER_SAMPLE + 32 + 64 + 12) + chunks * img
+    mlp_bytes_compulsory = (dvert * (32 + 1) * 2 + samples * SAMPLE_RECORD_BYTES + n * (64 + 12)
+                            + synth.desc.num_tiles * img)
+    mlp_bytes_gather = samples * (GATHER_BYTES_PER_SAMPLE + SAMPLE_RECORD_BYTES + 64 + 12) + chunks * img
     t_mlp = stages["mlp_tc"] * 1e-3
     tflops = mlp_flop / t_mlp / 1e12
     gbs = mlp_bytes_compulsory / t_mlp / 1e9

@@ -142,7 +142,9 @@ snisr_status snisr_scene_set_mlp(snisr_scene* scene, const float* params_dev, vo
 /* per-frame op chain of FRender.render (rendering/src/__init__.py:246-341).  */
 /* ------------------------------------------------------------------------ */
 /* rgb_dev [H*W*3], depth_dev [H*W], opacity_dev [H*W] FP32 device buffers.
- * depth = sum_i w_i t_i (ray distance), opacity = 1 - final transmittance. */
+ * depth = sum_i w_i t_i (ray distance), opacity = 1 - final transmittance.
+ * The tensor-core form takes at most 2^24 rays per call (SNISR_INVALID_ARG
+ * beyond: its sample records hold a 24-bit pixel index). */
 snisr_status snisr_render(snisr_scene* scene, const snisr_camera* cam, int32_t form,
                           float* rgb_dev, float* depth_dev, float* opacity_dev,
                           void* stream);

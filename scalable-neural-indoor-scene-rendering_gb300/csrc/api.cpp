@@ -330,6 +330,8 @@ snisr_status render_impl(snisr_scene* sc, const CamDev* cam, const float* origin
   if (n == 0) return SNISR_OK;
   if (!rgb || !depth || !opac) return set_error(SNISR_INVALID_ARG, "render: output buffer is null");
   if (form != SNISR_FORM_PLAIN_FP32 && form != SNISR_FORM_TC) return set_error(SNISR_INVALID_ARG, "render: bad form");
+  if (form == SNISR_FORM_TC && n > kMaxBatchedRays)
+    return set_error(SNISR_INVALID_ARG, "render: the tensor-core form takes at most 2^24 rays per call");
   DeviceGuard guard(sc->device);
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t* ev = sc->profiling ? sc->ev : nullptr;

@@ -340,9 +340,7 @@ __global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S
         const uint32_t k = pre + (uint32_t)j;
         const uint32_t slot = k < rem ? base_old + k : nb + (k - rem);
         if (slot < cap) {
-          uint4* dst = reinterpret_cast<uint4*>(recs + slot);
-          dst[0] = make_uint4(vrec, ray_id, __float_as_uint(vw[j]), vtile);
-          dst[1] = make_uint4(__float_as_uint(vf[j][0]), __float_as_uint(vf[j][1]), __float_as_uint(vf[j][2]), 0u);
+          recs[slot] = pack_sample(vrec, ray_id, vw[j], vf[j]);
         } else {
           dropped = true;
         }
@@ -408,15 +406,27 @@ __global__ void scan_kernel(int* ctrl, int NT, uint32_t cap) {
 // single global atomic, and writes.  Slot s is valid iff s % 256 <
 // blk_count[s / 256] (per-warp blocks are filled in order; only each warp's
 // last block is partial).  Consecutive records of one tile keep their order
-// within a warp (samples of one voxel stay adjacent).
+// within a warp (samples of one voxel stay adjacent).  A record's tile is the
+// last tile whose first voxel id does not exceed the record's (binary search
+// over the tiles' first ids in shared memory).
 constexpr int kScatThreads = 256, kScatU = 4;
-__global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* __restrict__ recs, uint32_t cap,
-                                                               const uint32_t* __restrict__ blk_count, int* ctrl,
-                                                               int NT, SampleRec* sorted) {
-  extern __shared__ uint32_t sh_scat[];  // count[NT], base[NT]
+__global__ void __launch_bounds__(kScatThreads) scatter_kernel(SceneDev S, const SampleRec* __restrict__ recs,
+                                                               uint32_t cap, const uint32_t* __restrict__ blk_count,
+                                                               int* ctrl, int NT, SampleRec* sorted) {
+  extern __shared__ uint32_t sh_scat[];  // count[NT], base[NT], first voxel id[NT]
   uint32_t* scount = sh_scat;
   uint32_t* sbase = sh_scat + NT;
+  uint32_t* sfirst = sh_scat + 2 * NT;
   const int tid = threadIdx.x, lane = tid & 31;
+  for (int t = tid; t < NT; t += kScatThreads) sfirst[t] = S.occ[(size_t)t * S.words_per_tile].base;
+  auto tile_of = [&](uint32_t rec) {
+    int lo = 0, hi = NT;  // largest t with sfirst[t] <= rec
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (sfirst[mid] <= rec) lo = mid; else hi = mid;
+    }
+    return (uint32_t)lo;
+  };
   const uint32_t total = min((uint32_t)ctrl[CTRL_RESERVED], cap);
   const int* off = ctrl + CTRL_HEADER + NT;
   int* cursor = ctrl + CTRL_HEADER + NT + (NT + 1) + (NT + 1);
@@ -424,27 +434,24 @@ __global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* 
   for (uint32_t slab = blockIdx.x * kSlab; slab < total; slab += gridDim.x * kSlab) {
     for (int t = tid; t < NT; t += kScatThreads) scount[t] = 0;
     __syncthreads();
-    uint4 a[kScatU], b[kScatU];
-    uint32_t rank[kScatU];
+    uint4 a[kScatU];
+    uint32_t rank[kScatU], tl[kScatU];
     bool valid[kScatU];
 #pragma unroll
     for (int u = 0; u < kScatU; ++u) {
       const uint32_t sidx = slab + u * kScatThreads + tid;
       valid[u] = sidx < total && (sidx % kBlk) < __ldg(blk_count + sidx / kBlk);
-      if (valid[u]) {
-        const uint4* src = reinterpret_cast<const uint4*>(recs + sidx);
-        a[u] = __ldg(src);
-        b[u] = __ldg(src + 1);
-      }
+      if (valid[u]) a[u] = __ldg(reinterpret_cast<const uint4*>(recs + sidx));
     }
 #pragma unroll
     for (int u = 0; u < kScatU; ++u) {
       const unsigned m = __ballot_sync(kFull, valid[u]);
       if (valid[u]) {
-        const unsigned g = __match_any_sync(m, a[u].w);
+        tl[u] = tile_of(a[u].x);
+        const unsigned g = __match_any_sync(m, tl[u]);
         const int leader = __ffs(g) - 1;
         uint32_t r0 = 0;
-        if (lane == leader) r0 = atomicAdd(scount + a[u].w, (uint32_t)__popc(g));
+        if (lane == leader) r0 = atomicAdd(scount + tl[u], (uint32_t)__popc(g));
         r0 = __shfl_sync(g, r0, leader);
         rank[u] = r0 + __popc(g & lanemask_lt());
       }
@@ -456,10 +463,8 @@ __global__ void __launch_bounds__(kScatThreads) scatter_kernel(const SampleRec* 
 #pragma unroll
     for (int u = 0; u < kScatU; ++u) {
       if (valid[u]) {
-        const uint32_t t = a[u].w;
-        uint4* dst = reinterpret_cast<uint4*>(sorted + off[t] + sbase[t] + rank[u]);
-        dst[0] = a[u];
-        dst[1] = b[u];
+        const uint32_t t = tl[u];
+        *reinterpret_cast<uint4*>(sorted + off[t] + sbase[t] + rank[u]) = a[u];
       }
     }
     __syncthreads();  // counts are reset for the next slab
@@ -553,14 +558,9 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     r.cnt = min(128, __ldg(off + lo + 1) - r.row0);
     return r;
   };
-  auto load_row = [&](const ChunkRows& r, uint4& ra, uint4& rb) {
+  auto load_row = [&](const ChunkRows& r, uint4& ra) {
     ra = make_uint4(kInvalid, 0, 0, 0);
-    rb = make_uint4(0, 0, 0, 0);
-    if (r.c < total_chunks && tid < r.cnt) {
-      const uint4* src = reinterpret_cast<const uint4*>(sorted + r.row0 + tid);
-      ra = __ldg(src);
-      rb = __ldg(src + 1);
-    }
+    if (r.c < total_chunks && tid < r.cnt) ra = __ldg(reinterpret_cast<const uint4*>(sorted + r.row0 + tid));
   };
   // Software pipeline: while chunk c runs its MMA chain, the threads gather
   // chunk c + 1's A rows into registers, a share of the row groups during
@@ -588,13 +588,14 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     uint4 cv[8];
     uint4 e[NENC];
   };
-  auto gather_issue = [&](int it, const uint4& ra, const uint4& rb, Pending& p) {
+  auto gather_issue = [&](int it, const uint4& ra, Pending& p) {
     const int src = it * RPI + my_row;
     const uint32_t rec = __shfl_sync(kFull, ra.x, src);
-    const uint32_t ray = __shfl_sync(kFull, ra.y, src);
-    p.fx = __uint_as_float(__shfl_sync(kFull, rb.x, src));
-    p.fy = __uint_as_float(__shfl_sync(kFull, rb.y, src));
-    p.fz = __uint_as_float(__shfl_sync(kFull, rb.z, src));
+    const uint32_t ray = sample_pix(__shfl_sync(kFull, ra.y, src));
+    const uint32_t w_fx = __shfl_sync(kFull, ra.z, src), fy_fz = __shfl_sync(kFull, ra.w, src);
+    p.fx = sample_pos(w_fx >> 16);
+    p.fy = sample_pos(fy_fz & 0xFFFFu);
+    p.fz = sample_pos(fy_fz >> 16);
     p.valid = rec != kInvalid;
     if (p.valid) {
       const uint4* fp = S.feat16 + (size_t)rec * 8 * G + my_g;
@@ -653,8 +654,8 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
   }
   __syncthreads();
   ChunkRows cr = locate(chunk_slot[0]);
-  uint4 my_ra, my_rb;
-  load_row(cr, my_ra, my_rb);
+  uint4 my_ra;
+  load_row(cr, my_ra);
   bool w_pending = false;  // a weight image copy is in flight (block-uniform)
   if (cr.c < total_chunks) {
     // prologue: the first chunk's weights and rows
@@ -666,7 +667,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     w_pending = true;
 #pragma unroll
     for (int it = 0; it < G; ++it) {
-      gather_issue(it, my_ra, my_rb, pend);
+      gather_issue(it, my_ra, pend);
       gather_finish(it, pend);
     }
     tc::fence_proxy_async();
@@ -677,8 +678,8 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     const ChunkRows nx = locate(chunk_slot[(iter + 1) % 3]);
     const int cnt = cr.cnt;
     // this thread's output row (ray id, compositing weight)
-    const uint32_t my_ray = my_ra.y;
-    const float my_wt = __uint_as_float(my_ra.z);
+    const uint32_t my_ray = sample_pix(my_ra.y);
+    const float my_wt = sample_weight(my_ra.y, my_ra.z);
     if (w_pending) {
       // one thread polls the barrier; the others wait at bar.sync, which
       // keeps the shared-memory pipe free for the gathers of other CTAs
@@ -695,8 +696,8 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     // The next chunk's row groups are gathered alongside: group l's loads
     // are issued during layer l and interpolated during layer l + 1, when
     // the A tile (read only by layer 0) is free to take them.
-    uint4 nra, nrb;
-    load_row(nx, nra, nrb);
+    uint4 nra;
+    load_row(nx, nra);
     float out3[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int l = 0; l <= L; ++l) {
@@ -718,7 +719,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
         tc::mma_commit(mbar);
       }
       if (l >= 1 && l - 1 < G) gather_finish(l - 1, pend);  // layer 0 has read the A tile
-      if (l < G) gather_issue(l, nra, nrb, pend);
+      if (l < G) gather_issue(l, nra, pend);
       bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
       mphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
@@ -764,7 +765,7 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     // and any beyond one per layer)
 #pragma unroll
     for (int it = L; it < G; ++it) {
-      if (it > L) gather_issue(it, nra, nrb, pend);
+      if (it > L) gather_issue(it, nra, pend);
       gather_finish(it, pend);
     }
     tc::fence_proxy_async();
@@ -774,7 +775,6 @@ __global__ void __launch_bounds__(128, 4) mlp_tc_kernel(SceneDev S, const Sample
     }
     cr = nx;
     my_ra = nra;
-    my_rb = nrb;
   }
   bool drained = true;
   if (failed && tid == 0) {
@@ -902,8 +902,8 @@ cudaError_t launch_render_tc(const SceneDev& S, const Workspace& ws, int64_t n, 
   scan_kernel<<<1, 32, 0, st>>>(ws.ctrl, S.num_tiles, ws.cap);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], st)) != cudaSuccess) return e;
-  scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, kScatThreads, 2 * S.num_tiles * (int)sizeof(uint32_t),
-                   st>>>(ws.recs, ws.cap, ws.blk_count, ws.ctrl, S.num_tiles, ws.sorted);
+  scatter_kernel<<<num_sms * ws.tune.scatter_blocks_per_sm, kScatThreads, 3 * S.num_tiles * (int)sizeof(uint32_t),
+                   st>>>(S, ws.recs, ws.cap, ws.blk_count, ws.ctrl, S.num_tiles, ws.sorted);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[3], st)) != cudaSuccess) return e;
   const int F = S.feat_dim, H = S.mlp_hidden, L = S.mlp_layers;

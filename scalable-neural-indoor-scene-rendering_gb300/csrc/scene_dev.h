@@ -53,15 +53,34 @@ struct SceneDev {
 // either; the CTA kept its tensor memory and the context is unusable.
 enum : uint32_t { ERR_OVERFLOW = 1u, ERR_TIMEOUT = 2u, ERR_TMEM = 4u, ERR_DRAIN = 8u };
 
-// One compacted sample of the batched form (32 bytes).
+// One compacted sample of the batched form (16 bytes): the voxel's global
+// id (its tile follows from the id: tiles own consecutive id ranges); the
+// ray's pixel (24 bits) under the top 8 bits of the 24-bit compositing weight
+// w = T_i alpha_i; the weight's low 16 bits under the position inside the
+// voxel along x; the positions along y and z.  The weight keeps 16 of FP32's
+// 23 mantissa bits (rounded to nearest, relative error <= 2^-17), the
+// positions are 16-bit fixed point in [0, 1] (error <= 2^-17 voxel).
 struct __align__(16) SampleRec {
-  uint32_t rec;   // global voxel id, 0xFFFFFFFF for an unused slot
-  uint32_t ray;
-  float w;        // compositing weight T_i * alpha_i
-  uint32_t tile;
-  float f[3];     // position inside the voxel
-  uint32_t pad;
+  uint32_t rec;   // global voxel id
+  uint32_t pix_w;
+  uint32_t w_fx;
+  uint32_t fy_fz;
 };
+constexpr int64_t kMaxBatchedRays = 1 << 24;  // the 24-bit pixel field
+
+__host__ __device__ inline SampleRec pack_sample(uint32_t rec, uint32_t pix, float w, const float f[3]) {
+  union { float f; uint32_t u; } wb{w};
+  const uint32_t w24 = (wb.u + 0x40u) >> 7;  // w >= 0: sign bit 0
+  uint32_t q[3];
+  for (int a = 0; a < 3; ++a) q[a] = (uint32_t)(f[a] * 65535.0f + 0.5f);
+  return SampleRec{rec, pix | ((w24 >> 16) << 24), (w24 & 0xFFFFu) | (q[0] << 16), q[1] | (q[2] << 16)};
+}
+__host__ __device__ inline uint32_t sample_pix(uint32_t pix_w) { return pix_w & 0xFFFFFFu; }
+__host__ __device__ inline float sample_weight(uint32_t pix_w, uint32_t w_fx) {
+  union { uint32_t u; float f; } wb{(((pix_w >> 24) << 16) | (w_fx & 0xFFFFu)) << 7};
+  return wb.f;
+}
+__host__ __device__ inline float sample_pos(uint32_t q16) { return (float)q16 * (1.0f / 65535.0f); }
 
 // Control words of one batched frame (zeroed per frame).
 enum : int {
