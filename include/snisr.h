@@ -341,14 +341,17 @@ snisr_status snisr_op_inference_mlp(int32_t samples_per_ray, int32_t num_block, 
  * with soft_hit != 0 a pixel without a first hit whose last examined tile has
  * a group takes that group and 1 / (the tile's exit distance).
  * FP16 trilinear and compositing with the CUDA half intrinsics; tile ids
- * outside [0, num_tiles) are skipped. */
+ * outside [0, num_tiles) are skipped.  image_width > 0: the pixels are a
+ * row-major image that wide, marched in 4 x 8-pixel warp tiles where it
+ * divides into them (outputs identical); 0: pixel order. */
 snisr_status snisr_op_rendering_diffuse_octree(
     const float* rays_d_dev, const int32_t* visited_dev, int64_t npix, int32_t K,
     const float* origin_dev, const int32_t* group_map_dev, const uint16_t* data_voxels_dev,
     const int32_t* block_map_dev, const int16_t* node_map_dev, const uint8_t* sample_flags_dev,
     const int64_t* voxels_start_dev, const float* centers_dev, int32_t num_tiles, float tile_size,
     float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
-    int32_t soft_hit, float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, void* stream);
+    int32_t soft_hit, float* frame_dev, float* inverse_near_dev, int16_t* net_idx_dev, int32_t image_width,
+    void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Training-ray preparation of one tile from posed views (get_trainData_v3,  */

@@ -23,6 +23,7 @@
 #include <string>
 
 #include "device_common.cuh"
+#include "kernels.h"
 #include "snisr.h"
 #include "snisr_internal.h"
 
@@ -45,7 +46,7 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
                                       const uint8_t* __restrict__ flags, const int64_t* __restrict__ vstart,
                                       const float* __restrict__ centers, int num_tiles, float tile_size,
                                       float voxel_size, float sample_step, int D, __half trans_th, float early,
-                                      bool soft_hit, float* frame, float* inv_near, int16_t* net) {
+                                      bool soft_hit, float* frame, float* inv_near, int16_t* net, RayOrder ord) {
   const int DD = D * D, D3 = D * D * D;
   const float bs = fdiv(tile_size, (float)kOctBlocks);
   // float3 / float multiplies by the reciprocal (cutil_math.h:397-401)
@@ -53,7 +54,8 @@ __global__ void octree_diffuse_kernel(const float* __restrict__ rays_d, const in
   const __half early_h = __float2half(early);
   const __half one = __float2half(1.0f);
   const float o[3] = {__ldg(origin), __ldg(origin + 1), __ldg(origin + 2)};
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = ray_pixel(i, ord);  // this thread's pixel (warps march 4 x 8 pixel tiles of an image)
     const float d[3] = {rays_d[3 * p], rays_d[3 * p + 1], rays_d[3 * p + 2]};
     __half col[3] = {__float2half(0.f), __float2half(0.f), __float2half(0.f)};
     __half T = one;
@@ -196,7 +198,7 @@ extern "C" snisr_status snisr_op_rendering_diffuse_octree(
     const int32_t* group_map, const uint16_t* data_voxels, const int32_t* block_map, const int16_t* node_map,
     const uint8_t* sample_flags, const int64_t* voxels_start, const float* centers, int32_t num_tiles,
     float tile_size, float voxel_size, float sample_step, int32_t dilated_voxels, float trans_th, float early_stop,
-    int32_t soft_hit, float* frame, float* inverse_near, int16_t* net_idx, void* stream) {
+    int32_t soft_hit, float* frame, float* inverse_near, int16_t* net_idx, int32_t image_width, void* stream) {
   if (npix < 0 || K <= 0 || num_tiles <= 0 || dilated_voxels <= 1 || !(tile_size > 0) || !(voxel_size > 0) ||
       !(sample_step > 0))
     return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: bad size");
@@ -208,12 +210,18 @@ extern "C" snisr_status snisr_op_rendering_diffuse_octree(
     return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: null argument");
   if (reinterpret_cast<uintptr_t>(data_voxels) % 8 != 0)
     return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: data_voxels must be 8-byte aligned");
+  if (image_width < 0) return set_error(SNISR_INVALID_ARG, "rendering_diffuse_octree: negative image width");
+  // pixels [npix] of an image image_width wide (row-major): warps take 4 x 8
+  // pixel tiles when the image divides into them (outputs identical)
+  const RayOrder ord =
+      image_width > 0 && npix % image_width == 0 ? frame_ray_order(image_width, (int)(npix / image_width), npix)
+                                                 : RayOrder{};
   const int64_t blocks = (npix + 127) / 128;
   octree_diffuse_kernel<<<(int)(blocks < (1 << 20) ? blocks : (1 << 20)), 128, 0, (cudaStream_t)stream>>>(
       rays_d, visited, npix, K, origin, group_map,
       reinterpret_cast<const uint2*>(data_voxels), block_map, node_map, sample_flags, voxels_start, centers, num_tiles,
       tile_size, voxel_size, sample_step, dilated_voxels, __float2half(trans_th), early_stop, soft_hit != 0, frame,
-      inverse_near, net_idx);
+      inverse_near, net_idx, ord);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return set_error(SNISR_CUDA_ERROR, std::string("rendering_diffuse_octree: ") + cudaGetErrorString(e));

@@ -134,7 +134,7 @@ _SIGNATURES = {
     "snisr_op_inference_mlp_param_count": (C.c_int32, []),
     "snisr_op_rendering_diffuse_octree": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32,
                                                     C.c_float, C.c_float, C.c_float, C.c_int32, C.c_float, C.c_float,
-                                                    C.c_int32, P, P, P, P]),
+                                                    C.c_int32, P, P, P, C.c_int32, P]),
     "snisr_render_host_async": (C.c_int, [P, C.POINTER(Camera), C.c_int32, P, P, P, P]),
     "snisr_render_host_wait": (C.c_int, [P]),
     "snisr_op_train_rays": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P, P]),

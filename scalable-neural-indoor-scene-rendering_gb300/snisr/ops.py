@@ -246,7 +246,9 @@ def rendering_diffuse_octree_fp16(rays_d, visitedTiles, origin, groupMap, data_v
         voxels_start.data_ptr(), centers.data_ptr(), centers.shape[0], float(tile_size), float(voxel_size),
         float(sample_step), int(num_voxel), float(trans_th), float(early_stop), int(bool(soft_hit)),
         frame_diffuse.data_ptr(),
-        inverse_near.data_ptr(), netIdxs.data_ptr(), _stream()))
+        inverse_near.data_ptr(), netIdxs.data_ptr(),
+        frame_diffuse.shape[1] if frame_diffuse.dim() == 3 else 0,  # an [H, W, 3] frame: its width
+        _stream()))
 
 
 # ---------------------------------------------------------------------------

@@ -151,15 +151,18 @@ def test_op_argument_validation_without_cuda():
     assert L.snisr_op_inference_mlp(16, 4, 0.1, 0.01, None, 16, *bufs, None) == BAD
     # FP16 octree diffuse renderer
     oct_args = lambda npix, K, tile: (None, None, npix, K) + (None,) * 8 + (1, tile, 0.1, 0.02, 18, 0.8, 0.01, 0,
-                                                                           None, None, None, None)
+                                                                           None, None, None, 0, None)
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(0, 30, 6.4)) == OK
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 6.4)) == BAD  # null buffers
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 0, 6.4)) == BAD
     assert L.snisr_op_rendering_diffuse_octree(*oct_args(10, 30, 0.0)) == BAD
     tiny = lambda step: (fake, fake, 10, 30) + (fake,) * 8 + (1, 6.4, 0.1, step, 18, 0.8, 0.01, 0, fake, fake, fake,
-                                                              None)
+                                                              0, None)
     assert L.snisr_op_rendering_diffuse_octree(*tiny(1e-9)) == BAD  # step < voxel / 1024 would never advance z
     assert b"sample_step" in L.snisr_last_error_string()
+    neg_width = list(tiny(0.02))
+    neg_width[-2] = -1
+    assert L.snisr_op_rendering_diffuse_octree(*neg_width) == BAD
     # pruning
     assert L.snisr_op_transparency_statistic(None, None, 0, 18, None, 1.0, 0.0625, 0.006, None, None, None,
                                              None) == OK
