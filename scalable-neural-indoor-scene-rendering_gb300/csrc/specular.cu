@@ -167,18 +167,30 @@ __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
   return d;
 }
 
-// shared memory: A (16 KB, the position encodings: layer 0's operand) |
-// W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) | FP32 biases [6][64] (1.5 KB,
-// added by the epilogues) | barriers, slots: ~62 KB, three CTAs per SM.
-// Tensor memory (128 columns): the accumulator [0, 64) and the hidden
-// activations [64, 96) (FP16 pairs), the A operand of layers 1..5.
-constexpr int kSpA = 0, kSpW = 16384, kSpWout = kSpW + 5 * 8192, kSpBias = kSpWout + 4096,
-              kSpBars = kSpBias + 6 * 64 * 4, kSpSmem = kSpBars + 64;
+// One CTA = two groups of 4 warps sharing one copy of the network.  Shared
+// memory: W0..W4 (5 x 8 KB) | Wout (32 rows, 4 KB) | FP32 biases [6][64]
+// (1.5 KB, added by the epilogues) | per group an A tile (16 KB, the
+// position encodings: layer 0's operand) | per group and row the current
+// chunk's output slot, live flag and view direction (24 B) | barriers,
+// slots: ~86 KB, two CTAs per SM.  Tensor memory: per group 128 columns at 128 g, the
+// accumulator [0, 64) and the hidden activations [64, 96) (FP16 pairs), the
+// A operand of layers 1..5.
+constexpr int kSpGroups = 2;
+constexpr int kSpW = 0, kSpWout = kSpW + 5 * 8192, kSpBias = kSpWout + 4096,
+              kSpA = (kSpBias + 6 * 64 * 4 + 1023) & ~1023, kSpRows = kSpA + kSpGroups * 16384,
+              kSpBars = kSpRows + kSpGroups * 128 * 24, kSpSmem = kSpBars + 64;
+struct __align__(8) SpRowOut {  // a row's sample: output slot (-1: not live), view direction
+  int64_t ori;
+  float d[3];
+  float pad;
+};
+static_assert(sizeof(SpRowOut) == 24, "24-byte row slots");
 
-// pack network g's parameters (reference layout, FP16) into the swizzled tiles
-__device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
+// pack network g's parameters (reference layout, FP16) into the swizzled
+// tiles; threads tid of nth
+__device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid, int nth) {
   // hidden layers: row = output j, K = input i
-  for (int e = tid; e < kSpHidden * kSpH * (kSpH / 8); e += 128) {
+  for (int e = tid; e < kSpHidden * kSpH * (kSpH / 8); e += nth) {
     const int l = e / (kSpH * 8), j = (e / 8) % kSpH, c = e % 8;
     const int fi = l == 0 ? kSpIn : kSpH, off = sp_layer_off(l) + kSpH;
     uint32_t w[4];
@@ -192,7 +204,7 @@ __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
     *reinterpret_cast<uint4*>(sm + kSpW + l * 8192 + swz(j, 8 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
   // output layer: 32 rows (28 used)
-  for (int e = tid; e < 32 * 8; e += 128) {
+  for (int e = tid; e < 32 * 8; e += nth) {
     const int j = e / 8, c = e % 8, off = sp_layer_off(kSpHidden) + kSpOut;
     uint32_t w[4];
 #pragma unroll
@@ -206,7 +218,7 @@ __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
   }
   // biases (FP32), layer l at [l][64]; output layer: 28 used
   float* bias = reinterpret_cast<float*>(sm + kSpBias);
-  for (int e = tid; e < 6 * 64; e += 128) {
+  for (int e = tid; e < 6 * 64; e += nth) {
     const int l = e / 64, j = e % 64;
     float b = 0.f;
     if (l < kSpHidden) b = __half2float(P[sp_layer_off(l) + j]);
@@ -215,32 +227,40 @@ __device__ void pack_net(const __half* __restrict__ P, uint8_t* sm, int tid) {
   }
 }
 
-// One CTA: chunks of 128 samples of one network's pixel block.  Layer 0
-// reads the position encodings from shared memory; each hidden layer's
-// epilogue (bias, LeakyReLU, FP16 pack) writes its row of activations into
-// tensor memory with tcgen05.st, where the next layer's MMA reads its A
-// operand, so no activation goes through shared memory.  Software pipeline:
-// the next chunk's tasks are fetched during layer 0's MMA, and its encodings
-// computed and stored into the (then free) shared A tile during layer 1's.
-__global__ void __launch_bounds__(128, 3)
+// One CTA: chunks of 128 samples of one network's pixel block; group g of
+// the two takes chunks g, g + 2, g + 4, ... of the block, with its own A tile,
+// tensor memory, MMA issuer (its first thread), mbarrier and named barrier,
+// so that the groups' chains overlap.  Layer 0 reads the position encodings
+// from shared memory; each hidden layer's epilogue (bias, LeakyReLU, FP16
+// pack) writes its row of activations into tensor memory with tcgen05.st,
+// where the next layer's MMA reads its A operand.  Software pipeline: the
+// group's next chunk's tasks are fetched during layer 0's MMA, and its
+// encodings computed and stored into the (then free) A tile during layer
+// 1's.
+__global__ void __launch_bounds__(128 * kSpGroups, 2)
     inference_mlp_kernel(int spr, int num_block, float inv_far, float trans_stop, const int16_t* __restrict__ net,
                          int num_groups, const float* __restrict__ transparency, const int32_t* __restrict__ qpix,
                          const int32_t* __restrict__ pstarts, const float* __restrict__ centers,
                          const float* __restrict__ samples, const float* __restrict__ rays_d,
                          const __half* __restrict__ params, float4* results, int* work, uint32_t* err) {
+  constexpr int NTH = 128 * kSpGroups;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSpBars);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kSpGroups);
   int* blk_slot = reinterpret_cast<int*>(tmem_slot + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const uint32_t mbar = tc::smem_addr(bars);
+  const int tid = threadIdx.x, warp = tid >> 5, grp = warp >> 2, row = tid & 127;
+  const int leader = 128 * grp;
+  const uint32_t gbar = 1u + (uint32_t)grp;
+  const uint32_t mbar = tc::smem_addr(bars + grp);
+  uint8_t* A = sm + kSpA + grp * 16384;  // this group's A tile
+  SpRowOut* my_out = reinterpret_cast<SpRowOut*>(sm + kSpRows) + grp * 128 + row;  // this row's current sample
   if (tid == 0) {
-    tc::mbar_init(mbar, 1);
+    for (int g = 0; g < kSpGroups; ++g) tc::mbar_init(tc::smem_addr(bars + g), 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(tmem_slot), 128);
+    tc::tmem_alloc(tc::smem_addr(tmem_slot), 128 * kSpGroups);
     tc::tmem_relinquish();
   }
   tc::fence_proxy_async();
@@ -248,15 +268,16 @@ __global__ void __launch_bounds__(128, 3)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tact = tmem + kSpH;  // activation columns (A operand of layers 1..5)
-  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t gacc = tmem + 128u * (uint32_t)grp;  // the group's accumulator
+  const uint32_t tact = gacc + kSpH;                   // its activation columns (A operand of layers 1..5)
+  const uint32_t taddr = gacc + ((uint32_t)((warp & 3) * 32) << 16);
   const float* bias = reinterpret_cast<const float*>(sm + kSpBias);
-  const uint32_t a_base = tc::smem_addr(sm + kSpA);
+  const uint32_t a_base = tc::smem_addr(A);
   const uint32_t id_h = tc::idesc_f16(kSpH, 0), id_o = tc::idesc_f16(32, 0);
   uint32_t mphase = 0;
   int cur_net = -1;
   bool failed = false;
-  tc::Drain drain;
+  tc::Drain drain;  // on the group leaders: MMAs in flight at a timeout
   // The task of this thread's A row: its pixel, whether it is live, the
   // encoded position and the view direction.
   struct Task {
@@ -264,42 +285,48 @@ __global__ void __launch_bounds__(128, 3)
     int64_t ori;
     float p[3], d[3];
   };
-  // this thread's row of the shared A tile: the position encoding of task k
-  // (zeros when it is not live).  sin/cos of 2^i p (i = 0..9): one accurate
-  // sincos per coordinate, then double-angle steps (error ~2^9 x FP32
-  // rounding at i = 9, below half an FP16 ulp)
+  // this thread's row of the group's A tile: the position encoding of task k
+  // (zeros when it is not live), [p, sin(2^i p), cos(2^i p)] for i = 0..9.
+  // sin/cos of 2^i p: one accurate sincos per coordinate, then double-angle
+  // steps (error ~2^9 x FP32 rounding at i = 9, below half an FP16 ulp).  The
+  // 64 values are produced in order and stored 8 at a time (16-byte chunks).
   auto encode_row = [&](const Task& k) {
-    uint32_t h[32];
-    if (k.live) {
-      float x[64];
-      x[0] = k.p[0]; x[1] = k.p[1]; x[2] = k.p[2];
-      float sn[3], cs[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) sincosf(k.p[a], &sn[a], &cs[a]);
-#pragma unroll
-      for (int i = 0; i < 10; ++i) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          x[3 + 6 * i + a] = sn[a];
-          x[6 + 6 * i + a] = cs[a];
-          const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
-          sn[a] = s2;
-          cs[a] = c2;
-        }
+    float buf[8];
+    int nb = 0, chunk = 0;
+    auto emit = [&](float v) {
+      buf[nb++] = v;
+      if (nb == 8) {
+        *reinterpret_cast<uint4*>(A + tc::sw128_offset(row, chunk)) =
+            make_uint4(pack_h2(buf[0], buf[1]), pack_h2(buf[2], buf[3]), pack_h2(buf[4], buf[5]),
+                       pack_h2(buf[6], buf[7]));
+        ++chunk;
+        nb = 0;
       }
-      x[63] = 0.f;
+    };
+    const bool live = k.live;
+    float sn[3], cs[3];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) h[q] = pack_h2(x[2 * q], x[2 * q + 1]);
-    } else {
-#pragma unroll
-      for (int q = 0; q < 32; ++q) h[q] = 0u;
+    for (int a = 0; a < 3; ++a) {
+      emit(live ? k.p[a] : 0.f);
+      sincosf(live ? k.p[a] : 0.f, &sn[a], &cs[a]);
     }
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      *reinterpret_cast<uint4*>(sm + kSpA + tc::sw128_offset(tid, c)) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+    for (int i = 0; i < 10; ++i) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) emit(live ? sn[a] : 0.f);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) emit(live ? cs[a] : 0.f);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
+        sn[a] = s2;
+        cs[a] = c2;
+      }
+    }
+    emit(0.f);
   };
   for (;;) {
-    __syncthreads();  // every thread has read the previous slot value
+    __syncthreads();  // every thread has read the previous slot value; the network copy is free
     if (tid == 0) *blk_slot = atomicAdd(work, 1);
     __syncthreads();
     const int b = *blk_slot;
@@ -307,7 +334,7 @@ __global__ void __launch_bounds__(128, 3)
     const int g = net[b];
     if (g < 0 || g >= num_groups) continue;  // -1: no network (the reference returns); bad ids are skipped
     if (g != cur_net) {
-      pack_net(params + (size_t)g * kSpParams, sm, tid);
+      pack_net(params + (size_t)g * kSpParams, sm, tid, NTH);
       tc::fence_proxy_async();
       __syncthreads();
       cur_net = g;
@@ -316,7 +343,7 @@ __global__ void __launch_bounds__(128, 3)
     const int64_t t0 = (int64_t)pstarts[b] * spr, t1 = (int64_t)pstarts[b + 1] * spr;
     auto fetch = [&](int64_t c) {
       Task k;
-      const int64_t t = c + tid;
+      const int64_t t = c + row;
       k.live = t < t1;
       k.ori = 0;
       if (k.live) {
@@ -334,101 +361,118 @@ __global__ void __launch_bounds__(128, 3)
       }
       return k;
     };
-    Task cur = fetch(t0);
-    encode_row(cur);  // the block's first chunk
-    tc::fence_proxy_async();
-    for (int64_t c0 = t0; c0 < t1; c0 += 128) {
-      const bool more = c0 + 128 < t1;
-      __syncthreads();  // this chunk's A rows are visible to the MMA issuer
-      Task nxt;
-      nxt.live = false;
-      float out[32];
-      for (int l = 0; l <= kSpHidden; ++l) {
-        if (tid == 0) {
-          tc::fence_after_sync();
-          const bool last = l == kSpHidden;
-          const uint32_t wb = tc::smem_addr(sm + (last ? kSpWout : kSpW + l * 8192));
-          const uint32_t id = last ? id_o : id_h;
-          if (l == 0) {  // K = 64 position encodings from shared memory
-            for (int kk = 0; kk < 4; ++kk)
-              tc::mma_f16(tmem, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
-          } else {  // K = 64 activations from tensor memory (8 columns per K = 16 step)
-            for (int kk = 0; kk < 4; ++kk)
-              tc::mma_f16_ta(tmem, tact + 8 * kk, tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
-          }
-          tc::mma_commit(mbar);
-        }
-        if (l == 0 && more) nxt = fetch(c0 + 128);
-        if (l == 1 && more) {  // layer 0 has read the A tile: the next chunk's encodings
-          encode_row(nxt);
-          tc::fence_proxy_async();
-        }
-        const bool ok = tid == 0 ? tc::mbar_wait(mbar, mphase) : true;
-        mphase ^= 1u;
-        if (__syncthreads_or(!ok)) { failed = true; drain.set(mbar, mphase ^ 1u); break; }
-        tc::fence_after_sync();
-        if (l < kSpHidden) {
-          // bias + LeakyReLU + FP16 pack of 16 columns at a time into this
-          // row's lane of the activation columns
-#pragma unroll
-          for (int part = 0; part < kSpH / 16; ++part) {
-            float v[16];
-            tc::tmem_ld16(taddr + 16 * part, v);
-            tc::tmem_wait_ld();
-            uint32_t o[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int col = 16 * part + 2 * j;
-              float a0 = v[2 * j] + bias[64 * l + col], a1 = v[2 * j + 1] + bias[64 * l + col + 1];
-              a0 = a0 < 0.f ? 0.01f * a0 : a0;
-              a1 = a1 < 0.f ? 0.01f * a1 : a1;
-              o[j] = pack_h2(a0, a1);
-            }
-            tc::tmem_st8(taddr + kSpH + 8 * part, o);
-          }
-          tc::tmem_wait_st();
-        } else {
-          tc::tmem_ld16(taddr, out);
-          tc::tmem_ld16(taddr + 16, out + 16);
-          tc::tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < kSpOut; ++j) out[j] += bias[64 * kSpHidden + j];
-        }
+    // this group's chunks of the block: t0 + 128 grp, then every 128 x 2 rows
+    const int64_t gstart = t0 + 128 * grp, gstep = 128 * kSpGroups;
+    bool gfail = false;
+    // the row's sample of the current chunk, kept in shared memory for the
+    // output step (registers hold only the next chunk's task)
+    auto keep = [&](const Task& k) { *my_out = SpRowOut{k.live ? k.ori : -1, {k.d[0], k.d[1], k.d[2]}, 0.f}; };
+    if (gstart < t1) {
+      {
+        const Task first = fetch(gstart);
+        encode_row(first);
+        keep(first);
+      }
+      tc::fence_proxy_async();
+      for (int64_t c0 = gstart; c0 < t1; c0 += gstep) {
+        const bool more = c0 + gstep < t1;
         tc::fence_before_sync();
-        __syncthreads();
-      }
-      if (failed) break;
-      if (cur.live) {
-        const float dx = cur.d[0], dy = cur.d[1], dz = cur.d[2];
-        const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
-        const float X = dx * inv, Y = dy * inv, Z = dz * inv;
-        const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f;
-        const float C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
-                             0.5462742152960396f};
-        const float xx = X * X, yy = Y * Y, zz = Z * Z;
-        float rgb[3];
+        tc::bar_sync(gbar, 128);  // this chunk's A rows are visible to the group's MMA issuer
+        Task nxt;
+        nxt.live = false;
+        float out[32];
+        for (int l = 0; l <= kSpHidden; ++l) {
+          if (tid == leader) {
+            tc::fence_after_sync();
+            const bool last = l == kSpHidden;
+            const uint32_t wb = tc::smem_addr(sm + (last ? kSpWout : kSpW + l * 8192));
+            const uint32_t id = last ? id_o : id_h;
+            if (l == 0) {  // K = 64 position encodings from shared memory
+              for (int kk = 0; kk < 4; ++kk)
+                tc::mma_f16(gacc, tc::sdesc_sw128(a_base + 32 * kk), tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+            } else {  // K = 64 activations from tensor memory (8 columns per K = 16 step)
+              for (int kk = 0; kk < 4; ++kk)
+                tc::mma_f16_ta(gacc, tact + 8 * kk, tc::sdesc_sw128(wb + 32 * kk), id, kk > 0);
+            }
+            tc::mma_commit(mbar);
+          }
+          if (l == 0 && more) nxt = fetch(c0 + gstep);
+          if (l == 1 && more) {  // layer 0 has read the A tile: the next chunk's encodings
+            encode_row(nxt);
+            tc::fence_proxy_async();
+          }
+          const bool ok = tid == leader ? tc::mbar_wait(mbar, mphase) : true;
+          mphase ^= 1u;
+          if (tc::bar_or(gbar, 128, !ok)) {
+            gfail = true;
+            if (tid == leader) drain.set(mbar, mphase ^ 1u);
+            break;
+          }
+          tc::fence_after_sync();
+          if (l < kSpHidden) {
+            // bias + LeakyReLU + FP16 pack of 16 columns at a time into this
+            // row's lane of the activation columns
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          float v = C0 * out[i] - C1 * Y * out[3 + i] + C1 * Z * out[6 + i] - C1 * X * out[9 + i];
-          v += C2[0] * X * Y * out[12 + i] + C2[1] * Y * Z * out[15 + i] + C2[2] * (2.f * zz - xx - yy) * out[18 + i] +
-               C2[3] * X * Z * out[21 + i] + C2[4] * (xx - yy) * out[24 + i];
-          rgb[i] = 1.0f / (1.0f + expf(-v));
+            for (int part = 0; part < kSpH / 16; ++part) {
+              float v[16];
+              tc::tmem_ld16(taddr + 16 * part, v);
+              tc::tmem_wait_ld();
+              uint32_t o[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int col = 16 * part + 2 * j;
+                float a0 = v[2 * j] + bias[64 * l + col], a1 = v[2 * j + 1] + bias[64 * l + col + 1];
+                a0 = a0 < 0.f ? 0.01f * a0 : a0;
+                a1 = a1 < 0.f ? 0.01f * a1 : a1;
+                o[j] = pack_h2(a0, a1);
+              }
+              tc::tmem_st8(taddr + kSpH + 8 * part, o);
+            }
+            tc::tmem_wait_st();
+          } else {
+            tc::tmem_ld16(taddr, out);
+            tc::tmem_ld16(taddr + 16, out + 16);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < kSpOut; ++j) out[j] += bias[64 * kSpHidden + j];
+          }
+          tc::fence_before_sync();
+          tc::bar_sync(gbar, 128);
         }
-        results[cur.ori] = make_float4(rgb[0], rgb[1], rgb[2], fmaxf(out[kSpOut - 1], 0.f));
+        if (gfail) break;
+        const SpRowOut cur = *my_out;
+        if (cur.ori >= 0) {
+          const float dx = cur.d[0], dy = cur.d[1], dz = cur.d[2];
+          const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+          const float X = dx * inv, Y = dy * inv, Z = dz * inv;
+          const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f;
+          const float C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+                               0.5462742152960396f};
+          const float xx = X * X, yy = Y * Y, zz = Z * Z;
+          float rgb[3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            float v = C0 * out[i] - C1 * Y * out[3 + i] + C1 * Z * out[6 + i] - C1 * X * out[9 + i];
+            v += C2[0] * X * Y * out[12 + i] + C2[1] * Y * Z * out[15 + i] + C2[2] * (2.f * zz - xx - yy) * out[18 + i] +
+                 C2[3] * X * Z * out[21 + i] + C2[4] * (xx - yy) * out[24 + i];
+            rgb[i] = 1.0f / (1.0f + expf(-v));
+          }
+          results[cur.ori] = make_float4(rgb[0], rgb[1], rgb[2], fmaxf(out[kSpOut - 1], 0.f));
+        }
+        if (more) keep(nxt);
       }
-      cur = nxt;
     }
-    if (failed) break;
+    if (__syncthreads_or(gfail)) { failed = true; break; }
   }
   bool drained = true;
-  if (failed && tid == 0) {
-    if (err) atomicOr(err, kErrTimeout);
+  if (failed && tid % 128 == 0) {
+    if (err && tid == 0) atomicOr(err, kErrTimeout);
     drained = drain.run();
     if (!drained && err) atomicOr(err, kErrDrain);
   }
   tc::fence_before_sync();
   // tensor memory stays allocated when in-flight work did not drain
-  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 128);
+  if (__syncthreads_or(!drained) == 0 && warp == 0) tc::tmem_dealloc(tmem, 128 * kSpGroups);
 }
 
 }  // namespace
@@ -503,8 +547,8 @@ cudaError_t launch_inference_mlp(int spr, int num_block, float inv_far, float tr
   });
   if (e != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(work, 0, sizeof(int), st)) != cudaSuccess) return e;
-  const int grid = min(3 * num_sms, num_block);  // three CTAs per SM (shared memory ~63 KB each)
-  inference_mlp_kernel<<<grid, 128, smem, st>>>(spr, num_block, inv_far, trans_stop, net, num_groups, transparency,
+  const int grid = min(2 * num_sms, num_block);  // two CTAs of two groups per SM (shared memory ~80 KB each)
+  inference_mlp_kernel<<<grid, 128 * kSpGroups, smem, st>>>(spr, num_block, inv_far, trans_stop, net, num_groups, transparency,
                                                 qpix, pstarts, centers, samples, rays_d,
                                                 reinterpret_cast<const __half*>(params),
                                                 reinterpret_cast<float4*>(results), work, err);
