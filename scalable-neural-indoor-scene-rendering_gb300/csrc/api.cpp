@@ -500,6 +500,11 @@ snisr_status snisr_scene_create(const snisr_scene_desc* d, int32_t device, snisr
     std::vector<BvhNode> nodes;
     std::vector<int32_t> order;
     build_bvh(d->mesh_vertices, d->mesh_faces, d->num_triangles, 4, nodes, order);
+    // the traversal packs a node's child index / first triangle and count
+    // into one word: first < 2^27, count < 32
+    for (const BvhNode& nd : nodes)
+      if (nd.first < 0 || nd.first >= (1 << 27) || nd.count < 0 || nd.count > 31)
+        return fail(set_error(SNISR_INVALID_ARG, "scene_create: proxy mesh too large for the BVH node format"));
     std::vector<float> tri((size_t)d->num_triangles * 12);
     for (int64_t s = 0; s < d->num_triangles; ++s) {
       int32_t t = order[(size_t)s];

@@ -92,23 +92,36 @@ __device__ __forceinline__ bool box_hit(const float o[3], const float inv[3], co
 }
 
 // Nearest hit of the ray with the proxy mesh.  Returns the hit distance or
-// -1, and the original triangle id (or -1).
+// -1, and the original triangle id (or -1).  A node goes on the stack with
+// the distance at which the ray enters its box, tested when it was pushed,
+// and its child index / triangle range (first << 5 | count; leaves hold at
+// most 16 triangles): popped, it needs no load and only the comparison of
+// that distance with the current best (the box's exit passed the test when
+// pushed), the same test as re-testing the box.
 __device__ __forceinline__ float bvh_nearest(const SceneDev& S, const float o[3], const float d[3], int& tri_out) {
   float inv[3];
   for (int a = 0; a < 3; ++a) inv[a] = fdiv(1.0f, d[a]);
   float best = 3.0e38f;
   int best_id = -1;
-  int stack[64];
+  uint32_t stack[64];
+  float snear[64];
   int sp = 0;
-  stack[sp++] = 0;
-  while (sp > 0) {
-    int ni = stack[--sp];
-    BvhNodeDev nd = S.bvh[ni];
+  {
+    const BvhNodeDev r = S.bvh[0];
     float tn;
-    if (!box_hit(o, inv, nd.bmin, nd.bmax, best, tn)) continue;
-    if (nd.count > 0) {
-      for (int k = 0; k < nd.count; ++k) {
-        int slot = nd.first + k;
+    if (box_hit(o, inv, r.bmin, r.bmax, best, tn)) {
+      stack[0] = ((uint32_t)r.first << 5) | (uint32_t)r.count;
+      snear[0] = tn;
+      sp = 1;
+    }
+  }
+  while (sp > 0) {
+    --sp;
+    if (!(snear[sp] <= fmul(best, 1.0000005f))) continue;
+    const int first = (int)(stack[sp] >> 5), count = (int)(stack[sp] & 31u);
+    if (count > 0) {
+      for (int k = 0; k < count; ++k) {
+        int slot = first + k;
         float4 a4 = __ldg(S.tri + 3 * slot), b4 = __ldg(S.tri + 3 * slot + 1), c4 = __ldg(S.tri + 3 * slot + 2);
         float A[3] = {a4.x, a4.y, a4.z}, B[3] = {b4.x, b4.y, b4.z}, C[3] = {c4.x, c4.y, c4.z};
         float t;
@@ -118,16 +131,20 @@ __device__ __forceinline__ float bvh_nearest(const SceneDev& S, const float o[3]
         }
       }
     } else {
-      BvhNodeDev l = S.bvh[nd.first], r = S.bvh[nd.first + 1];
+      const BvhNodeDev l = S.bvh[first], r = S.bvh[first + 1];
       float tl, tr;
-      bool hl = box_hit(o, inv, l.bmin, l.bmax, best, tl);
-      bool hr = box_hit(o, inv, r.bmin, r.bmax, best, tr);
+      const bool hl = box_hit(o, inv, l.bmin, l.bmax, best, tl);
+      const bool hr = box_hit(o, inv, r.bmin, r.bmax, best, tr);
       if (sp + 2 > 64) { atomicOr(S.err, ERR_OVERFLOW); break; }
-      if (hl && hr) {
-        if (tl <= tr) { stack[sp++] = nd.first + 1; stack[sp++] = nd.first; }
-        else { stack[sp++] = nd.first; stack[sp++] = nd.first + 1; }
-      } else if (hl) stack[sp++] = nd.first;
-      else if (hr) stack[sp++] = nd.first + 1;
+      const uint32_t el = ((uint32_t)l.first << 5) | (uint32_t)l.count, er = ((uint32_t)r.first << 5) | (uint32_t)r.count;
+      if (hl && hr) {  // the nearer child on top
+        if (tl <= tr) { stack[sp] = er; snear[sp++] = tr; stack[sp] = el; snear[sp++] = tl; }
+        else { stack[sp] = el; snear[sp++] = tl; stack[sp] = er; snear[sp++] = tr; }
+      } else if (hl) {
+        stack[sp] = el; snear[sp++] = tl;
+      } else if (hr) {
+        stack[sp] = er; snear[sp++] = tr;
+      }
     }
   }
   tri_out = best_id;
