@@ -50,12 +50,12 @@ TRAIN_WORKLOAD = ("cfg3 training step (forward + backward): 1 tile of 256^3 over
 # summaries with their commands are under profiles/.
 SAMPLE_RECORD_BYTES = 16  # SampleRec: voxel id, 24-bit pixel + weight, 16-bit fixed-point position
 NCU_DRAM_BYTES_PER_LAUNCH = {
-    "mlp_tc": {"bytes": 335270042,
+    "mlp_tc": {"bytes": 226571827,
                "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of mlp_tc_kernel<32, 64, 3>, mean of the "
                          "5 launches (5 poses) of `bench.py --profile-run render --steps 2 --warmup 1` "
                          "(profiles/launches_render_cfg2.md)"},
-    "traverse": {"bytes": 193275546, "source": "same capture"},
-    "scatter": {"bytes": 350698496, "source": "same capture"},
+    "traverse": {"bytes": 88752588, "source": "same capture"},
+    "scatter": {"bytes": 154275891, "source": "same capture"},
 }
 
 
