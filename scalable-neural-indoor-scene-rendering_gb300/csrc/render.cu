@@ -248,12 +248,13 @@ __global__ void __launch_bounds__(128) render_plain_kernel(SceneDev S, const flo
 // transmittance and early stop do not wait for the MLP.
 // ---------------------------------------------------------------------------
 constexpr int kTravMaxThreads = 256;  // block size is a tuning knob (multiple of 32)
-// traverse_kernel is latency-bound: 3 resident 256-thread blocks' worth of
-// registers (at most 85 per thread; it uses 79) raise the resident warps
-// from 20 to 25 per SM, measured 8 % faster than the uncapped 99 registers.
+// traverse_kernel is issue-bound and latency-sensitive: 4 resident 256-thread
+// blocks' worth of registers (64 per thread, with some spilling) measured
+// 5 % faster than 3 (80 registers) on the 1920x1080 frame and the same on the
+// 1280x720 one; 2 (95 registers, no spills) was slower on both.
 constexpr uint32_t kBlk = 256;
 
-__global__ void __launch_bounds__(kTravMaxThreads, 3) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
+__global__ void __launch_bounds__(kTravMaxThreads, 4) traverse_kernel(SceneDev S, const float4* __restrict__ ray_o,
                                                                 const float4* __restrict__ ray_d, int64_t n,
                                                                 SampleRec* recs, uint32_t cap, uint32_t* blk_count,
                                                                 int* ctrl, float* depth, float* opac, RayOrder ord) {
