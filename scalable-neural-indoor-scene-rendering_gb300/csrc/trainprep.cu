@@ -113,6 +113,11 @@ __global__ void train_tracing_kernel(const float* __restrict__ ro, const float* 
 // Two nearest hits (with multiplicity) of the ray with the proxy mesh whose
 // points lie in the box c +- (h + kThresh).  BVH nodes are clipped to that
 // box before the slab test, so only the tile's part of the mesh is visited.
+// A node is tested when pushed and goes on the stack with its entry distance
+// and child index / triangle range (first << 5 | count), the nearer child on
+// top; popped, only that distance is compared with the current second hit
+// (the same test as re-testing the clipped box).  The result -- the two
+// smallest in-box hit distances -- does not depend on the visiting order.
 __device__ float2 bvh_two_nearest_in_box(const SceneDev& S, const float o[3], const float d[3], const float c[3],
                                          float h) {
   float inv[3], lo[3], hi[3];
@@ -123,12 +128,8 @@ __device__ float2 bvh_two_nearest_in_box(const SceneDev& S, const float o[3], co
     hi[a] = fadd(fadd(c[a], h), 2.0f * kThresh);
   }
   float near1 = SNISR_INF, near2 = SNISR_INF;
-  int stack[64];
-  int sp = 0;
-  stack[sp++] = 0;
-  while (sp > 0) {
-    const int ni = stack[--sp];
-    const BvhNodeDev nd = S.bvh[ni];
+  // the node's box clipped to the tile box, against [0, near2]
+  auto clipped_hit = [&](const BvhNodeDev& nd, float& tn) {
     float bmin[3], bmax[3];
     bool empty = false;
 #pragma unroll
@@ -137,11 +138,27 @@ __device__ float2 bvh_two_nearest_in_box(const SceneDev& S, const float o[3], co
       bmax[a] = fminf(nd.bmax[a], hi[a]);
       empty = empty || bmin[a] > bmax[a];
     }
+    return !empty && box_hit(o, inv, bmin, bmax, near2, tn);
+  };
+  uint32_t stack[64];
+  float snear[64];
+  int sp = 0;
+  {
+    const BvhNodeDev r = S.bvh[0];
     float tn;
-    if (empty || !box_hit(o, inv, bmin, bmax, near2, tn)) continue;
-    if (nd.count > 0) {
-      for (int k = 0; k < nd.count; ++k) {
-        const int slot = nd.first + k;
+    if (clipped_hit(r, tn)) {
+      stack[0] = ((uint32_t)r.first << 5) | (uint32_t)r.count;
+      snear[0] = tn;
+      sp = 1;
+    }
+  }
+  while (sp > 0) {
+    --sp;
+    if (!(snear[sp] <= fmul(near2, 1.0000005f))) continue;
+    const int first = (int)(stack[sp] >> 5), count = (int)(stack[sp] & 31u);
+    if (count > 0) {
+      for (int k = 0; k < count; ++k) {
+        const int slot = first + k;
         const float4 a4 = __ldg(S.tri + 3 * slot), b4 = __ldg(S.tri + 3 * slot + 1), c4 = __ldg(S.tri + 3 * slot + 2);
         const float A[3] = {a4.x, a4.y, a4.z}, B[3] = {b4.x, b4.y, b4.z}, Cc[3] = {c4.x, c4.y, c4.z};
         float t;
@@ -158,12 +175,22 @@ __device__ float2 bvh_two_nearest_in_box(const SceneDev& S, const float o[3], co
         }
       }
     } else {
+      const BvhNodeDev l = S.bvh[first], r = S.bvh[first + 1];
+      float tl, tr;
+      const bool hl = clipped_hit(l, tl), hr = clipped_hit(r, tr);
       if (sp + 2 > 64) {
         atomicOr(S.err, ERR_OVERFLOW);
         break;
       }
-      stack[sp++] = nd.first + 1;
-      stack[sp++] = nd.first;
+      const uint32_t el = ((uint32_t)l.first << 5) | (uint32_t)l.count, er = ((uint32_t)r.first << 5) | (uint32_t)r.count;
+      if (hl && hr) {
+        if (tl <= tr) { stack[sp] = er; snear[sp++] = tr; stack[sp] = el; snear[sp++] = tl; }
+        else { stack[sp] = el; snear[sp++] = tl; stack[sp] = er; snear[sp++] = tr; }
+      } else if (hl) {
+        stack[sp] = el; snear[sp++] = tl;
+      } else if (hr) {
+        stack[sp] = er; snear[sp++] = tr;
+      }
     }
   }
   return make_float2(near1, near2);
