@@ -554,6 +554,13 @@ snisr_status snisr_diag_wait_timeout(int64_t limit_ns, int64_t* waited_ns, void*
 snisr_status snisr_diag_march_math(int32_t fn, const float* x_dev, int64_t n, float* out_dev,
                                    void* stream);
 
+/* The scene's per-tile 4^3-block distances, on the host (no GPU): mask
+ * [(nb^3 + 31) / 32] bits of block occupancy (block (x, y, z) at bit
+ * (x nb + y) nb + z), out [nb^3] = the Chebyshev distance, in blocks, to the
+ * nearest occupied block (0 for an occupied one), at most 16.  The march
+ * crosses the box of blocks within distance - 1 without occupancy loads. */
+snisr_status snisr_diag_block_distance(const uint32_t* mask_host, int32_t nb, uint8_t* out_host);
+
 const char* snisr_last_error_string(void);
 const char* snisr_version(void);
 int32_t snisr_abi_version(void);

@@ -827,6 +827,12 @@ snisr_status snisr_scene_frame_footprint(snisr_scene* sc, int64_t* out, void* st
   return SNISR_OK;
 }
 
+snisr_status snisr_diag_block_distance(const uint32_t* mask, int32_t nb, uint8_t* out) {
+  if (!mask || !out || nb <= 0 || nb > 1024) return set_error(SNISR_INVALID_ARG, "diag_block_distance: bad argument");
+  block_distance(mask, nb, out);
+  return SNISR_OK;
+}
+
 snisr_status snisr_scene_get_tuning(const snisr_scene* sc, snisr_tuning* out) {
   if (check_scene(const_cast<snisr_scene*>(sc)) != SNISR_OK || !out)
     return set_error(SNISR_INVALID_ARG, "get_tuning: null argument");

@@ -160,6 +160,7 @@ _SIGNATURES = {
     "snisr_diag_mma": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, P]),
     "snisr_diag_wait_timeout": (C.c_int, [C.c_int64, C.POINTER(C.c_int64), P]),
     "snisr_diag_march_math": (C.c_int, [C.c_int32, P, C.c_int64, P, P]),
+    "snisr_diag_block_distance": (C.c_int, [P, C.c_int32, P]),
     "snisr_scene_set_profiling": (C.c_int, [P, C.c_int32]),
     "snisr_scene_stage_times": (C.c_int, [P, P, C.c_int32, P]),
     "snisr_scene_frame_stats": (C.c_int, [P, P, P]),
