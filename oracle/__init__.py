@@ -118,10 +118,10 @@ def _p(a: np.ndarray | None):
 
 
 # operand emulation of the tensor-core training form: "tc" is the kernels'
-# (three-part split BF16 forward for the colours, two-part split in the
-# backward's recomputation, single BF16 backward products); the others
-# attribute its error: the two-part split in both passes ("tc_split2"), its
-# forward or backward rounding alone, the three-part split in both passes
+# (three-part split BF16 forward whose activations the backward reuses,
+# exact biases, single BF16 backward products); the others attribute its
+# error: the two-part split ("tc_split2"), its forward or backward rounding
+# alone, the three-part split with three-part biases ("tc_split3")
 _EMUL = {None: 0, "tc": 5, "tc_split2": 1, "tc_forward": 2, "tc_backward": 3, "tc_split3": 4}
 
 

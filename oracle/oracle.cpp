@@ -843,33 +843,33 @@ struct TrainParams {
   const float* vdens;  // [NV]
   const float* mlp;    // [NT][P]
   // emul = 5: operand emulation of the tensor-core training form.  The
-  // forward pass that produces the colours splits its operands in three
-  // BF16 parts, v = hi + mid + lo (hi = bf16(v), mid = bf16(v - hi),
-  // lo = bf16(v - hi - mid)): MLP inputs, weights, biases and post-ReLU
-  // activations (rf).  A product of two split operands is taken down to the
-  // 2^-24 terms, hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid (six
-  // MMAs per K step).  The backward pass recomputes the activations with a
-  // two-part split, v = hi + lo and hi.hi + hi.lo + lo.hi (three MMAs);
-  // they set the ReLU masks and, rounded once more, the weight-gradient
-  // operands.  The colour pass adds the exact biases, the recomputation
-  // their three-part split.  Backward products use single BF16 operands (rb): the
-  // output-logit gradient, each hidden delta, W^T in the data gradient and
-  // the activation in the weight gradient.
-  // emul = 1: the two-part split in both passes; 4: the three-part split in
-  // both; 2 / 3: only the forward / only the backward rounding of emul = 1
-  // (these attribute the tensor-core form's error).
+  // forward pass splits its operands in three BF16 parts, v = hi + mid + lo
+  // (hi = bf16(v), mid = bf16(v - hi), lo = bf16(v - hi - mid)): MLP inputs,
+  // weights and post-ReLU activations (rf); biases are exact.  A product of
+  // two split operands is taken down to the 2^-24 terms, hi.hi + hi.mid +
+  // mid.hi + hi.lo + lo.hi + mid.mid (six MMAs per K step).  The backward
+  // takes the forward's activations (their hi parts are stored by the
+  // kernels): they set the ReLU masks and, rounded to BF16, the
+  // weight-gradient operands.  Backward products use single BF16 operands
+  // (rb): the output-logit gradient, each hidden delta, W^T in the data
+  // gradient and the activation in the weight gradient.
+  // emul = 1: the two-part split (v = hi + lo, three products) with
+  // two-part biases; 4: emul = 5 with three-part biases; 2 / 3: only the
+  // forward / only the backward rounding of emul = 1 (these attribute the
+  // tensor-core form's error).
   int emul = 0;
   // parts of the forward operand split: 0 (exact), 2 or 3; `colour` selects
-  // the pass that produces the colours, otherwise the backward's recomputation
+  // the pass that produces the colours, otherwise the one whose activations
+  // the backward uses (the same pass in every mode now)
   int split(bool colour) const {
+    (void)colour;
     switch (emul) {
       case 1: case 2: return 2;
-      case 4: return 3;
-      case 5: return colour ? 3 : 2;
+      case 4: case 5: return 3;
       default: return 0;
     }
   }
-  int bias_split(bool colour) const { return emul == 5 ? (colour ? 0 : 3) : split(colour); }
+  int bias_split(bool colour) const { return emul == 5 ? 0 : split(colour); }
   bool bwd_r() const { return emul == 1 || emul == 3 || emul == 4 || emul == 5; }
   static double rf(double v, int parts) {
     if (parts == 0) return v;

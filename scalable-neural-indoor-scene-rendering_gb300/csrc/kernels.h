@@ -141,6 +141,7 @@ struct TrainTcArgs {
   float* gstage;  // [NT][4][64 x 64 + 64] weight-gradient staging of the backward kernel
   int num_sms;
   int fwd_warps;
+  uint8_t* htiles;  // [128-row chunks][L][16 KB] the forward's hidden activations (hi, swizzled)
 };
 int train_tc_image_bytes(int H, int L);
 int train_tc_bwd_smem_bytes(int H, int L);

@@ -535,8 +535,12 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   const int64_t rays = n, cap = n * (int64_t)msr, nb = (rays + 1023) / 1024 + 2;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const int img_stride = (train_tc_image_bytes(64, 3) + 127) & ~127;
+  // T->act holds the plain form's per-sample activations or the TC form's
+  // activation tiles (3 hidden layers x 16 KB per 128-row chunk; at most
+  // cap / 128 + NT chunks): the larger of the two
+  const size_t act_bytes = std::max((size_t)cap * kActStride * 4, ((size_t)cap / 128 + NT + 1) * 3 * 16384);
   size_t sz = al(rays * 4) * 2 + al(nb * 4) + al(16) + al((NT + 2) * 4) + al(cap * sizeof(TrainRec)) +
-              al(cap * 16) * 2 + al(cap * kActStride * 4) + al(cap * kDltStride * 4) + al(2 * (NT + 2) * 4) + al(16) +
+              al(cap * 16) * 2 + al(act_bytes) + al(cap * kDltStride * 4) + al(2 * (NT + 2) * 4) + al(16) +
               al(rays * 192) + al((size_t)img_stride * NT) + al((size_t)rays * kStage * sizeof(TrainRec)) +
               al((size_t)nvox * 32) + al((size_t)NT * 4 * (64 * 64 + 64) * 4);
   void* p = nullptr;
@@ -552,7 +556,7 @@ snisr_status train_ws_reserve(TrainWS* T, int64_t n, int msr, int NT, int64_t nv
   T->recs = (TrainRec*)take(cap * sizeof(TrainRec));
   T->c = (float4*)take(cap * 16);
   T->dout = (float4*)take(cap * 16);
-  T->act = (float*)take(cap * kActStride * 4);
+  T->act = (float*)take(act_bytes);  // plain form: activations per sample; TC form: activation tiles
   T->dlt = (float*)take(cap * kDltStride * 4);
   T->coff = (int32_t*)take(2 * (NT + 2) * 4);  // chunk offsets per tile: 128-row chunks, then 256-row units
   T->work = (int*)take(16);
@@ -646,7 +650,8 @@ extern "C" snisr_status snisr_train_forward(snisr_scene* sc, const float* vfeat,
   cudaError_t e;
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, nullptr, nullptr, nullptr, num_sms, ws.tune.train_fwd_warps};
+                  T->c, T->dout, nullptr, nullptr, nullptr, num_sms, ws.tune.train_fwd_warps,
+                  reinterpret_cast<uint8_t*>(T->act)};
     e = launch_train_tc(S, a, false, st);
     if (e == cudaErrorInvalidValue) return set_error(SNISR_UNSUPPORTED, "train_forward: MLP shape not built for training");
   } else if (F == 32 && H == 64 && L == 3) e = train_plain_mlp_fwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->c, num_sms, st);
@@ -701,7 +706,8 @@ extern "C" snisr_status snisr_train_backward(snisr_scene* sc, const float* vfeat
   if (T->last_form != form) return set_error(SNISR_INVALID_ARG, "train_backward: the forward call used another form");
   if (form != SNISR_FORM_PLAIN_FP32) {
     TrainTcArgs a{vfeat, mlp, dirs, n, T->recs, T->tstart, T->coff, T->work, T->enc, T->wimg, T->img_stride,
-                  T->c, T->dout, gvfeat, gmlp, T->gstage, num_sms, ws.tune.train_fwd_warps};
+                  T->c, T->dout, gvfeat, gmlp, T->gstage, num_sms, ws.tune.train_fwd_warps,
+                  reinterpret_cast<uint8_t*>(T->act)};
     e = launch_train_tc(S, a, true, st);
   } else if (F == 32 && H == 64 && L == 3)
     e = train_plain_mlp_bwd<32, 64, 3>(S, vfeat, mlp, T->recs, T->total, T->cap, dirs, T->dout, T->act, T->dlt, gvfeat,

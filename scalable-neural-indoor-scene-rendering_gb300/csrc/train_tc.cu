@@ -17,14 +17,12 @@
 // as accurate as an FP32 evaluation.  The colours feed the loss, whose
 // residuals near convergence are small: a two-part split (~2^-17 per
 // operand) moved the loss gradient of the MLP parameters by ~1 %.  The
-// backward's recomputation of the activations uses the two-part split
-// v = hi + mid, A_hi.B_hi + A_mid.B_hi + A_hi.B_mid (about 16 significant
-// bits): it only sets the ReLU masks, which then follow an FP32 evaluation
-// except within ~2^-16 of a kink, and the weight-gradient operands, which
-// are rounded to BF16 anyway.  The colour pass adds the FP32 biases; the
-// recomputation takes them in three BF16 parts.
-// Backward products (hidden deltas, weight gradients) use single BF16
-// operands: their rounding error is smooth (~2^-9 per operand).
+// biases enter in FP32.  The forward stores the hi parts of its hidden
+// activations (16 KB per layer and 128-sample chunk, in the swizzled tile
+// layout), and the backward loads them instead of recomputing: they give
+// the ReLU masks and the weight-gradient operands.  Backward products
+// (hidden deltas, weight gradients) use single BF16 operands: their
+// rounding error is smooth (~2^-9 per operand).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -42,8 +40,6 @@ struct __align__(16) TrainRecT {  // mirror of the record written by the march k
   float T, alpha, s, pad1;
 };
 
-constexpr uint32_t kBf16Eighth = 0x3E003E00u;  // 1/8, two lanes
-constexpr uint32_t kBf16Quarter = 0x3E803E80u; // 1/4, two lanes
 constexpr uint32_t kBf16One = 0x3F803F80u;     // 1.0, two lanes
 
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
@@ -92,24 +88,17 @@ __device__ __forceinline__ uint32_t idesc_bf16(int n, bool a_mn, bool b_mn) {
 // All sub-tiles K-major, 128-byte swizzled, 64 K columns:
 //   hi part : W_l [H][64] (l < L), W_out [16][64]
 //   mid part: the same shapes holding bf16(w - hi)
-//   bias    : [H][64], K slice 16l..16l+15 of row o = 8 x hi, 4 x mid, 4 x lo
-//             of b_l[o] (the MMA's A operand is 1/8 in K columns 0..7 and
-//             1/4 in 8..15, so that the slice sums to hi + mid + lo)
-//   out bias: [16][64], K slice 0..15 likewise for the output layer
 //   W^T     : per layer l <= L, [64 rows = inputs of l][K = outputs] (hi only)
 //   lo part : the shapes of the hi part holding bf16(w - hi - mid)
 //   FP32 biases: per layer l <= L, 64 floats
-// The backward's copy ends at the W^T part (bwd_bytes); the forward copies
-// the hi and mid parts, then the lo part and the FP32 biases.
+// The forward copies the hi and mid parts, then the lo part and the FP32
+// biases; the backward copies the W^T part [t_off, bwd_bytes).
 struct ImageLayout {
-  int hi_part, mid_off, bias_off, obias_off, fwd_bytes, t_off, bwd_bytes, lo_off, fbias_off, total;
+  int hi_part, mid_off, t_off, bwd_bytes, lo_off, fbias_off, total;
   __host__ __device__ ImageLayout(int H, int L) {
     hi_part = L * H * 128 + 2048;
     mid_off = hi_part;
-    bias_off = 2 * hi_part;
-    obias_off = bias_off + H * 128;
-    fwd_bytes = obias_off + 2048;
-    t_off = fwd_bytes;
+    t_off = 2 * hi_part;
     bwd_bytes = t_off + (L + 1) * 8192;
     lo_off = bwd_bytes;
     fbias_off = lo_off + hi_part;
@@ -136,7 +125,6 @@ __global__ void pack_train_weights(const float* __restrict__ mlp, int P, int IN,
     uint8_t* whi = img + wofs;
     uint8_t* wmid = img + lay.mid_off + wofs;
     uint8_t* wlo = img + lay.lo_off + wofs;
-    uint8_t* btile = img + (l < L ? lay.bias_off : lay.obias_off);
     uint8_t* tt = img + lay.t_off + l * 8192;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * fi; e += gridDim.x * blockDim.x) {
       const int o = e / fi, i = e % fi;
@@ -147,13 +135,8 @@ __global__ void pack_train_weights(const float* __restrict__ mlp, int P, int IN,
       *reinterpret_cast<uint16_t*>(wlo + sw_off(o, i)) = lo;
       *reinterpret_cast<uint16_t*>(tt + sw_off(i, o)) = h;
     }
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fo * 16; e += gridDim.x * blockDim.x) {
-      const int o = e / 16, k = e % 16;
-      uint16_t h, m, lo;
-      split3_bf16(p[off + (int64_t)fi * fo + o], h, m, lo);
-      *reinterpret_cast<uint16_t*>(btile + sw_off(o, (l < L ? 16 * l : 0) + k)) = k < 8 ? h : k < 12 ? m : lo;
-      if (k == 0) reinterpret_cast<float*>(img + lay.fbias_off)[64 * l + o] = p[off + (int64_t)fi * fo + o];
-    }
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < fo; o += gridDim.x * blockDim.x)
+      reinterpret_cast<float*>(img + lay.fbias_off)[64 * l + o] = p[off + (int64_t)fi * fo + o];
     off += (int64_t)fi * fo + fo;
   }
 }
@@ -174,16 +157,6 @@ __global__ void ray_enc_kernel(const float* __restrict__ dirs, int64_t n, uint4*
       enc[kEncQuads * i + 4 + q] = make_uint4(m[0], m[1], m[2], m[3]);
       enc[kEncQuads * i + 8 + q] = make_uint4(l[0], l[1], l[2], l[3]);
     }
-  }
-}
-
-// the A operand of the bias MMAs: 8 rows of 64 K columns (128-byte swizzle),
-// 1/8 in K columns 0..7 and 1/4 in 8..15 of every 16-column slice
-__device__ __forceinline__ void init_bias_ones(uint8_t* ones, int tid, int nth) {
-  for (int k = tid; k < 64; k += nth) {
-    const int r = k >> 3, c = (k & 7) ^ r;  // 16-byte chunk k of the tile holds K chunk c of row r
-    const uint32_t v = (c & 1) ? kBf16Quarter : kBf16Eighth;
-    reinterpret_cast<uint4*>(ones)[k] = make_uint4(v, v, v, v);
   }
 }
 
@@ -221,7 +194,7 @@ __device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* coff, const 
 }
 
 // Gather of the split input rows [0,128) of the chunk into the NP part tiles
-// X[0..NP) (hi, mid and, for NP = 3, lo): lane (g, row) interpolates 8 FP32
+// X[0..NP) (hi; mid for NP >= 2; lo for NP = 3): lane (g, row) interpolates 8 FP32
 // channels over the 8 corners of each of its rows; view encoding copied from
 // the per-ray split table.  Loads are issued in stages across the lane's rows
 // (records, then corner ids and encodings, then features) so that each stage
@@ -239,7 +212,7 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
   // NW warps share the 128 rows: RPW rows per warp, RPI rows per lane pass
   constexpr int G = F / 8, RPI = 32 / G, RPW = 128 / NW, ITS = RPW / RPI;
   static_assert(RPW % RPI == 0, "rows per warp must be a multiple of rows per pass");
-  static_assert(NP == 2 || NP == 3, "two or three parts");
+  static_assert(NP >= 1 && NP <= 3, "one to three parts");
   const int my_g = lane / RPI, my_row = lane % RPI;
   const uint4 z = make_uint4(0, 0, 0, 0);
   uint4 head[ITS], fr[ITS];  // {rec, ray, tile, pad}, {f0, f1, f2, dv}
@@ -300,8 +273,10 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
       for (int j = 0; j < 4; ++j) {
         if (NP == 3)
           split3_bf2(acc[2 * j], acc[2 * j + 1], pv[0][j], pv[1][j], pv[2][j]);
-        else
+        else if (NP == 2)
           split_bf2(acc[2 * j], acc[2 * j + 1], pv[0][j], pv[1][j]);
+        else
+          pv[0][j] = pack_bf2(acc[2 * j], acc[2 * j + 1]);
       }
 #pragma unroll
       for (int q = 0; q < NP; ++q)
@@ -331,30 +306,6 @@ __device__ __forceinline__ void gather_x(const SceneDev& S, const float* __restr
   }
 }
 
-// ReLU + two-part split BF16 pack of one of NC column parts of a 128 x H
-// accumulator (H / NC columns, a multiple of 16; part p covers
-// [p H / NC, (p + 1) H / NC)) into the hi and mid activation tiles (dst_mid
-// may be null: hi only)
-template <int H, int NC>
-__device__ __forceinline__ void epi_relu_split(uint32_t taddr, uint8_t* dst_hi, uint8_t* dst_mid, int row, int part) {
-  constexpr int CP = H / NC;
-  static_assert(CP % 16 == 0, "column parts of 16");
-  float v[CP];
-#pragma unroll
-  for (int j = 0; j < CP; j += 16) tc::tmem_ld16(taddr + part * CP + j, v + j);
-  tc::tmem_wait_ld();
-#pragma unroll
-  for (int q = 0; q < CP / 8; ++q) {
-    const int chunk = part * (CP / 8) + q;
-    uint32_t h[4], m[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      split_bf2(fmaxf(v[8 * q + 2 * j], 0.f), fmaxf(v[8 * q + 2 * j + 1], 0.f), h[j], m[j]);
-    *reinterpret_cast<uint4*>(dst_hi + tc::sw128_offset(row, chunk)) = make_uint4(h[0], h[1], h[2], h[3]);
-    if (dst_mid) *reinterpret_cast<uint4*>(dst_mid + tc::sw128_offset(row, chunk)) = make_uint4(m[0], m[1], m[2], m[3]);
-  }
-}
-
 struct Bars {
   uint32_t wbar, mbar;
   uint32_t wphase, mphase;
@@ -366,24 +317,6 @@ __device__ __forceinline__ bool wait_mma(Bars& b, int tid) {
   ok = !__syncthreads_or(!ok);
   tc::fence_after_sync();
   return ok;
-}
-
-// One two-part split layer of the backward's recomputation: tmem = A.W^T +
-// bias with N = n outputs, K = 16 * ksteps: A_hi.W_hi + A_mid.W_hi +
-// A_hi.W_mid, then the bias step (A = 1/8 in K columns 0..7 and 1/4 in
-// 8..15, B slice = 8 x hi, 4 x mid, 4 x lo of the bias).
-__device__ __forceinline__ void issue_split_layer(uint32_t tmem, uint32_t a_hi, uint32_t a_mid, uint32_t w_hi,
-                                                  uint32_t w_mid, uint32_t bias_slice, uint64_t ones8, int n,
-                                                  int ksteps) {
-  const uint32_t id = idesc_bf16(n, false, false);
-  for (int kk = 0; kk < ksteps; ++kk) {
-    const uint64_t ah = tc::sdesc_sw128(a_hi + 32 * kk), am = tc::sdesc_sw128(a_mid + 32 * kk);
-    const uint64_t wh = tc::sdesc_sw128(w_hi + 32 * kk), wm = tc::sdesc_sw128(w_mid + 32 * kk);
-    tc::mma_f16(tmem, ah, wh, id, kk > 0);
-    tc::mma_f16(tmem, am, wh, id, 1);
-    tc::mma_f16(tmem, ah, wm, id, 1);
-  }
-  tc::mma_f16(tmem, ones8, tc::sdesc_sw128(bias_slice), id, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -470,10 +403,11 @@ template <int F, int H, int L, int NG>
 __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const float* __restrict__ vfeat,
                                                              const TrainRecT* __restrict__ recs,
                                                              const int32_t* __restrict__ tstart,
-                                                             const int32_t* __restrict__ uoff, int* work,
+                                                             const int32_t* __restrict__ uoff,
+                                                             const int32_t* __restrict__ coff, int* work,
                                                              const uint4* __restrict__ enc,
                                                              const uint8_t* __restrict__ wimg, int img_stride,
-                                                             float4* cout) {
+                                                             float4* cout, uint8_t* htiles) {
   constexpr int KH = H / 16, NTMEM = NG == 1 ? 256 : 512;
   static_assert(NG == 1 || NG == 2, "one or two groups");
   static_assert(KH % 2 == 0 && H <= 64, "two hi.hi accumulators of up to 64 columns");
@@ -521,6 +455,10 @@ __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const f
     if (c >= total) break;
     const ChunkPos cp = chunk_pos(c, uoff, tstart, NT, 128 * NG);
     const int my_cnt = min(128, cp.cnt - 128 * grp);  // rows of this group (uniform per group)
+    // this group's 128-row chunk in the backward's chunk list (units of NG
+    // chunks start at the same rows), where its hidden activations go
+    const int my_chunk = NG == 1 ? c : __ldg(coff + cp.tile) + NG * (c - __ldg(uoff + cp.tile)) + grp;
+    uint8_t* my_htiles = htiles + (size_t)my_chunk * L * 16384;
     const bool new_w = cp.tile != cur_tile;
     if (new_w && tid == 0) {
       const uint8_t* img = wimg + (size_t)cp.tile * img_stride;
@@ -556,6 +494,9 @@ __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const f
           const uint32_t w3[3] = {w + wofs, w + lay.hi_part + wofs, w + 2 * lay.hi_part + wofs};
           issue_fwd_layer(gacc, a3, w3, l < L ? H : 16, l == 0 ? 4 : KH);
           tc::mma_commit(mbar);
+          // the previous layer's activation tile has been read out before
+          // this layer's epilogue overwrites it
+          if (l > 0) tc::bulk_wait_read();
         }
         const bool ok = tid == leader ? tc::mbar_wait(mbar, mphase) : true;
         mphase ^= 1u;
@@ -575,6 +516,10 @@ __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const f
         }
         tc::fence_before_sync();
         tc::bar_sync(gbar, 128);
+        if (l < L && tid == leader) {  // the hi activations of hidden layer l, for the backward
+          tc::bulk_s2g(my_htiles + (size_t)l * 16384, a3[0], 16384u);
+          tc::bulk_commit();
+        }
       }
     }
     if (__syncthreads_or(gfail)) { failed = true; break; }
@@ -582,6 +527,7 @@ __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const f
       cout[cp.row0 + 128 * grp + row] =
           make_float4(sigmoidf_(out3[0]), sigmoidf_(out3[1]), sigmoidf_(out3[2]), 0.f);
   }
+  if (tid == leader) tc::bulk_wait_all();  // the activation tiles are written
   bool drained = true;
   if (failed && tid % 128 == 0) {
     if (tid == 0) atomicOr(S.err, ERR_TIMEOUT);
@@ -600,9 +546,9 @@ __global__ void __launch_bounds__(128 * NG, 1) tr_mlp_fwd_tc(SceneDev S, const f
 // accumulator (column 0 used), both living across the chunks of a tile.
 //
 // Shared memory tiles (16 KB, one sample per 128-byte row), in this order:
-//   D (hidden delta), X (input hi), H1..HL (activation hi), DO (output-logit
-//   gradient), MidA, MidB (the mid parts of the recomputation's two-part
-//   split operands, ping-pong).
+//   D (hidden delta), X (input hi), H1..HL (activation hi: the forward's,
+//   bulk-loaded per chunk), DO (output-logit gradient); then the weight
+//   image's W^T part.
 // An MN-major M = 128 operand spans two 64-wide atoms 16 KB apart: for D and
 // DO the second atom is the next tile, whose products land in accumulator
 // lanes 64..127 (output units that do not exist) and are never read.
@@ -644,9 +590,9 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
                                                         const int32_t* __restrict__ coff, int* work,
                                                         const uint4* __restrict__ enc, const uint8_t* __restrict__ wimg,
                                                         int img_stride, const float4* __restrict__ dout, float* gvfeat,
-                                                        float* gstage) {
+                                                        float* gstage, const uint8_t* __restrict__ htiles) {
   constexpr int IN = F + 27;
-  constexpr int kTiles = 5 + L;
+  constexpr int kTiles = 3 + L;
   const ImageLayout lay(H, L);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -654,12 +600,11 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   uint8_t* Xt = base + 16384;
   uint8_t* Ht = base + 2 * 16384;  // H_l at Ht + (l-1)*16384, l = 1..L
   uint8_t* DOt = base + (2 + L) * 16384;
-  uint8_t* MidA = DOt + 16384;
-  uint8_t* MidB = MidA + 16384;
-  uint8_t* Wsm = base + kTiles * 16384;
-  uint8_t* ones = Wsm + ((lay.bwd_bytes + 1023) & ~1023);  // 1 KB bias-step A operand, 1 KB of 1.0
-  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 2048);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  uint8_t* Wsm = base + kTiles * 16384;  // the weight image's W^T part
+  const int wt_bytes = lay.bwd_bytes - lay.t_off;
+  uint8_t* ones = Wsm + ((wt_bytes + 1023) & ~1023);  // 1 KB of 1.0
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ones + 1024);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
   int* chunk_slot = reinterpret_cast<int*>(tmem_slot + 1);
   // 8 warps: warps w and w + 4 read the same tensor-memory lane quarter
   // (rows 32 (w % 4) ..) and split the accumulator columns (part = w / 4)
@@ -667,18 +612,20 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   const int row = tid & 127, part = tid >> 7;
   const int NT = S.num_tiles;
   Bars B{tc::smem_addr(bars), tc::smem_addr(bars + 1), 0u, 0u};
+  const uint32_t hbar = tc::smem_addr(bars + 2);  // the chunk's activation tiles
+  uint32_t hphase = 0;
   if (tid == 0) {
     tc::mbar_init(B.wbar, 1);
     tc::mbar_init(B.mbar, 1);
+    tc::mbar_init(hbar, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
     tc::tmem_alloc(tc::smem_addr(tmem_slot), 512);
     tc::tmem_relinquish();
   }
-  init_bias_ones(ones, tid, 256);
   for (int k = tid; k < 64; k += 256)
-    reinterpret_cast<uint4*>(ones + 1024)[k] = make_uint4(kBf16One, kBf16One, kBf16One, kBf16One);
+    reinterpret_cast<uint4*>(ones)[k] = make_uint4(kBf16One, kBf16One, kBf16One, kBf16One);
   // all tiles start zeroed: DO columns beyond 3 and the columns beyond H of
   // the activation / delta tiles are never written afterwards
   for (int k = tid; k < kTiles * 16384 / 16; k += 256) reinterpret_cast<uint4*>(base)[k] = make_uint4(0, 0, 0, 0);
@@ -690,8 +637,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
   const uint32_t tw = tmem;  // data accumulator
   auto tdw = [&](int l) { return tmem + 64u + 64u * (uint32_t)l; };
   auto tdb = [&](int l) { return tmem + 64u + 64u * (uint32_t)(L + 1) + 16u * (uint32_t)l; };
-  const uint64_t ones8 = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
-  const uint64_t ones1 = tc::sdesc_sw128_sbo(tc::smem_addr(ones + 1024), 0);
+  const uint64_t ones1 = tc::sdesc_sw128_sbo(tc::smem_addr(ones), 0);
   const int total = coff[NT];
   int cur_tile = -1;
   bool failed = false, have_acc = false;
@@ -753,8 +699,8 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       __syncthreads();
     }
     if (new_w && tid == 0) {
-      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)lay.bwd_bytes);
-      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride, (uint32_t)lay.bwd_bytes, B.wbar);
+      tc::mbar_arrive_expect_tx(B.wbar, (uint32_t)wt_bytes);
+      tc::bulk_g2s(tc::smem_addr(Wsm), wimg + (size_t)cp.tile * img_stride + lay.t_off, (uint32_t)wt_bytes, B.wbar);
     }
     const bool first_of_tile = new_w;
     cur_tile = cp.tile;
@@ -772,7 +718,13 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       my_fr = __ldg(src + 1);
       my_cn = __ldg(reinterpret_cast<const int4*>(S.corners + (size_t)my_rec * 8) + part);
     }
-    gather_x<F, 8, 2>(S, vfeat, recs, cp.row0, cp.cnt, enc, PartTiles<2>{{Xt, MidA}}, warp, lane);
+    // the forward's hidden activations of this chunk (hi parts, swizzled tiles)
+    if (tid == 0) {
+      tc::mbar_arrive_expect_tx(hbar, (uint32_t)(L * 16384));
+      for (int l = 0; l < L; ++l)
+        tc::bulk_g2s(tc::smem_addr(Ht + l * 16384), htiles + ((size_t)c * L + l) * 16384, 16384u, hbar);
+    }
+    gather_x<F, 8, 1>(S, vfeat, recs, cp.row0, cp.cnt, enc, PartTiles<1>{{Xt}}, warp, lane);
     // output-gradient rows (3 values, BF16) of the DO tile; other columns stay 0
     if (part == 0)
       *reinterpret_cast<uint2*>(DOt + tc::sw128_offset(row, 0)) =
@@ -784,26 +736,13 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
       B.wphase ^= 1u;
       if (__syncthreads_or(!ok)) { failed = true; drain.set(B.wbar, B.wphase ^ 1u); break; }
     }
-    const uint32_t w = tc::smem_addr(Wsm);
-    // forward recomputation of the hidden activations H1..HL (two-part split
-    // operands; the mid parts alternate between MidA and MidB)
-    for (int l = 0; l < L; ++l) {
-      uint8_t* mid_in = (l & 1) ? MidB : MidA;
-      uint8_t* mid_out = (l & 1) ? MidA : MidB;
-      if (tid == 0) {
-        tc::fence_after_sync();
-        issue_split_layer(tw, tc::smem_addr(l == 0 ? Xt : Ht + (l - 1) * 16384), tc::smem_addr(mid_in),
-                          w + l * H * 128, w + lay.mid_off + l * H * 128, w + lay.bias_off + 32 * l, ones8, H,
-                          l == 0 ? 4 : H / 16);
-        tc::mma_commit(B.mbar);
-      }
-      if (!wait_mma(B, tid)) { failed = true; drain.set(B.mbar, B.mphase ^ 1u); break; }
-      epi_relu_split<H, 2>(taddr, Ht + l * 16384, l + 1 < L ? mid_out : nullptr, row, part);
-      tc::fence_proxy_async();
-      tc::fence_before_sync();
-      __syncthreads();
+    {
+      bool ok = tid == 0 ? tc::mbar_wait(hbar, hphase) : true;
+      hphase ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; drain.set(hbar, hphase ^ 1u); break; }
+      tc::fence_after_sync();
     }
-    if (failed) break;
+    const uint32_t w = tc::smem_addr(Wsm);
     // backward: layer L (output) down to 0.  delta of layer l's output is in
     // DO (l = L) or D; its input activation is HL..H1 or X.
     for (int l = L; l >= 0; --l) {
@@ -822,7 +761,7 @@ __global__ void __launch_bounds__(256, 1) tr_mlp_bwd_tc(SceneDev S, const float*
         for (int kk = 0; kk < 8; ++kk)
           tc::mma_f16(tdb(l), sdesc_mn(dlt + 2048 * kk, 16384), ones1, idb, (acc0 || kk > 0) ? 1u : 0u);
         // data gradient w.r.t. the layer input: delta x W_l^T (N = 64 inputs)
-        const uint32_t wt = w + (uint32_t)lay.t_off + 8192u * (uint32_t)l;
+        const uint32_t wt = w + 8192u * (uint32_t)l;
         const uint32_t idd = idesc_bf16(64, false, false);
         const int ksteps = l == L ? 1 : H / 16;
         for (int kk = 0; kk < ksteps; ++kk)
@@ -902,7 +841,8 @@ int train_tc_image_bytes(int H, int L) { return ImageLayout(H, L).total; }
 
 // dynamic shared memory of the backward kernel (checked against the 227 KB limit)
 int train_tc_bwd_smem_bytes(int H, int L) {
-  return 1024 + 16384 * (5 + L) + ((ImageLayout(H, L).bwd_bytes + 1023) & ~1023) + 2048 + 64;
+  const ImageLayout lay(H, L);
+  return 1024 + 16384 * (3 + L) + ((lay.bwd_bytes - lay.t_off + 1023) & ~1023) + 1024 + 64;
 }
 
 template <int F, int H, int L>
@@ -934,7 +874,8 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
     if (e != cudaSuccess) return e;
     const int32_t* uoff = ng == 1 ? a.coff : a.coff + S.num_tiles + 2;
     (ng == 1 ? tr_mlp_fwd_tc<F, H, L, 1> : tr_mlp_fwd_tc<F, H, L, 2>)<<<a.num_sms, 128 * ng, smem, st>>>(
-        S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, uoff, a.work, a.enc, a.wimg, a.img_stride, a.cout);
+        S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, uoff, a.coff, a.work, a.enc, a.wimg, a.img_stride, a.cout,
+        a.htiles);
   } else {
     const int smem = train_tc_bwd_smem_bytes(H, L);
     static unsigned long long cfg = 0;
@@ -946,7 +887,7 @@ cudaError_t launch_train_tc_t(const SceneDev& S, const TrainTcArgs& a, bool back
     if (e != cudaSuccess) return e;
     tr_mlp_bwd_tc<F, H, L><<<a.num_sms, 256, smem, st>>>(S, a.vfeat, (const TrainRecT*)a.recs, a.tstart, a.coff,
                                                          a.work, a.enc, a.wimg, a.img_stride, a.dout, a.gvfeat,
-                                                         a.gstage);
+                                                         a.gstage, a.htiles);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int64_t np = (int64_t)S.num_tiles * S.params_per_tile;
     apply_dw_kernel<<<(int)((np + 255) / 256 < 65536 ? (np + 255) / 256 : 65536), 256, 0, st>>>(
