@@ -1,6 +1,6 @@
 // Tensor-core (tcgen05, BF16 operands, FP32 accumulation) form of the
-// training MLP: forward colours and the backward pass with per-chunk
-// recomputation of the activations.
+// training MLP: forward colours, which also leave each hidden layer's
+// activations in global memory, and the backward pass over them.
 //
 // Samples are processed in chunks of 128 rows of one tile (chunk lists are
 // per tile).  Activation tiles are written by the epilogues in the 128-byte
